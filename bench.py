@@ -1,0 +1,309 @@
+#!/usr/bin/env python3
+"""Steady-state HEOM solves/s on GB300: the serial double-quantum-dot model (nd = 16,
+truncation tier 4: 30453 ADOs, 393812 stored entries) over a sweep of bias points,
+solved by the mixed-precision batched TFQMR (FP32x2 arithmetic, FP64 refinement) to
+||b - A x|| <= crit, with the plain FP64 GPU solve and the CPU restatement timed beside.
+
+One step = one batched solve of B bias points from the Boltzmann initial guess.
+`value` times device-resident solves; `e2e` times the same batch through the C ABI with
+host buffers (initial guesses and parameters in, steady states out).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "heom-quick2_gb300"))
+
+METRIC = "HEOM steady solves/s & matvec GB/s: mixed vs FP64 GPU at 1e-8 current err"
+WORKLOAD = "serial double quantum dot nd=16, tier L=4 (30453 ADOs, 393812 stored entries), Pade M=3, T=0.1, W=10"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=8, help="bias points per solve (per GPU)")
+    ap.add_argument("--crit", type=float, default=1e-8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiler run: warm-up solves, then one timed mixed solve; prints one short line")
+    return ap.parse_args()
+
+
+def bias_points(n):
+    """Bias sweep centred on V = 0.8 (meV): V_b uniformly spaced in [0.4, 1.2]."""
+    return [0.8] if n == 1 else [0.4 + 0.8 * b / (n - 1) for b in range(n)]
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local, dist
+
+
+def clocks_start():
+    path = os.path.join(tempfile.gettempdir(), f"heom_clocks_{os.getpid()}.csv")
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=f, stderr=subprocess.DEVNULL)
+        return p, f, path
+    except (OSError, FileNotFoundError):
+        return None, None, path
+
+
+def clocks_stop(h, gpu):
+    p, f, path = h
+    if p is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    p.terminate()
+    p.wait()
+    f.close()
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or parts[0] != str(gpu):
+            continue
+        try:
+            sm.append(float(parts[1]))
+            mx = float(parts[2])
+        except ValueError:
+            continue
+        for k, name in enumerate(names):
+            if parts[5 + k].lower() == "active":
+                reasons.add(name)
+    os.unlink(path)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "apply_fp32x2_dqd_L4_batch8.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def cpu_reference(cfgs, nthreads, crit):
+    """The oracle (C restatement of the reference FP64 path) on the host cores: one solve."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_ffi
+
+    m = oracle_ffi.Model(cfgs[0])
+    t0 = time.perf_counter()
+    rho, info = m.solve_tfqmr(crit=crit, maxit0=20000, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return dt, m.current(rho)[0].sum(), info
+
+
+def run_reference(args, ws, rank, dist):
+    import heomq.models as models
+
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    cfgs = [models.dqd(ntier=5, nmats=3, V=v) for v in bias_points(args.batch)]
+    for _ in range(args.warmup):
+        cpu_reference(cfgs[:1], nthreads, args.crit)
+    times = []
+    for k in range(args.steps):
+        dt, _, _ = cpu_reference([cfgs[k % len(cfgs)]], nthreads, args.crit)
+        times.append(dt)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "batch": 1, "crit": args.crit, "solver": "TFQMR FP64 (oracle restatement)"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                         "sample": "one full FP64 TFQMR solve of one bias point per step (OpenMP over ADOs)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, ws, rank, local, dist):
+    import numpy as np
+    import torch
+
+    import heomq
+
+    dev = local
+    torch.cuda.set_device(dev)
+    B = args.batch
+    Vs = bias_points(B)
+    cfg = heomq.models.dqd(ntier=5, nmats=3, V=0.8)
+    model = heomq.Model(cfg)
+    ctx = heomq.Context(model, device=dev, adjoint=False)
+    hb = 0.658211928
+    es = np.zeros((B, 2, 2))
+    for b, V in enumerate(Vs):   # eleadinfty(ialf, ispin) = +-V/2 / hbar, (nalf, nspin) column-major per instance
+        es[b] = np.array([[V / 2, V / 2], [-V / 2, -V / 2]]) / hb
+    es_cm = np.ascontiguousarray(np.transpose(es, (0, 2, 1)).reshape(B, 4))
+    batch = heomq.Batch(ctx, eshift_batch=es_cm, nbatch=B)
+    L = model.lunk
+    stride = batch.stride
+    x0h = model.initial_guess()
+    x0 = torch.zeros((B, stride), dtype=torch.complex128, device="cuda")
+    x0[:, :L] = torch.from_numpy(x0h).to("cuda")
+    x = torch.empty_like(x0)
+
+    def step(prec):
+        x.copy_(x0)
+        torch.cuda.synchronize()
+        return batch.solve_dev(x.data_ptr(), crit=args.crit, precision=prec)
+
+    for _ in range(args.warmup):
+        step(heomq.PREC_MIXED)
+    if args.profile:
+        info = step(heomq.PREC_MIXED)
+        print(json.dumps({"profile_run": True, "batch": B, "applies": info.iters, "seconds": info.seconds,
+                          "launches": info.launches}), flush=True)
+        batch.close()
+        ctx.close()
+        return 0
+    # FP64 GPU path beside (same batch, same criterion)
+    info64 = step(heomq.PREC_FP64)
+    cur64 = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
+
+    clk = clocks_start() if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev_s, launches = 0.0, 0
+    infos = []
+    for _ in range(args.steps):
+        info = step(heomq.PREC_MIXED)
+        dev_s += info.seconds
+        launches += info.launches
+        infos.append(info)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clocks = clocks_stop(clk, dev) if rank == 0 else None
+    curm = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
+    t_step = dev_s / args.steps
+    if dist:
+        t = torch.tensor([t_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = ws * B / t_step
+
+    # FP64 timing beside (one step, after the timed region)
+    t64 = info64.seconds
+    # end to end through the C ABI with host buffers
+    rhos = np.tile(x0h, (B, 1))
+    hs_b = None
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        out, info_e = ctx.solve_batch(rhos, hs_batch=hs_b, eshift_batch=es_cm, crit=args.crit,
+                                      precision=heomq.PREC_MIXED)
+        jt = [ctx.current(out[b])[0].sum() for b in range(B)]
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = ws * B / statistics.median(e2e_times)
+    h2d = B * L * 16 + B * 4 * 8 + B * model.nrho ** 2 * 16
+    d2h = B * L * 16
+
+    # roofline of the dominant kernel: the FP32x2 apply over the batch
+    sec, alg_bytes = ctx.bench_apply(heomq.PREC_MIXED, reps=20, nbatch=B)
+    sec64, alg64 = ctx.bench_apply(heomq.PREC_FP64, reps=10, nbatch=B)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / sec / 1e9
+    traffic = profile_traffic()
+    err = max(abs(a - b) / abs(b) for a, b in zip(curm, cur64))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        dt, jcpu, _ = cpu_reference([heomq.models.dqd(ntier=5, nmats=3, V=Vs[0])], nthreads, args.crit)
+        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": nthreads, "kind": "port",
+               "sample": f"one FP64 TFQMR solve of one bias point (V={Vs[0]:.2f}) by the C oracle, OpenMP over ADOs",
+               "current_rel_diff_vs_gpu_fp64": abs(jcpu - cur64[0]) / abs(cur64[0])}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32x2+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": B, "bias_points_meV": [round(v, 4) for v in Vs],
+                       "crit": args.crit, "solver": "TFQMR, FP32x2 arithmetic, FP64 residual refinement",
+                       "l2": f"inputs larger than L2: {B} x 9 solver vectors x {L * 16 / 1e6:.1f} MB",
+                       "parallelism": f"replicas x{ws}", "wall_s": wall,
+                       "applies_per_solve": infos[-1].iters, "refinements": infos[-1].refinements,
+                       "fp64": {"solves_per_s": ws * B / t64, "applies_per_solve": info64.iters,
+                                "apply_us": sec64 * 1e6, "apply_gbs_alg": alg64 / sec64 / 1e9},
+                       "speedup_mixed_vs_fp64": (ws * B / t_step) / (ws * B / t64),
+                       "current_rel_err_mixed_vs_fp64": err},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_apply<FP32x2> over the batch",
+                         "apply_us": sec * 1e6, "alg_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        return run_reference(args, ws, rank, dist)
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+
+    if rank == 0:
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+    return run_gb300(args, ws, rank, local, dist)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,119 @@
+// The sparse HEOM Liouvillian apply on GB300 (sm_103a), one thread per stored entry.
+//
+// Role: tfqmr_double/calc_ax_tfqmr_spa_omp.f90 (steady, with the Tr rho0 row),
+// td/calcderiv_spa_omp.f90 (time-dependent lead shifts, no trace row) and the
+// adjoint of the former.  Per output entry the thread accumulates
+//   g x  +  same-tier commutator terms of its pattern class  +  one or two signed
+//   gathers per coupled ADO (left and right operator products),
+// where every gather is a precomputed index into the source ADO's stored entries.
+// The higher-tier couplings have coefficients +-i and cost only additions; the
+// lower-tier ones multiply by the bath residues cb, cd.  In FP64 the kernel is
+// bounded by the FP64 pipe; in FP32 and FP32x2 by gather latency and bandwidth.
+#include "device.cuh"
+
+namespace heom {
+
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const typename Num<T>::V *__restrict__ x,
+                                               typename Num<T>::V *__restrict__ y, int64_t vstride,
+                                               const int *__restrict__ active)
+{
+    using N = Num<T>;
+    using A = typename N::A;
+    const int b = blockIdx.y;
+    if (active && !active[b]) return;
+    x += (int64_t)b * vstride;
+    y += (int64_t)b * vstride;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > P.lunk) return;
+    if (t == P.lunk) {   // the trace slot
+        A s = N::zero();
+        if (!ADJ && C.trace_on)
+            for (int k = 0; k < P.ntrace; k++) s = N::add(s, N::load(x[P.trace_idx[k]]));
+        y[t] = N::store(s);
+        return;
+    }
+    const int n = __ldg(P.ent_ado + t);
+    const int off = __ldg(P.ado_off + n);
+    const int p = (int)(t - off);
+    const int c = __ldg(P.ado_cls + n);
+    const typename N::V *hv = C.hval + (int64_t)b * P.nh;
+
+    // g = sum over the drawers of (cgamma + i dipm eshift)
+    const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
+    double es = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) es += (double)(int8_t)(cnt >> (8 * k)) * C.eshift[b * 4 + k];
+    A g = N::scale(N::load(C.g0[n]), C.g0_scale);
+    g = N::add(g, N::from_d(0.0, es));
+    if (ADJ) g = N::conj(g);
+    A acc = N::mul(g, N::load(x[t]));
+
+    // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
+    const int tb = __ldg(P.cls_tptr + c) + p;
+    const int k0 = __ldg(P.term_ptr + tb), k1 = __ldg(P.term_ptr + tb + 1);
+    A sl = N::zero(), sr = N::zero();   // sum H x over left terms and over right terms
+    for (int k = k0; k < k1; k++) {
+        const uint32_t w = __ldg(P.terms + k);
+        A h = N::load(hv[(w >> 16) & 0x7FFF]);
+        if (ADJ) h = N::conj(h);
+        const A xs = N::load(x[off + (int)(w & 0xFFFF)]);
+        const A hx = C.h_real ? N::scale(xs, N::re(h)) : N::mul(h, xs);
+        if (w >> 31) sr = N::add(sr, hx); else sl = N::add(sl, hx);
+    }
+    // forward: acc += i (sr - sl); adjoint: acc += -i (sr - sl)
+    A dlt = N::mul_i(N::sub(sr, sl));
+    acc = N::add(acc, ADJ ? N::neg(dlt) : dlt);
+
+    // couplings to the neighbouring tiers
+    const int e0 = __ldg(P.coup_ptr + n), e1 = __ldg(P.coup_ptr + n + 1);
+    A ua = N::zero();   // sum of unit-coefficient contributions (times -i at the end)
+    for (int e = e0; e < e1; e++) {
+        const int4 rec = __ldg(P.coup + e);
+        const uint32_t mw = __ldg(P.maps + rec.y + p);
+        if (!mw) continue;
+        const bool cj = rec.z < 0;
+        const uint32_t lo = mw & 0xFFFFu, hi = mw >> 16;
+        A vl = N::zero(), vr = N::zero();
+        if (lo) {
+            vl = N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            if (cj) vl = N::conj(vl);
+            if (lo & 0x8000u) vl = N::neg(vl);
+        }
+        if (hi) {
+            vr = N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            if (cj) vr = N::conj(vr);
+            if (hi & 0x8000u) vr = N::neg(vr);
+        }
+        if (rec.z & kCoefUnit) {
+            // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
+            if (C.unit_on) {
+                ua = N::add(ua, (rec.z & 1) ? N::neg(vl) : vl);
+                ua = N::add(ua, (rec.z & 2) ? N::neg(vr) : vr);
+            }
+        } else {
+            const int cid = rec.z & 0x3FFFFFFF;
+            if (lo) acc = N::add(acc, N::mul(N::load(C.cl[cid]), vl));
+            if (hi) acc = N::add(acc, N::mul(N::load(C.cr[cid]), vr));
+        }
+    }
+    acc = N::add(acc, N::mul_i(ua));
+    y[t] = N::store(acc);
+}
+
+template <typename T, bool ADJ>
+void launch_apply(const DevPlan &P, const DevCoef<T> &C, const typename Num<T>::V *x, typename Num<T>::V *y,
+                  int nbatch, int64_t vstride, const int *active, cudaStream_t s)
+{
+    dim3 grid((unsigned)((P.lunk + 1 + 255) / 256), (unsigned)nbatch);
+    k_apply<T, ADJ><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
+}
+
+template void launch_apply<double, false>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
+template void launch_apply<double, true>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
+template void launch_apply<float, false>(const DevPlan &, const DevCoef<float> &, const float2 *, float2 *, int, int64_t, const int *, cudaStream_t);
+template void launch_apply<float, true>(const DevPlan &, const DevCoef<float> &, const float2 *, float2 *, int, int64_t, const int *, cudaStream_t);
+template void launch_apply<DF, false>(const DevPlan &, const DevCoef<DF> &, const float4 *, float4 *, int, int64_t, const int *, cudaStream_t);
+template void launch_apply<DF, true>(const DevPlan &, const DevCoef<DF> &, const float4 *, float4 *, int, int64_t, const int *, cudaStream_t);
+
+}  // namespace heom

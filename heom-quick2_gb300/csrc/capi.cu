@@ -1,0 +1,764 @@
+// extern "C" entry points of the GB300 HEOM library (declared in include/heom_gb300.h).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "context.cuh"
+
+namespace heom {
+
+static thread_local std::string g_error;
+void set_error(const std::string &msg) { g_error = msg; }
+void fail(int code, const std::string &msg) { throw HeomError{code, msg}; }
+void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) fail(HEOM_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+static T *dalloc(std::vector<void *> &blocks, size_t n)
+{
+    T *p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc((void **)&p, sizeof(T) * n) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation failed");
+    blocks.push_back(p);
+    return p;
+}
+template <typename T>
+static T *upload_vec(std::vector<void *> &blocks, const std::vector<T> &v)
+{
+    T *p = dalloc<T>(blocks, v.size());
+    if (!v.empty()) CK(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return p;
+}
+
+void PlanDev::upload(const HostPlan &P)
+{
+    view = DevPlan();
+    view.lunk = P.lunk; view.nado = P.nado; view.nslots = P.nslots; view.nh = P.nh;
+    view.ntrace = (int32_t)P.trace_idx.size();
+    view.ent_ado = upload_vec(blocks, P.ent_ado);
+    view.ado_off = upload_vec(blocks, P.ado_off);
+    view.ado_cls = upload_vec(blocks, P.ado_cls);
+    view.ado_cnt = upload_vec(blocks, P.ado_cnt);
+    view.coup_ptr = upload_vec(blocks, P.coup_ptr);
+    view.cls_tptr = upload_vec(blocks, P.cls_tptr);
+    view.term_ptr = upload_vec(blocks, P.term_ptr);
+    view.trace_idx = upload_vec(blocks, P.trace_idx);
+    view.terms = upload_vec(blocks, P.terms);
+    view.maps = upload_vec(blocks, P.maps);
+    std::vector<int4> coup(P.coup.size());
+    for (size_t k = 0; k < coup.size(); k++) coup[k] = make_int4(P.coup[k].src_off, P.coup[k].map_base, P.coup[k].cid, 0);
+    view.coup = upload_vec(blocks, coup);
+    auto to64 = [](const std::vector<cd> &v) { std::vector<double2> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = make_double2(v[k].real(), v[k].imag()); return o; };
+    auto to32 = [](const std::vector<cd> &v) { std::vector<float2> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = make_float2((float)v[k].real(), (float)v[k].imag()); return o; };
+    g0_64 = upload_vec(blocks, to64(P.g0)); cl_64 = upload_vec(blocks, to64(P.cl)); cr_64 = upload_vec(blocks, to64(P.cr));
+    g0_32 = upload_vec(blocks, to32(P.g0)); cl_32 = upload_vec(blocks, to32(P.cl)); cr_32 = upload_vec(blocks, to32(P.cr));
+    auto todf = [](const std::vector<cd> &v) { std::vector<float4> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = Num<DF>::store(Num<DF>::from_d(v[k].real(), v[k].imag())); return o; };
+    g0_df = upload_vec(blocks, todf(P.g0)); cl_df = upload_vec(blocks, todf(P.cl)); cr_df = upload_vec(blocks, todf(P.cr));
+    ncoef = (int64_t)P.cl.size();
+}
+
+void PlanDev::release()
+{
+    for (void *p : blocks) cudaFree(p);
+    blocks.clear();
+}
+
+template <> DevCoef<double> PlanDev::coef<double>() const { DevCoef<double> c; c.g0 = g0_64; c.cl = cl_64; c.cr = cr_64; return c; }
+template <> DevCoef<float> PlanDev::coef<float>() const { DevCoef<float> c; c.g0 = g0_32; c.cl = cl_32; c.cr = cr_32; return c; }
+template <> DevCoef<DF> PlanDev::coef<DF>() const { DevCoef<DF> c; c.g0 = g0_df; c.cl = cl_df; c.cr = cr_df; return c; }
+
+}  // namespace heom
+
+using namespace heom;
+
+heom_ctx::~heom_ctx()
+{
+    dfwd.release();
+    dadj.release();
+    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch};
+    for (void *p : ptrs) if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+struct heom_batch {
+    heom_ctx *ctx = nullptr;
+    int nbatch = 0;
+    int64_t vs = 0;
+    double2 *h64 = nullptr;
+    float4 *hdf = nullptr;
+    double *e64 = nullptr;
+    int h_real = 0;
+    ~heom_batch() { if (h64) cudaFree(h64); if (hdf) cudaFree(hdf); if (e64) cudaFree(e64); }
+};
+
+namespace {
+
+// H values of the context's structure from a dense hs, in the three number types
+void hvalues(heom_ctx *c, const cd *hs, std::vector<double2> &h64, std::vector<float2> &h32, std::vector<float4> &hdf, int &real)
+{
+    size_t nh = c->hst.rows.size();
+    h64.resize(nh); h32.resize(nh); hdf.resize(nh);
+    real = 1;
+    for (size_t k = 0; k < nh; k++) {
+        cd v = hs[(size_t)c->hst.rows[k] + (size_t)c->hst.cols[k] * c->nrho];
+        h64[k] = make_double2(v.real(), v.imag());
+        h32[k] = make_float2((float)v.real(), (float)v.imag());
+        hdf[k] = Num<DF>::store(Num<DF>::from_d(v.real(), v.imag()));
+        if (v.imag() != 0.0) real = 0;
+    }
+}
+
+void set_params(heom_ctx *c, const std::vector<cd> &hs, const double *es)
+{
+    std::vector<double2> h64; std::vector<float2> h32; std::vector<float4> hdf;
+    hvalues(c, hs.data(), h64, h32, hdf, c->h_real);
+    CK(cudaMemcpyAsync(c->hval64, h64.data(), sizeof(double2) * h64.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->hval32, h32.data(), sizeof(float2) * h32.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->hvaldf, hdf.data(), sizeof(float4) * hdf.size(), cudaMemcpyHostToDevice, c->stream));
+    double e4[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++) e4[k] = es[k];
+    CK(cudaMemcpyAsync(c->es64, e4, sizeof e4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+}
+
+template <typename T> DevCoef<T> main_coef(heom_ctx *c, bool adj)
+{
+    DevCoef<T> k = (adj ? c->dadj : c->dfwd).template coef<T>();
+    k.eshift = c->es64;
+    k.h_real = c->h_real;
+    return k;
+}
+template <typename T> void set_hval(DevCoef<T> &k, heom_ctx *c);
+template <> void set_hval<double>(DevCoef<double> &k, heom_ctx *c) { k.hval = c->hval64; }
+template <> void set_hval<float>(DevCoef<float> &k, heom_ctx *c) { k.hval = c->hval32; }
+template <> void set_hval<DF>(DevCoef<DF> &k, heom_ctx *c) { k.hval = c->hvaldf; }
+template <typename T> DevCoef<T> ctx_coef(heom_ctx *c, bool adj)
+{
+    DevCoef<T> k = main_coef<T>(c, adj);
+    set_hval<T>(k, c);
+    return k;
+}
+
+void require_ctx(heom_ctx *c) { if (!c) fail(HEOM_E_ARG, "null context"); }
+
+// Hermitise the RDO part of a host rho: upper triangle defines the lower one and the
+// diagonal is made real (utility/zmat_herm_coo.f90 with uplo = 'u').
+void herm_rdo(heom_ctx *c, cd *rho)
+{
+    int n = c->nrho;
+    std::vector<cd> t((size_t)n * n, 0.0);
+    for (size_t q = 0; q < c->rdo_rows.size(); q++) {
+        int r = c->rdo_rows[q], cc = c->rdo_cols[q];
+        if (cc > r) { t[(r - 1) + (size_t)(cc - 1) * n] = rho[q]; t[(cc - 1) + (size_t)(r - 1) * n] = std::conj(rho[q]); }
+        if (cc == r) t[(r - 1) + (size_t)(cc - 1) * n] = rho[q].real();
+    }
+    for (size_t q = 0; q < c->rdo_rows.size(); q++) rho[q] = t[(c->rdo_rows[q] - 1) + (size_t)(c->rdo_cols[q] - 1) * n];
+}
+
+__global__ void k_add_real(double2 *p, double v) { p->x += v; }
+
+void drandn_stream(int64_t n, std::vector<double> &out)
+{
+    // tfqmr_double/drandn.f90 with SEED = 1: multiplicative congruential generator with
+    // multiplier 2^29 + 5 modulo 2^31 - 1 on 32-bit wrapping integers
+    out.resize(n);
+    int32_t im = (1 << 29) + 5, imax = 2147483647, is = 1;
+    for (int64_t i = 0; i < n; i++) {
+        out[i] = (double)is / (double)imax;
+        int32_t prod = (int32_t)((uint32_t)im * (uint32_t)is);
+        int32_t r = prod % imax;
+        is = r < 0 ? -r : r;
+    }
+}
+
+template <typename T>
+void upload_rt(heom_ctx *c, TfqWork<T> &W)
+{
+    using V = typename Num<T>::V;
+    std::vector<V> rt(W.N);
+    for (int64_t i = 0; i < W.N; i++) rt[i] = Num<T>::store(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
+    CK(cudaMemcpyAsync(W.rt, rt.data(), sizeof(V) * W.N, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+}
+
+// Run TFQMR iterations until every instance finished; graph-captured chunks of `chunk`
+// iterations, host polls the done flags between chunks.
+template <typename T>
+void tfq_run(heom_ctx *c, TfqWork<T> &W, const ApplyFn<T> &apply, int nlim, int &iters_out, int64_t &launches)
+{
+    const int chunk = 25;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < chunk; k++) tfq_iteration<T>(W, apply, c->stream);
+    CK(cudaStreamEndCapture(c->stream, &g));
+    CK(cudaGraphInstantiate(&ge, g, 0));
+    std::vector<int> act(W.nbatch);
+    int launched = 0;
+    while (true) {
+        CK(cudaGraphLaunch(ge, c->stream));
+        launched += chunk;
+        CK(cudaMemcpyAsync(act.data(), W.act_main, sizeof(int) * W.nbatch, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        bool any = false;
+        for (int a : act) any = any || a;
+        if (!any || launched > nlim + chunk) break;
+    }
+    cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    iters_out = launched;
+    launches += (int64_t)launched * 15;   // kernels of one tfq_iteration
+}
+
+template <typename T>
+ApplyFn<T> make_apply(heom_ctx *c, const DevCoef<T> &K, int nbatch, int64_t vstride, bool adj)
+{
+    const DevPlan P = adj ? c->dadj.view : c->dfwd.view;
+    cudaStream_t s = c->stream;
+    return [P, K, nbatch, vstride, s, adj](const typename Num<T>::V *x, typename Num<T>::V *y, const int *act) {
+        if (adj) launch_apply<T, true>(P, K, x, y, nbatch, vstride, act, s);
+        else launch_apply<T, false>(P, K, x, y, nbatch, vstride, act, s);
+    };
+}
+
+// y = e_trace - A x  (FP64, device)
+void residual64(heom_ctx *c, const DevCoef<double> &K, const double2 *x, double2 *r, int nbatch, int64_t vstride, bool adj,
+                const double2 *rhs = nullptr)
+{
+    const DevPlan &P = adj ? c->dadj.view : c->dfwd.view;
+    if (adj) launch_apply<double, true>(P, K, x, r, nbatch, vstride, nullptr, c->stream);
+    else launch_apply<double, false>(P, K, x, r, nbatch, vstride, nullptr, c->stream);
+    if (rhs) vec_axpby<double>(vstride * nbatch, r, -1.0, r, 1.0, rhs, c->stream);
+    else {
+        vec_axpby<double>(vstride * nbatch, r, -1.0, r, 0.0, r, c->stream);
+        for (int b = 0; b < nbatch; b++) k_add_real<<<1, 1, 0, c->stream>>>(r + (int64_t)b * vstride + c->lunk, 1.0);
+    }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------
+namespace heom {
+
+// Solve A x = rhs (rhs = e_trace when rhs == nullptr) for nbatch instances, in FP64 or
+// mixed precision.  x: device FP64, nbatch vectors with stride vstride (vstride >= lunk+1),
+// holding the initial guess on entry.
+void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, bool adj,
+                  const double2 *rhs, heom_solve_info &info, const DevCoef<double> &K64, const DevCoef<DF> &KDF)
+{
+    const int64_t N = c->lunk + 1;
+    int nlim = o.maxit0 / 2;
+    if (nlim < 1) nlim = 1;
+    info = heom_solve_info{};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    std::vector<void *> tmp;
+    double2 *r64 = nullptr;
+    CK(cudaMalloc((void **)&r64, sizeof(double2) * (size_t)vstride * nbatch));
+    tmp.push_back(r64);
+    int total_iters = 0, last_ierr = 0;
+    bool converged = false;
+    std::vector<double> norms(nbatch, 0.0);
+    int64_t aux = 0;   // launches outside the TFQMR graphs
+    auto batch_norms = [&](const double2 *v) {
+        for (int b = 0; b < nbatch; b++) norms[b] = device_norm2(N, v + (int64_t)b * vstride, c->dscratch, c->stream);
+        aux += nbatch;
+    };
+    auto residual = [&](const double2 *xx, double2 *r) {
+        residual64(c, K64, xx, r, nbatch, vstride, adj, rhs);
+        aux += rhs ? 2 : 2 + nbatch;
+    };
+    if (o.precision == HEOM_PREC_FP64) {
+        TfqWork<double> W;
+        tfq_alloc<double>(W, nbatch, N);
+        try {
+            upload_rt(c, W);
+            // b = rhs - A x0 per instance, stored with the workspace stride
+            residual(x, r64);
+            for (int b = 0; b < nbatch; b++)
+                CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, r64 + (int64_t)b * vstride, sizeof(double2) * N, cudaMemcpyDeviceToDevice, c->stream));
+            tfq_start<double>(W, o.crit * 1e-3, nlim, o.crit, c->stream);
+            aux++;
+            int it = 0;
+            tfq_run<double>(c, W, make_apply<double>(c, K64, nbatch, W.vstride, adj), nlim, it, info.launches);
+            total_iters = it;
+            for (int b = 0; b < nbatch; b++)
+                vec_axpby<double>(N, x + (int64_t)b * vstride, 1.0, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
+            std::vector<TfqState> st(nbatch);
+            CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
+            int axb = 0;
+            for (auto &s : st) { axb = std::max(axb, s.axb); last_ierr = s.ierr; }
+            total_iters = axb;
+        } catch (...) { tfq_free(W); for (void *p : tmp) cudaFree(p); throw; }
+        tfq_free(W);
+    } else {
+        // FP32x2 TFQMR on the FP64 residual, refined in FP64 until ||b - A x|| <= crit
+        TfqWork<DF> W;
+        tfq_alloc<DF>(W, nbatch, N);
+        try {
+            upload_rt(c, W);
+            int round = 0;
+            for (; round < std::max(1, o.max_refine); round++) {
+                residual(x, r64);
+                batch_norms(r64);
+                bool all_ok = true;
+                for (double v : norms) all_ok = all_ok && v <= o.crit;
+                if (all_ok) { converged = true; break; }
+                for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
+                    vec_from_d<DF>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride, norms[b] <= o.crit ? 0.0 : 1.0, c->stream);
+                tfq_start<DF>(W, o.crit * 1e-3, nlim, o.crit, c->stream);
+                aux += 1 + nbatch;
+                int it = 0;
+                tfq_run<DF>(c, W, make_apply<DF>(c, KDF, nbatch, W.vstride, adj), nlim, it, info.launches);
+                std::vector<TfqState> st(nbatch);
+                CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
+                int axb = 0;
+                for (auto &s : st) { axb = std::max(axb, s.axb); last_ierr = s.ierr; }
+                total_iters += axb;
+                for (int b = 0; b < nbatch; b++)
+                    if (norms[b] > o.crit) vec_axpy_to_d<DF>(N, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
+            }
+            info.refinements = round;
+        } catch (...) { tfq_free(W); for (void *p : tmp) cudaFree(p); throw; }
+        tfq_free(W);
+    }
+    // final FP64 residual
+    residual(x, r64);
+    batch_norms(r64);
+    double worst = 0;
+    for (double v : norms) worst = std::max(worst, v);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    for (void *p : tmp) cudaFree(p);
+    info.iters = total_iters;
+    info.ierr = last_ierr;
+    info.resid = worst;
+    info.converged = worst <= o.crit || converged;
+    info.seconds = ms * 1e-3;
+    info.launches += aux;
+}
+
+}  // namespace heom
+
+extern "C" {
+
+const char *heom_last_error(void) { return heom::g_error.c_str(); }
+
+int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **out)
+{
+    return guarded([&] {
+        if (!t || !out) fail(HEOM_E_ARG, "null argument");
+        *out = nullptr;
+        int dev = opts ? opts->device : 0;
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(HEOM_E_CUDA, "no CUDA device available");
+        CK(cudaSetDevice(dev));
+        std::unique_ptr<heom_ctx> c(new heom_ctx());
+        c->device = dev;
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->norbs = t->norbs; c->nspin = t->nspin; c->nalf = t->nalf; c->ncor = t->ncor; c->nrho = t->nrho; c->ntier = t->ntier;
+        c->lunk = t->lunk_spa; c->nunk = t->nunk;
+        std::vector<const double _Complex *> extra;
+        if (opts) for (auto *d : opts->dhs) if (d) extra.push_back(d);
+        c->hst = make_hstructure(*t, extra);
+        build_forward_plan(*t, c->hst, c->fwd);
+        c->dfwd.upload(c->fwd);
+        bool want_adj = !opts || opts->build_adjoint;
+        if (want_adj) {
+            build_adjoint_plan(*t, c->fwd, c->adj);
+            c->dadj.upload(c->adj);
+            c->has_adj = true;
+        }
+        size_t nh = c->hst.rows.size();
+        CK(cudaMalloc((void **)&c->hval64, sizeof(double2) * nh));
+        CK(cudaMalloc((void **)&c->hval32, sizeof(float2) * nh));
+        CK(cudaMalloc((void **)&c->hvaldf, sizeof(float4) * nh));
+        CK(cudaMalloc((void **)&c->es64, sizeof(double) * 4));
+        const cd *hs = reinterpret_cast<const cd *>(t->hs);
+        c->hs_host.assign(hs, hs + (size_t)c->nrho * c->nrho);
+        if (opts) for (auto *d : opts->dhs) if (d) c->dhs_host.emplace_back(reinterpret_cast<const cd *>(d), reinterpret_cast<const cd *>(d) + (size_t)c->nrho * c->nrho);
+        for (int a = 0; a < t->nalf; a++)
+            for (int s = 0; s < t->nspin; s++) {
+                int slot = a + s * t->nalf;
+                c->eleadinfty[slot] = t->eleadinfty[a + (size_t)s * t->nalf];
+                c->amps[slot] = opts && opts->amps ? opts->amps[a + (size_t)s * t->nalf] : c->eleadinfty[slot];
+                c->tchar[slot] = opts && opts->tchar ? opts->tchar[a + (size_t)s * t->nalf] : 0.0;
+            }
+        set_params(c.get(), c->hs_host, c->eleadinfty);
+        // observables
+        int nz0 = t->nnz_spa[0];
+        c->rdo_rows.assign(t->irow_spa, t->irow_spa + nz0);
+        c->rdo_cols.assign(t->icol_spa, t->icol_spa + nz0);
+        const int n = t->nrho;
+        for (int s = 1; s <= t->nspin; s++)
+            for (int o = 1; o <= t->norbs; o++) {
+                size_t base = (size_t)t->nams * ((o - 1) + (size_t)(s - 1) * t->norbs);
+                std::vector<int> cofr(n + 1, 0), sg(n + 1, 0);
+                for (int k = 0; k < t->nams; k++) { cofr[t->rowams[base + k]] = t->colams[base + k]; sg[t->rowams[base + k]] = t->sgnams[base + k] ? -1 : 1; }
+                // occupation: n_ms = a^+ a is diagonal with ones on the columns holding an element
+                std::vector<char> occupied(n + 1, 0);
+                for (int k = 0; k < t->nams; k++) occupied[t->colams[base + k]] = 1;
+                for (int q = 0; q < nz0; q++)
+                    if (t->irow_spa[q] == t->icol_spa[q] && occupied[t->irow_spa[q]]) { c->occ_entry.push_back(q); c->occ_slot.push_back((o - 1) + (s - 1) * t->norbs); }
+                // current: tr(a_{ms} rho+) over the first-tier ADOs of every lead and memory component
+                for (int al = 1; al <= t->nalf; al++)
+                    for (int k = 1; k <= t->ncor; k++) {
+                        int iopr = ((s - 1) * t->norbs + o - 1) * t->nalf + al;
+                        int d = (iopr - 1) * t->ncor + k;
+                        int64_t u = t->nfirst[1] - 1 + t->indexdraw[d - 1];
+                        int64_t st = t->ind_spa[u - 1] - 1;
+                        for (int q = 0; q < t->nnz_spa[u - 1]; q++) {
+                            int r = t->irow_spa[st + q], cc = t->icol_spa[st + q];
+                            if (cofr[cc] == r) c->cur_terms.push_back(CurrentTerm{(int32_t)(st + q), (al - 1) + (s - 1) * t->nalf, (float)sg[cc]});
+                        }
+                    }
+            }
+        c->n_cur_terms = (int32_t)c->cur_terms.size();
+        CK(cudaMalloc((void **)&c->d_cur_terms, sizeof(CurrentTerm) * std::max<size_t>(1, c->cur_terms.size())));
+        if (!c->cur_terms.empty()) CK(cudaMemcpy(c->d_cur_terms, c->cur_terms.data(), sizeof(CurrentTerm) * c->cur_terms.size(), cudaMemcpyHostToDevice));
+        int64_t N = c->lunk + 1;
+        CK(cudaMalloc((void **)&c->dx, sizeof(double2) * N));
+        CK(cudaMalloc((void **)&c->dy, sizeof(double2) * N));
+        CK(cudaMalloc((void **)&c->dz, sizeof(double2) * N));
+        CK(cudaMalloc((void **)&c->fx, sizeof(float2) * N));
+        CK(cudaMalloc((void **)&c->fy, sizeof(float2) * N));
+        CK(cudaMalloc((void **)&c->dscratch, sizeof(double) * 2048));
+        drandn_stream(2 * N, c->rt_host);
+        CK(cudaDeviceSynchronize());
+        *out = c.release();
+    });
+}
+
+void heom_ctx_destroy(heom_ctx *ctx) { delete ctx; }
+
+int64_t heom_ctx_lunk(const heom_ctx *ctx) { return ctx ? ctx->lunk : -1; }
+
+int heom_calc_ax(heom_ctx *c, int64_t ldim, const double _Complex *x, double _Complex *y)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (ldim != c->lunk) fail(HEOM_E_ARG, "ldim does not match lunk_spa");
+        if (!x || !y) fail(HEOM_E_ARG, "null vector");
+        int64_t N = c->lunk + 1;
+        CK(cudaMemcpyAsync(c->dx, x, sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
+        launch_apply<double, false>(c->dfwd.view, ctx_coef<double>(c, false), c->dx, c->dy, 1, N, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(y, c->dy, sizeof(double2) * N, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int heom_calc_ax_dev(heom_ctx *c, const void *dx, void *dy)
+{
+    return guarded([&] {
+        require_ctx(c);
+        launch_apply<double, false>(c->dfwd.view, ctx_coef<double>(c, false), (const double2 *)dx, (double2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int heom_calc_ax_fp32_dev(heom_ctx *c, const void *dx, void *dy)
+{
+    return guarded([&] {
+        require_ctx(c);
+        launch_apply<float, false>(c->dfwd.view, ctx_coef<float>(c, false), (const float2 *)dx, (float2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int heom_calc_atrx(heom_ctx *c, int64_t ldim, const double _Complex *x, double _Complex *y)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!c->has_adj) fail(HEOM_E_ARG, "context built without the adjoint plan");
+        if (ldim != c->lunk) fail(HEOM_E_ARG, "ldim does not match lunk_spa");
+        int64_t N = c->lunk + 1;
+        CK(cudaMemcpyAsync(c->dx, x, sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
+        launch_apply<double, true>(c->dadj.view, ctx_coef<double>(c, true), c->dx, c->dy, 1, N, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(y, c->dy, sizeof(double2) * N, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int heom_calc_atrx_dev(heom_ctx *c, const void *dx, void *dy)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!c->has_adj) fail(HEOM_E_ARG, "context built without the adjoint plan");
+        launch_apply<double, true>(c->dadj.view, ctx_coef<double>(c, true), (const double2 *)dx, (double2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    });
+}
+
+int heom_calcderiv(heom_ctx *c, double t, const double _Complex *x, double _Complex *y)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!x || !y) fail(HEOM_E_ARG, "null vector");
+        double es[4];
+        for (int k = 0; k < 4; k++) {
+            double tc = c->tchar[k];
+            es[k] = tc > 0 ? c->amps[k] * (1.0 - std::exp(-t / tc)) : (t > 0 ? c->amps[k] : 0.0);
+        }
+        set_params(c, c->hs_host, es);
+        int64_t N = c->lunk + 1;
+        CK(cudaMemsetAsync(c->dx, 0, sizeof(double2) * N, c->stream));
+        CK(cudaMemcpyAsync(c->dx, x, sizeof(double2) * c->lunk, cudaMemcpyHostToDevice, c->stream));
+        DevCoef<double> K = ctx_coef<double>(c, false);
+        K.trace_on = 0;
+        launch_apply<double, false>(c->dfwd.view, K, c->dx, c->dy, 1, N, nullptr, c->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(y, c->dy, sizeof(double2) * c->lunk, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        set_params(c, c->hs_host, c->eleadinfty);
+    });
+}
+
+int heom_solve_tfqmr(heom_ctx *c, const heom_solve_opts *o, double _Complex *rho, heom_solve_info *info)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!o || !rho) fail(HEOM_E_ARG, "null argument");
+        int64_t N = c->lunk + 1;
+        std::vector<cd> x(N, 0.0);
+        std::memcpy(x.data(), rho, sizeof(cd) * c->lunk);
+        herm_rdo(c, x.data());
+        CK(cudaMemcpyAsync(c->dz, x.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
+        heom_solve_info inf;
+        solve_device(c, *o, c->dz, 1, N, false, nullptr, inf, ctx_coef<double>(c, false), ctx_coef<DF>(c, false));
+        CK(cudaMemcpyAsync(rho, c->dz, sizeof(double2) * c->lunk, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (info) *info = inf;
+        if (!inf.converged) fail(inf.ierr == 8 ? HEOM_E_BREAKDOWN : HEOM_E_NOCONV, "TFQMR did not reach crit");
+    });
+}
+
+int heom_current(heom_ctx *c, const double _Complex *rho, double *jt)
+{
+    return guarded([&] {
+        require_ctx(c);
+        const cd *r = reinterpret_cast<const cd *>(rho);
+        int ns = c->nalf * c->nspin;
+        for (int k = 0; k < ns; k++) jt[k] = 0;
+        std::vector<cd> acc(ns, 0.0);
+        for (auto &tm : c->cur_terms) acc[tm.slot] += (double)tm.sign * r[tm.entry];
+        for (int k = 0; k < ns; k++) jt[k] = -2.0 * acc[k].imag() * kJconst;
+    });
+}
+
+int heom_occupation(heom_ctx *c, const double _Complex *rho, double *occ)
+{
+    return guarded([&] {
+        require_ctx(c);
+        const cd *r = reinterpret_cast<const cd *>(rho);
+        for (int k = 0; k < c->norbs * c->nspin; k++) occ[k] = 0;
+        for (size_t k = 0; k < c->occ_entry.size(); k++) occ[c->occ_slot[k]] += r[c->occ_entry[k]].real();
+    });
+}
+
+int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batch, const double *eshift_batch,
+                      heom_batch **out)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (nbatch < 1 || !out) fail(HEOM_E_ARG, "bad batch arguments");
+        *out = nullptr;
+        std::unique_ptr<heom_batch> B(new heom_batch());
+        B->ctx = c;
+        B->nbatch = nbatch;
+        int64_t N = c->lunk + 1;
+        B->vs = (N + 63) / 64 * 64;
+        size_t nh = c->hst.rows.size();
+        std::vector<double2> h64(nh * nbatch);
+        std::vector<float4> hdf(nh * nbatch);
+        std::vector<double> e64(4 * (size_t)nbatch, 0.0);
+        int all_real = 1;
+        for (int b = 0; b < nbatch; b++) {
+            const cd *hs = hs_batch ? reinterpret_cast<const cd *>(hs_batch) + (size_t)b * c->nrho * c->nrho : c->hs_host.data();
+            std::vector<double2> a64; std::vector<float2> a32; std::vector<float4> adf; int real;
+            hvalues(c, hs, a64, a32, adf, real);
+            all_real = all_real && real;
+            std::copy(a64.begin(), a64.end(), h64.begin() + b * nh);
+            std::copy(adf.begin(), adf.end(), hdf.begin() + b * nh);
+            for (int a = 0; a < c->nalf; a++)
+                for (int s = 0; s < c->nspin; s++) {
+                    int slot = a + s * c->nalf;
+                    e64[4 * b + slot] = eshift_batch ? eshift_batch[(size_t)b * c->nalf * c->nspin + a + (size_t)s * c->nalf] : c->eleadinfty[slot];
+                }
+        }
+        CK(cudaMalloc((void **)&B->h64, sizeof(double2) * h64.size()));
+        CK(cudaMalloc((void **)&B->hdf, sizeof(float4) * hdf.size()));
+        CK(cudaMalloc((void **)&B->e64, sizeof(double) * e64.size()));
+        CK(cudaMemcpy(B->h64, h64.data(), sizeof(double2) * h64.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(B->hdf, hdf.data(), sizeof(float4) * hdf.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(B->e64, e64.data(), sizeof(double) * e64.size(), cudaMemcpyHostToDevice));
+        B->h_real = all_real;
+        *out = B.release();
+    });
+}
+
+int64_t heom_batch_stride(const heom_batch *b) { return b ? b->vs : -1; }
+
+void heom_batch_destroy(heom_batch *b) { delete b; }
+
+int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, heom_solve_info *info)
+{
+    return guarded([&] {
+        if (!B || !o || !x_dev) fail(HEOM_E_ARG, "null argument");
+        heom_ctx *c = B->ctx;
+        DevCoef<double> K64 = c->dfwd.coef<double>(); K64.hval = B->h64; K64.eshift = B->e64; K64.h_real = B->h_real;
+        DevCoef<DF> KDF = c->dfwd.coef<DF>(); KDF.hval = B->hdf; KDF.eshift = B->e64; KDF.h_real = B->h_real;
+        heom_solve_info inf;
+        solve_device(c, *o, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, K64, KDF);
+        if (info) *info = inf;
+        if (!inf.converged) fail(HEOM_E_NOCONV, "batched TFQMR did not reach crit");
+    });
+}
+
+int heom_solve_batch(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batch, const double *eshift_batch,
+                     const heom_solve_opts *o, double _Complex *rho_batch, heom_solve_info *info)
+{
+    heom_batch *B = nullptr;
+    int rc = heom_batch_create(c, nbatch, hs_batch, eshift_batch, &B);
+    if (rc) return rc;
+    void *dxb = nullptr;
+    rc = guarded([&] {
+        if (!o || !rho_batch) fail(HEOM_E_ARG, "null argument");
+        int64_t N = c->lunk + 1, vs = B->vs;
+        CK(cudaMalloc(&dxb, sizeof(double2) * (size_t)vs * nbatch));
+        CK(cudaMemsetAsync(dxb, 0, sizeof(double2) * (size_t)vs * nbatch, c->stream));
+        std::vector<cd> x((size_t)vs * nbatch, 0.0);
+        for (int b = 0; b < nbatch; b++) {
+            cd *xb = x.data() + (size_t)b * vs;
+            std::memcpy(xb, reinterpret_cast<cd *>(rho_batch) + (size_t)b * c->lunk, sizeof(cd) * c->lunk);
+            herm_rdo(c, xb);
+        }
+        CK(cudaMemcpyAsync(dxb, x.data(), sizeof(double2) * x.size(), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        (void)N;
+    });
+    if (rc == 0) rc = heom_batch_solve_dev(B, o, dxb, info);
+    if (rc == 0 || rc == HEOM_E_NOCONV) {
+        int rc2 = guarded([&] {
+            std::vector<cd> x((size_t)B->vs * nbatch);
+            CK(cudaMemcpyAsync(x.data(), dxb, sizeof(double2) * x.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            for (int b = 0; b < nbatch; b++)
+                std::memcpy(reinterpret_cast<cd *>(rho_batch) + (size_t)b * c->lunk, x.data() + (size_t)b * B->vs, sizeof(cd) * c->lunk);
+        });
+        if (rc == 0) rc = rc2;
+    }
+    if (dxb) cudaFree(dxb);
+    heom_batch_destroy(B);
+    return rc;
+}
+
+int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (reps < 1) reps = 1;
+        if (nbatch < 1) nbatch = 1;
+        int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64;
+        size_t nh = c->hst.rows.size();
+        std::vector<void *> blocks;
+        auto cleanup = [&] { for (void *p : blocks) cudaFree(p); };
+        try {
+            void *xin = nullptr, *yout = nullptr, *hv = nullptr;
+            double *es = nullptr;
+            CK(cudaMalloc(&xin, 16 * (size_t)vs * nbatch)); blocks.push_back(xin);
+            CK(cudaMalloc(&yout, 16 * (size_t)vs * nbatch)); blocks.push_back(yout);
+            CK(cudaMalloc(&hv, 16 * nh * nbatch)); blocks.push_back(hv);
+            CK(cudaMalloc((void **)&es, sizeof(double) * 4 * nbatch)); blocks.push_back(es);
+            CK(cudaMemsetAsync(xin, 0, 16 * (size_t)vs * nbatch, c->stream));
+            std::vector<double> e(4 * (size_t)nbatch);
+            for (int b = 0; b < nbatch; b++) for (int k = 0; k < 4; k++) e[4 * b + k] = c->eleadinfty[k];
+            CK(cudaMemcpyAsync(es, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice, c->stream));
+            std::vector<double2> h64; std::vector<float2> h32; std::vector<float4> hdf; int real;
+            hvalues(c, c->hs_host.data(), h64, h32, hdf, real);
+            for (int b = 0; b < nbatch; b++) {
+                if (precision == HEOM_PREC_FP64) CK(cudaMemcpyAsync((double2 *)hv + b * nh, h64.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
+                else if (precision == HEOM_PREC_MIXED) CK(cudaMemcpyAsync((float4 *)hv + b * nh, hdf.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
+                else CK(cudaMemcpyAsync((float2 *)hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
+            }
+            CK(cudaStreamSynchronize(c->stream));
+            // precision: 0 FP64, 1 FP32x2 (the mixed solver's apply), 2 plain FP32
+            auto run = [&] {
+                if (precision == HEOM_PREC_FP64) {
+                    DevCoef<double> K = main_coef<double>(c, false); K.hval = (double2 *)hv; K.eshift = es;
+                    launch_apply<double, false>(c->dfwd.view, K, (double2 *)xin, (double2 *)yout, nbatch, vs, nullptr, c->stream);
+                } else if (precision == HEOM_PREC_MIXED) {
+                    DevCoef<DF> K = main_coef<DF>(c, false); K.hval = (float4 *)hv; K.eshift = es;
+                    launch_apply<DF, false>(c->dfwd.view, K, (float4 *)xin, (float4 *)yout, nbatch, vs, nullptr, c->stream);
+                } else {
+                    DevCoef<float> K = main_coef<float>(c, false); K.hval = (float2 *)hv; K.eshift = es;
+                    launch_apply<float, false>(c->dfwd.view, K, (float2 *)xin, (float2 *)yout, nbatch, vs, nullptr, c->stream);
+                }
+            };
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+            for (int w = 0; w < 3; w++) run();
+            CK(cudaEventRecord(e0, c->stream));
+            for (int r = 0; r < reps; r++) run();
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaGetLastError());
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            if (seconds) *seconds = ms * 1e-3 / reps;
+            double st[9];
+            heom_ctx_stats(c, st);
+            double s = precision == 2 ? 8.0 : 16.0;
+            // algorithmic bytes of one launch: x read once, y written once per instance, plus the plan
+            if (bytes) *bytes = nbatch * 2.0 * (double)N * s + st[8];
+            cleanup();
+        } catch (...) { cleanup(); throw; }
+    });
+}
+
+int heom_ctx_stats(const heom_ctx *c, double *out)
+{
+    return guarded([&] {
+        if (!c || !out) fail(HEOM_E_ARG, "null argument");
+        const HostPlan &P = c->fwd;
+        double lower = 0;
+        for (int32_t a = 0; a < P.nado; a++) {
+            int nz = P.ado_off[a + 1] - P.ado_off[a];
+            for (int e = P.coup_ptr[a]; e < P.coup_ptr[a + 1]; e++) {
+                if (P.coup[e].cid & kCoefUnit) continue;
+                for (int p = 0; p < nz; p++) {
+                    uint32_t w = P.maps[P.coup[e].map_base + p];
+                    lower += ((w & 0xFFFFu) != 0) + ((w >> 16) != 0);
+                }
+            }
+        }
+        out[0] = (double)(P.lunk + 1);
+        out[1] = P.nado;
+        out[2] = (double)P.n_classes;
+        out[3] = (double)P.n_couplings;
+        out[4] = (double)P.n_maps;
+        out[5] = P.gather_hits;
+        out[6] = (double)P.n_terms_same;
+        out[7] = lower;
+        // plan bytes read per apply: coupling records (16 B) + one map word per record and
+        // output entry (4 B) + per-entry ADO index (4 B) + per-ADO arrays (g0 16 B + 4 ints)
+        double mapwords = 0;
+        for (int32_t a = 0; a < P.nado; a++)
+            mapwords += (double)(P.coup_ptr[a + 1] - P.coup_ptr[a]) * (P.ado_off[a + 1] - P.ado_off[a]);
+        out[8] = (double)P.n_couplings * 16.0 + mapwords * 4.0 + (double)P.lunk * 4.0 + (double)P.nado * 32.0;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// The opaque heom_ctx: device plans, coefficient sets and work buffers of one model.
+#pragma once
+#include <memory>
+
+#include "solver.cuh"
+
+namespace heom {
+
+void cuda_check(cudaError_t e, const char *what);
+#define CK(call) ::heom::cuda_check((call), #call)
+
+// Device copy of one HostPlan plus its coefficient tables in both precisions.
+struct PlanDev {
+    DevPlan view;
+    std::vector<void *> blocks;
+    double2 *g0_64 = nullptr, *cl_64 = nullptr, *cr_64 = nullptr;
+    float2 *g0_32 = nullptr, *cl_32 = nullptr, *cr_32 = nullptr;
+    float4 *g0_df = nullptr, *cl_df = nullptr, *cr_df = nullptr;
+    int64_t ncoef = 0;
+    void upload(const HostPlan &P);
+    void release();
+    template <typename R> DevCoef<R> coef() const;
+};
+
+// Extra per-entry data used by observables.
+struct CurrentTerm {
+    int32_t entry;   // global entry of a first-tier + ADO
+    int32_t slot;    // ialf-1 + (ispin-1)*nalf
+    float sign;      // sign of the a_{ms} element
+};
+
+}  // namespace heom
+
+struct heom_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int norbs = 0, nspin = 0, nalf = 0, ncor = 0, nrho = 0, ntier = 0;
+    int64_t lunk = 0, nunk = 0;
+    heom::HStructure hst;
+    heom::HostPlan fwd, adj;
+    heom::PlanDev dfwd, dadj;
+    bool has_adj = false;
+    // parameter sets: H structure values (nh) in both precisions
+    double2 *hval64 = nullptr;
+    float2 *hval32 = nullptr;
+    float4 *hvaldf = nullptr;
+    double *es64 = nullptr;   // 4 lead-shift slots
+    int h_real = 0;
+    double eleadinfty[4] = {0, 0, 0, 0};
+    double amps[4] = {0, 0, 0, 0}, tchar[4] = {0, 0, 0, 0};
+    std::vector<heom::cd> hs_host;
+    std::vector<std::vector<heom::cd>> dhs_host;   // optional parameter derivatives of hs
+    // host copies for observables
+    std::vector<heom::CurrentTerm> cur_terms;
+    std::vector<int32_t> occ_entry, occ_slot;       // RDO diagonal entries contributing to occ(m,s)
+    std::vector<int32_t> rdo_rows, rdo_cols;        // RDO pattern (1-based)
+    heom::CurrentTerm *d_cur_terms = nullptr;
+    int32_t n_cur_terms = 0;
+    // scratch vectors (lunk + 1 complex)
+    double2 *dx = nullptr, *dy = nullptr, *dz = nullptr;
+    float2 *fx = nullptr, *fy = nullptr;
+    double *dscratch = nullptr;
+    std::vector<double> rt_host;                    // drandn stream (2*(lunk+1) reals)
+    ~heom_ctx();
+};

@@ -1,0 +1,118 @@
+// Number types of the device kernels: FP64 (double2), FP32 (float2) and FP32x2
+// (pairs of FP32 numbers, float4 = re_hi, im_hi, re_lo, im_lo).
+//
+// FP32x2 arithmetic uses error-free transformations: the two-sum of Knuth (TAOCP
+// vol. 2, 4.2.2) and the FMA-based exact product (p = a*b, e = fma(a, b, -p)),
+// combined as in Dekker (Numer. Math. 18 (1971) 224) "double-length" arithmetic.
+// A value is hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits; all
+// operations run on the FP32 pipe.  The intrinsics __fadd_rn/__fmul_rn keep the
+// compiler from contracting or reassociating the compensation terms.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace heom {
+
+struct DF {};   // tag of the FP32x2 number type
+
+template <typename T> struct Num;
+
+template <> struct Num<double> {
+    using V = double2;      // stored complex
+    using A = double2;      // accumulator / arithmetic complex
+    using S = double;       // real scalar used in arithmetic
+    static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
+    static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
+    static __host__ __device__ __forceinline__ A zero() { return make_double2(0, 0); }
+    static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_double2(re, im); }
+    static __device__ __forceinline__ A add(A a, A b) { return make_double2(a.x + b.x, a.y + b.y); }
+    static __device__ __forceinline__ A sub(A a, A b) { return make_double2(a.x - b.x, a.y - b.y); }
+    static __device__ __forceinline__ A mul(A a, A b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+    // a * (r real)
+    static __device__ __forceinline__ A scale(A a, double r) { return make_double2(a.x * r, a.y * r); }
+    // i * a
+    static __device__ __forceinline__ A mul_i(A a) { return make_double2(-a.y, a.x); }
+    static __device__ __forceinline__ A neg(A a) { return make_double2(-a.x, -a.y); }
+    static __device__ __forceinline__ A conj(A a) { return make_double2(a.x, -a.y); }
+    static __device__ __forceinline__ double re(A a) { return a.x; }
+    static __device__ __forceinline__ double im(A a) { return a.y; }
+};
+
+template <> struct Num<float> {
+    using V = float2;
+    using A = float2;
+    using S = float;
+    static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
+    static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
+    static __host__ __device__ __forceinline__ A zero() { return make_float2(0, 0); }
+    static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_float2((float)re, (float)im); }
+    static __device__ __forceinline__ A add(A a, A b) { return make_float2(a.x + b.x, a.y + b.y); }
+    static __device__ __forceinline__ A sub(A a, A b) { return make_float2(a.x - b.x, a.y - b.y); }
+    static __device__ __forceinline__ A mul(A a, A b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+    static __device__ __forceinline__ A scale(A a, double r) { float f = (float)r; return make_float2(a.x * f, a.y * f); }
+    static __device__ __forceinline__ A mul_i(A a) { return make_float2(-a.y, a.x); }
+    static __device__ __forceinline__ A neg(A a) { return make_float2(-a.x, -a.y); }
+    static __device__ __forceinline__ A conj(A a) { return make_float2(a.x, -a.y); }
+    static __device__ __forceinline__ double re(A a) { return a.x; }
+    static __device__ __forceinline__ double im(A a) { return a.y; }
+};
+
+// ---- FP32x2 ----
+struct f2r { float hi, lo; };   // real FP32x2
+struct f2c { f2r re, im; };     // complex FP32x2
+
+__host__ __device__ __forceinline__ f2r f2r_from_d(double d)
+{
+    float h = (float)d;
+    return {h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ f2r two_sum(float a, float b)
+{
+    float s = __fadd_rn(a, b);
+    float v = __fadd_rn(s, -a);
+    float e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -v)), __fadd_rn(b, -v));
+    return {s, e};
+}
+__device__ __forceinline__ f2r fast_two_sum(float a, float b)
+{
+    float s = __fadd_rn(a, b);
+    return {s, __fadd_rn(b, -__fadd_rn(s, -a))};
+}
+__device__ __forceinline__ f2r f2r_add(f2r a, f2r b)
+{
+    f2r s = two_sum(a.hi, b.hi);
+    float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ f2r f2r_neg(f2r a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ f2r f2r_mul(f2r a, f2r b)
+{
+    float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+
+template <> struct Num<DF> {
+    using V = float4;    // (re_hi, im_hi, re_lo, im_lo)
+    using A = f2c;
+    using S = f2r;
+    static __host__ __device__ __forceinline__ A load(const V &v) { return {{v.x, v.z}, {v.y, v.w}}; }
+    static __host__ __device__ __forceinline__ V store(const A &a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+    static __host__ __device__ __forceinline__ A zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+    static __host__ __device__ __forceinline__ A from_d(double re, double im) { return {f2r_from_d(re), f2r_from_d(im)}; }
+    static __device__ __forceinline__ A add(A a, A b) { return {f2r_add(a.re, b.re), f2r_add(a.im, b.im)}; }
+    static __device__ __forceinline__ A sub(A a, A b) { return {f2r_add(a.re, f2r_neg(b.re)), f2r_add(a.im, f2r_neg(b.im))}; }
+    static __device__ __forceinline__ A mul(A a, A b)
+    {
+        return {f2r_add(f2r_mul(a.re, b.re), f2r_neg(f2r_mul(a.im, b.im))), f2r_add(f2r_mul(a.re, b.im), f2r_mul(a.im, b.re))};
+    }
+    static __device__ __forceinline__ A scale(A a, double r) { f2r f = f2r_from_d(r); return {f2r_mul(a.re, f), f2r_mul(a.im, f)}; }
+    static __device__ __forceinline__ A mul_i(A a) { return {f2r_neg(a.im), a.re}; }
+    static __device__ __forceinline__ A neg(A a) { return {f2r_neg(a.re), f2r_neg(a.im)}; }
+    static __device__ __forceinline__ A conj(A a) { return {a.re, f2r_neg(a.im)}; }
+    static __device__ __forceinline__ double re(A a) { return (double)a.re.hi + (double)a.re.lo; }
+    static __device__ __forceinline__ double im(A a) { return (double)a.im.hi + (double)a.im.lo; }
+};
+
+}  // namespace heom

@@ -1,0 +1,400 @@
+"""heomq -- Python host interface of the GB300 HEOM library (ctypes over the C ABI).
+
+Mirrors the reference's sparse-path routines:
+  Context.calc_ax_tfqmr_spa(x)   <- calc_ax_tfqmr_spa_omp(ldim, rcgtmp, rcgrhs)
+  Context.calcderiv_spa(t, x)    <- calcderiv_spa_omp(tt)
+  Context.calc_atrx(x)           <- calc_atrx_bicg_omp (adjoint, here on the sparse layout)
+  Context.solve_tfqmr(rho, ...)  <- solve_tfqmr
+  Context.current / occupation   <- calcj / calcocc
+  Context.propagate(...)         <- intstp (RK4) / chebyshev
+and raises HeomError carrying the library's message where the reference would stop.
+The compute path is the CUDA library; there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import models  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libheom_gb300.so")
+
+PREC_FP64, PREC_MIXED = 0, 1
+PROP_RK4, PROP_CHEBYSHEV = 0, 1
+ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "out of memory", -4: "unsupported",
+          -5: "TFQMR breakdown", -6: "not converged", -7: "device wait timed out"}
+
+
+class HeomError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_p = C.POINTER
+
+
+class Tables(C.Structure):
+    _fields_ = [
+        ("norbs", C.c_int32), ("nspin", C.c_int32), ("nalf", C.c_int32), ("ncor", C.c_int32), ("ntier", C.c_int32),
+        ("nrho", C.c_int32), ("nams", C.c_int32), ("lscreen", C.c_int32),
+        ("nunk", C.c_int64), ("lall", C.c_int64), ("lunk_spa", C.c_int64),
+        ("cgamma", C.c_void_p), ("dipm", C.c_void_p),
+        ("mpm", C.c_void_p), ("morbs", C.c_void_p), ("mspin", C.c_void_p), ("ilead", C.c_void_p), ("mcor", C.c_void_p),
+        ("indexdraw", C.c_void_p), ("cb", C.c_void_p), ("cd", C.c_void_p), ("eleadinfty", C.c_void_p),
+        ("nfirst", C.c_void_p), ("nlast", C.c_void_p), ("ifirst", C.c_void_p), ("indextable", C.c_void_p),
+        ("index_coef_ref", C.c_void_p), ("indexcoef", C.c_void_p), ("itypecoef", C.c_void_p),
+        ("ifactfcoef", C.c_void_p), ("ifactrcoef", C.c_void_p),
+        ("rowams", C.c_void_p), ("colams", C.c_void_p), ("sgnams", C.c_void_p), ("hs", C.c_void_p),
+        ("nnz_spa", C.c_void_p), ("ind_spa", C.c_void_p), ("irow_spa", C.c_void_p), ("icol_spa", C.c_void_p),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("norbs", C.c_int32), ("nspin", C.c_int32), ("nalf", C.c_int32), ("nmats", C.c_int32), ("ntier", C.c_int32),
+        ("bandwidth", C.c_double * 2), ("linewidth", (C.c_double * 3) * 2), ("temperature", C.c_double * 2),
+        ("engyshift", (C.c_double * 2) * 2), ("lscreen", C.c_int32), ("doubledot", C.c_int32), ("model", C.c_int32),
+        ("eup", C.c_double), ("edown", C.c_double), ("uu", C.c_double),
+        ("e1up", C.c_double), ("e1down", C.c_double), ("e2up", C.c_double), ("e2down", C.c_double),
+        ("uu1", C.c_double), ("uu2", C.c_double), ("u12", C.c_double), ("t12", C.c_double),
+        ("kan_u", C.c_double), ("kan_j", C.c_double), ("kan_eps", C.c_double),
+        ("hs_in", C.c_void_p), ("tchar", (C.c_double * 2) * 2),
+    ]
+
+
+class CtxOpts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("build_adjoint", C.c_int32), ("amps", C.c_void_p), ("tchar", C.c_void_p),
+                ("dhs", C.c_void_p * 4)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32), ("inner_tol", C.c_double),
+                ("max_refine", C.c_int32)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iters", C.c_int32), ("ierr", C.c_int32), ("refinements", C.c_int32), ("converged", C.c_int32),
+                ("resid", C.c_double), ("seconds", C.c_double), ("launches", C.c_int64)]
+
+
+class GradOpts(C.Structure):
+    _fields_ = [("deshift", C.c_void_p), ("gamma", C.c_double), ("dhs_du", C.c_void_p), ("dhs_deps", C.c_void_p),
+                ("crit", C.c_double), ("maxit0", C.c_int32)]
+
+
+# symbol -> (restype, argtypes); also the list of entry points of include/heom_gb300.h
+SIGNATURES = {
+    "heom_model_build": (C.c_int, [_p(Params), _p(C.c_void_p)]),
+    "heom_model_destroy": (None, [C.c_void_p]),
+    "heom_model_tables": (_p(Tables), [C.c_void_p]),
+    "heom_model_initial_guess": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "heom_model_field": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_model_get": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
+    "heom_ctx_create": (C.c_int, [_p(Tables), _p(CtxOpts), _p(C.c_void_p)]),
+    "heom_ctx_destroy": (None, [C.c_void_p]),
+    "heom_ctx_lunk": (C.c_int64, [C.c_void_p]),
+    "heom_last_error": (C.c_char_p, []),
+    "heom_calc_ax": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "heom_calcderiv": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]),
+    "heom_calc_atrx": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "heom_calc_ax_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_calc_atrx_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_calc_ax_fp32_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_solve_tfqmr": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
+    "heom_current": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_occupation": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_propagate": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]),
+    "heom_steady_gradient": (C.c_int, [C.c_void_p, _p(GradOpts), C.c_void_p, C.c_int32, C.c_void_p, _p(SolveInfo)]),
+    "heom_td_gradient": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_solve_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
+    "heom_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "heom_ctx_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "heom_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(C.c_void_p)]),
+    "heom_batch_stride": (C.c_int64, [C.c_void_p]),
+    "heom_batch_solve_dev": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
+    "heom_batch_destroy": (None, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise HeomError(-4, f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise HeomError(rc, lib().heom_last_error().decode())
+
+
+def _c128(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} complex entries, got {a.size}")
+    return a
+
+
+def make_params(cfg):
+    p = Params()
+    p.norbs, p.nspin, p.nalf, p.nmats, p.ntier = cfg["norbs"], cfg["nspin"], cfg["nalf"], cfg["nmats"], cfg["ntier"]
+    for a in range(cfg["nalf"]):
+        p.bandwidth[a] = cfg["bandwidth"][a]
+        p.temperature[a] = cfg["temperature"][a]
+        for o in range(cfg["norbs"]):
+            p.linewidth[a][o] = cfg["linewidth"][a][o]
+        for s in range(cfg["nspin"]):
+            p.engyshift[a][s] = cfg["engyshift"][a][s]
+            p.tchar[a][s] = cfg.get("tchar", 0.0)
+    p.lscreen = int(cfg.get("lscreen", 0))
+    p.doubledot = int(cfg.get("doubledot", 0))
+    p.model = cfg["model"]
+    for k in ("eup", "edown", "uu", "e1up", "e1down", "e2up", "e2down", "uu1", "uu2", "u12", "t12", "kan_u", "kan_j", "kan_eps"):
+        setattr(p, k, float(cfg.get(k, 0.0)))
+    return p
+
+
+class Model:
+    """Host-side set-up of one job (evaluatepara, buildoperator, calchs, ball2drawer,
+    buildcoefindex, prelude_spa): the tables the sparse path consumes."""
+
+    def __init__(self, cfg, hs=None):
+        self.cfg = dict(cfg)
+        p = make_params(cfg)
+        self._hs = None
+        if hs is not None:
+            self._hs = _c128(np.asarray(hs).reshape(-1, order="F"))
+            p.hs_in = self._hs.ctypes.data
+            p.model = 9
+        h = C.c_void_p()
+        _check(lib().heom_model_build(C.byref(p), C.byref(h)))
+        self.h = h
+        self.tables = lib().heom_model_tables(h).contents
+        t = self.tables
+        self.nrho, self.lunk, self.nunk, self.lall = t.nrho, t.lunk_spa, t.nunk, t.lall
+        self.norbs, self.nspin, self.nalf, self.ncor, self.ntier = t.norbs, t.nspin, t.nalf, t.ncor, t.ntier
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.heom_model_destroy(self.h)
+            self.h = None
+
+    def array(self, name):
+        """numpy copy of one table of the heom_tables view."""
+        t = self.tables
+        nvar = 2 * t.norbs * t.nspin * t.nalf * t.ncor
+        ncb = t.norbs * t.nspin * t.ncor * t.nalf * 2
+        spec = {
+            "cgamma": (nvar, np.complex128), "dipm": (nvar, np.float64), "mpm": (nvar, np.int32), "morbs": (nvar, np.int32),
+            "mspin": (nvar, np.int32), "ilead": (nvar, np.int32), "mcor": (nvar, np.int32), "indexdraw": (nvar, np.int32),
+            "cb": (ncb, np.complex128), "cd": (ncb, np.complex128), "eleadinfty": (t.nalf * t.nspin, np.float64),
+            "nfirst": (t.ntier, np.int64), "nlast": (t.ntier, np.int64), "ifirst": (t.ntier, np.int64),
+            "index_coef_ref": (t.nunk, np.int64), "indexcoef": (t.lall, np.int64), "itypecoef": (t.lall, np.int8),
+            "ifactfcoef": (t.lall, np.int8), "ifactrcoef": (t.lall, np.int8),
+            "rowams": (t.nams * t.norbs * t.nspin, np.int32), "colams": (t.nams * t.norbs * t.nspin, np.int32),
+            "sgnams": (t.nams * t.norbs * t.nspin, np.int32), "hs": (t.nrho ** 2, np.complex128),
+            "nnz_spa": (t.nunk, np.int32), "ind_spa": (t.nunk, np.int64), "irow_spa": (t.lunk_spa, np.int32),
+            "icol_spa": (t.lunk_spa, np.int32),
+        }
+        if name == "indextable":
+            nlast = self.array("nlast")
+            nfirst = self.array("nfirst")
+            n = 1 + sum(int(nlast[k] - nfirst[k] + 1) * k for k in range(1, t.ntier))
+            spec[name] = (n, np.int32)
+        cnt, dt = spec[name]
+        ptr = getattr(t, name)
+        buf = (C.c_char * (cnt * np.dtype(dt).itemsize)).from_address(ptr)
+        return np.frombuffer(bytes(buf), dtype=dt).copy()
+
+    def get(self, name, count, dtype):
+        out = np.zeros(count, dtype=dtype)
+        _check(lib().heom_model_get(self.h, name.encode(), out.ctypes.data))
+        return out
+
+    def initial_guess(self):
+        r = np.zeros(self.lunk, dtype=np.complex128)
+        _check(lib().heom_model_initial_guess(self.h, r.ctypes.data))
+        return r
+
+    def field(self):
+        a = np.zeros(self.nalf * self.nspin)
+        tc = np.zeros(self.nalf * self.nspin)
+        _check(lib().heom_model_field(self.h, a.ctypes.data, tc.ctypes.data))
+        return a, tc
+
+
+class Context:
+    """Device-resident plan of one model (opaque heom_ctx)."""
+
+    def __init__(self, model, device=0, adjoint=True, amps=None, tchar=None, dhs=()):
+        self.model = model
+        o = CtxOpts()
+        o.device = device
+        o.build_adjoint = int(adjoint)
+        self._keep = []
+        if amps is not None:
+            a = np.ascontiguousarray(amps, dtype=np.float64)
+            self._keep.append(a)
+            o.amps = a.ctypes.data
+        if tchar is not None:
+            tc = np.ascontiguousarray(tchar, dtype=np.float64)
+            self._keep.append(tc)
+            o.tchar = tc.ctypes.data
+        for k, d in enumerate(dhs):
+            if d is not None:
+                dd = _c128(d)
+                self._keep.append(dd)
+                o.dhs[k] = dd.ctypes.data
+        h = C.c_void_p()
+        _check(lib().heom_ctx_create(C.byref(model.tables), C.byref(o), C.byref(h)))
+        self.h = h
+        self.lunk = model.lunk
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.heom_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    # -- reference-named entry points --
+    def calc_ax_tfqmr_spa(self, x):
+        x = _c128(x, self.lunk + 1)
+        y = np.zeros(self.lunk + 1, dtype=np.complex128)
+        _check(lib().heom_calc_ax(self.h, self.lunk, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def calcderiv_spa(self, t, x):
+        x = _c128(x, self.lunk)
+        y = np.zeros(self.lunk, dtype=np.complex128)
+        _check(lib().heom_calcderiv(self.h, float(t), x.ctypes.data, y.ctypes.data))
+        return y
+
+    def calc_atrx(self, x):
+        x = _c128(x, self.lunk + 1)
+        y = np.zeros(self.lunk + 1, dtype=np.complex128)
+        _check(lib().heom_calc_atrx(self.h, self.lunk, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def solve_tfqmr(self, rho=None, crit=1e-10, maxit0=20000, precision=PREC_FP64, inner_tol=1e-4, max_refine=8,
+                    check=True):
+        if rho is None:
+            rho = self.model.initial_guess()
+        rho = _c128(rho, self.lunk).copy()
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine)
+        info = SolveInfo()
+        rc = lib().heom_solve_tfqmr(self.h, C.byref(o), rho.ctypes.data, C.byref(info))
+        if check:
+            _check(rc)
+        return rho, info
+
+    def solve_batch(self, rhos, hs_batch=None, eshift_batch=None, crit=1e-10, maxit0=20000, precision=PREC_FP64,
+                    inner_tol=1e-4, max_refine=8):
+        rhos = np.ascontiguousarray(rhos, dtype=np.complex128).copy()
+        nb = rhos.shape[0]
+        hs = None if hs_batch is None else _c128(hs_batch)
+        es = None if eshift_batch is None else np.ascontiguousarray(eshift_batch, dtype=np.float64)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine)
+        info = SolveInfo()
+        _check(lib().heom_solve_batch(self.h, nb, None if hs is None else hs.ctypes.data,
+                                      None if es is None else es.ctypes.data, C.byref(o), rhos.ctypes.data, C.byref(info)))
+        return rhos, info
+
+    def current(self, rho):
+        rho = _c128(rho, self.lunk)
+        jt = np.zeros(self.model.nalf * self.model.nspin)
+        _check(lib().heom_current(self.h, rho.ctypes.data, jt.ctypes.data))
+        return jt.reshape(self.model.nspin, self.model.nalf).T   # jt[ialf, ispin]
+
+    def occupation(self, rho):
+        rho = _c128(rho, self.lunk)
+        occ = np.zeros(self.model.norbs * self.model.nspin)
+        _check(lib().heom_occupation(self.h, rho.ctypes.data, occ.ctypes.data))
+        return occ.reshape(self.model.nspin, self.model.norbs).T
+
+    def propagate(self, rho, t0, dt, nstep, method=PROP_RK4, currents=False):
+        rho = _c128(rho, self.lunk).copy()
+        jt = np.zeros((nstep, self.model.nalf * self.model.nspin)) if currents else None
+        _check(lib().heom_propagate(self.h, method, t0, dt, nstep, rho.ctypes.data, None if jt is None else jt.ctypes.data))
+        return (rho, jt) if currents else rho
+
+    def steady_gradient(self, rho, deshift=None, gamma=None, dhs_du=None, dhs_deps=None, which=0xF, crit=1e-10, maxit0=20000):
+        rho = _c128(rho, self.lunk)
+        o = GradOpts(crit=crit, maxit0=maxit0, gamma=gamma or 0.0)
+        keep = []
+        if deshift is not None:
+            d = np.ascontiguousarray(deshift, dtype=np.float64); keep.append(d); o.deshift = d.ctypes.data
+        if dhs_du is not None:
+            d = _c128(dhs_du); keep.append(d); o.dhs_du = d.ctypes.data
+        if dhs_deps is not None:
+            d = _c128(dhs_deps); keep.append(d); o.dhs_deps = d.ctypes.data
+        dI = np.zeros(4)
+        info = SolveInfo()
+        _check(lib().heom_steady_gradient(self.h, C.byref(o), rho.ctypes.data, which, dI.ctypes.data, C.byref(info)))
+        return dI, info
+
+    def td_gradient(self, rho0, dt, nstep, checkpoint_every=32):
+        rho0 = _c128(rho0, self.lunk)
+        val = C.c_double()
+        grad = C.c_double()
+        _check(lib().heom_td_gradient(self.h, dt, nstep, checkpoint_every, rho0.ctypes.data, C.byref(val), C.byref(grad)))
+        return val.value, grad.value
+
+    def bench_apply(self, precision=PREC_FP64, reps=20, nbatch=1):
+        """Average device time of one apply launch over nbatch instances, and its algorithmic bytes."""
+        s = C.c_double()
+        b = C.c_double()
+        _check(lib().heom_bench_apply(self.h, precision, nbatch, reps, C.byref(s), C.byref(b)))
+        return s.value, b.value
+
+    def stats(self):
+        """Plan statistics (see heom_ctx_stats in include/heom_gb300.h)."""
+        out = np.zeros(9)
+        _check(lib().heom_ctx_stats(self.h, out.ctypes.data))
+        keys = ("entries", "ados", "classes", "couplings", "maps", "gathers", "same_tier_terms", "lower_gathers", "plan_bytes")
+        return dict(zip(keys, out.tolist()))
+
+
+class Batch:
+    """Instances of one table set (bias / level sweeps) solved together; parameters stay on
+    the device.  x_dev: device pointer (int) to nbatch FP64 complex vectors of stride `stride`."""
+
+    def __init__(self, ctx, hs_batch=None, eshift_batch=None, nbatch=None):
+        self.ctx = ctx
+        if nbatch is None:
+            nbatch = len(hs_batch) if hs_batch is not None else len(eshift_batch)
+        self.nbatch = nbatch
+        self._hs = None if hs_batch is None else _c128(hs_batch)
+        self._es = None if eshift_batch is None else np.ascontiguousarray(eshift_batch, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().heom_batch_create(ctx.h, nbatch, None if self._hs is None else self._hs.ctypes.data,
+                                       None if self._es is None else self._es.ctypes.data, C.byref(h)))
+        self.h = h
+        self.stride = lib().heom_batch_stride(h)
+
+    def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, max_refine=3, check=True):
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=0.0, max_refine=max_refine)
+        info = SolveInfo()
+        rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
+        if check:
+            _check(rc)
+        return info
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.heom_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close

@@ -1,0 +1,230 @@
+/*
+ * heom_gb300.h -- C ABI of the GB300 (sm_103a) HEOM Liouvillian library.
+ *
+ * Drop-in for the sparse-mode hot path of HEOM-QUICK2.  The reference routines
+ * keep their arguments in Fortran modules; here they are passed once through
+ * heom_tables (a plain view of the module arrays) and live in an opaque context
+ * that owns the device copies.  All entry points return 0 on success or a
+ * negative HEOM_E* code and never abort; heom_last_error() describes the failure.
+ * A context is single-stream and not thread-safe, like the reference routines
+ * (whose SAVE counters make them non-reentrant).
+ *
+ * Complex data are double _Complex / float _Complex, i.e. interleaved (re, im),
+ * which is complex(c_double_complex) in ISO_C_BINDING.  Table values keep the
+ * reference conventions: 1-based ADO, drawer and matrix indices, column-major
+ * matrices.
+ */
+#ifndef HEOM_GB300_H
+#define HEOM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HEOM_ABI_VERSION 1
+
+enum {
+    HEOM_OK = 0,
+    HEOM_E_ARG = -1,        /* invalid argument / inconsistent table */
+    HEOM_E_CUDA = -2,       /* CUDA runtime failure (no device, launch error, ...) */
+    HEOM_E_NOMEM = -3,      /* host or device allocation failed */
+    HEOM_E_UNSUPPORTED = -4,/* option the library does not implement (e.g. lad, lsimple) */
+    HEOM_E_BREAKDOWN = -5,  /* TFQMR breakdown (reference ierr = 8) */
+    HEOM_E_NOCONV = -6,     /* iteration limit reached before convergence */
+    HEOM_E_TIMEOUT = -7     /* a bounded device-side wait gave up */
+};
+
+/* Precision of the steady-state solver. */
+enum { HEOM_PREC_FP64 = 0, HEOM_PREC_MIXED = 1 };
+
+/* View of the module data the reference keeps for the sparse path
+ * (module/matmod.f90:4-52, module/sparsemod.f90:34-42, include/common).  The
+ * arrays are read during heom_ctx_create only; the caller keeps ownership. */
+typedef struct {
+    int32_t norbs, nspin, nalf, ncor;       /* nvar = 2*norbs*nspin*nalf*ncor drawers */
+    int32_t ntier;                          /* reference ntier = truncation tier + 1 */
+    int32_t nrho;                           /* (2*nspin)^norbs */
+    int32_t nams;                           /* nonzeros per a_{ms} */
+    int32_t lscreen;                        /* drawers of screened operators are absent */
+    int64_t nunk, lall, lunk_spa;
+    /* per drawer (nvar entries, reference order sgn > spin > orbs > alf > cor) */
+    const double _Complex *cgamma;          /* damping rate of each drawer */
+    const double *dipm;                     /* +1 / -1 */
+    const int32_t *mpm, *morbs, *mspin, *ilead, *mcor;
+    const int32_t *indexdraw;               /* first-tier ADO of a + drawer (0 if screened) */
+    /* cb, cd laid out as cb(norbs, nspin, ncor, nalf, 2), column-major */
+    const double _Complex *cb, *cd;
+    const double *eleadinfty;               /* (nalf, nspin): lead shift as t -> infinity */
+    /* hierarchy tables (main/buildcoefindex.f90) */
+    const int64_t *nfirst, *nlast;          /* ntier entries */
+    const int64_t *ifirst;                  /* ntier entries */
+    const int32_t *indextable;              /* drawer tuples of every ADO */
+    const int64_t *index_coef_ref;          /* nunk entries: first coupling of each ADO */
+    const int64_t *indexcoef;               /* lall: target ADO (1-based) */
+    const int8_t *itypecoef, *ifactfcoef, *ifactrcoef;
+    /* a_{ms} in signed COO (main/arrangeoperator.f90): (nams, norbs, nspin) */
+    const int32_t *rowams, *colams, *sgnams;
+    /* system Hamiltonian in internal units (energy / hbar), nrho x nrho */
+    const double _Complex *hs;
+    /* per-ADO sparsity (fermion/prelude_spa.f90) */
+    const int32_t *nnz_spa;
+    const int64_t *ind_spa;
+    const int32_t *irow_spa, *icol_spa;
+} heom_tables;
+
+/* ------------------------------------------------------------------------- */
+/* Model builder.  Stands in for the Fortran driver's set-up when the caller has
+ * no Fortran (main/evaluatepara.f90, buildoperator, calchs, ball2drawer,
+ * buildcoefindex, prelude_spa): it produces tables identical to the reference's
+ * for the Lorentzian-PSD input subset below. */
+typedef struct {
+    int32_t norbs, nspin, nalf, nmats, ntier;
+    double bandwidth[2], linewidth[2][3], temperature[2], engyshift[2][2];
+    int32_t lscreen, doubledot;
+    int32_t model;            /* 1 $para1, 4 $para4, 5 Kanamori (lreadhs data), 9 hs given */
+    double eup, edown, uu;
+    double e1up, e1down, e2up, e2down, uu1, uu2, u12, t12;
+    double kan_u, kan_j, kan_eps;
+    const double _Complex *hs_in;     /* model 9: nrho*nrho, internal units */
+    double tchar[2][2];               /* fieldtype = 0 switch-on time of the lead shift */
+} heom_params;
+
+typedef struct heom_model heom_model;
+
+int  heom_model_build(const heom_params *p, heom_model **out);
+void heom_model_destroy(heom_model *m);
+/* Borrowed view of the built tables (valid while the model lives). */
+const heom_tables *heom_model_tables(const heom_model *m);
+/* Boltzmann reduced density matrix at the lead-1 temperature on the RDO pattern,
+ * zero ADOs (main/analyze_hs.f90:144-176 + fermion/initialize1_spa.f90). rho: lunk_spa. */
+int  heom_model_initial_guess(const heom_model *m, double _Complex *rho);
+/* Lead shifts / amplitudes of the model (nalf x nspin, column-major, internal units). */
+int  heom_model_field(const heom_model *m, double *amps, double *tchar);
+/* Copy a named derived quantity: "hs", "dhs_deps", "dhs_du" (nrho^2 complex),
+ * "cpcoef", "cppole", "amsori" (dense a_{ms}, real). Returns HEOM_E_ARG for an unknown name. */
+int  heom_model_get(const heom_model *m, const char *name, void *dst);
+
+/* ------------------------------------------------------------------------- */
+/* Context: device-resident plan of one model.  */
+typedef struct heom_ctx heom_ctx;
+
+typedef struct {
+    int32_t device;           /* CUDA device ordinal */
+    int32_t build_adjoint;    /* also build the transpose (adjoint) plan */
+    const double *amps;       /* (nalf, nspin) lead-shift amplitude for heom_calcderiv; NULL = eleadinfty */
+    const double *tchar;      /* (nalf, nspin) switch-on time, NULL = 0 (step) */
+    const double _Complex *dhs[4];  /* optional parameter derivatives of hs for gradients */
+} heom_ctx_opts;
+
+int  heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **out);
+void heom_ctx_destroy(heom_ctx *ctx);
+int64_t heom_ctx_lunk(const heom_ctx *ctx);
+const char *heom_last_error(void);
+
+/* y = A x  (calc_ax_tfqmr_spa_omp, tfqmr_double/calc_ax_tfqmr_spa_omp.f90:1).
+ * x, y: ldim+1 complex (host memory); ldim must equal lunk_spa; y[ldim] = Tr rho0. */
+int heom_calc_ax(heom_ctx *ctx, int64_t ldim, const double _Complex *x, double _Complex *y);
+/* dRho/dt at time t (calcderiv_spa_omp, td/calcderiv_spa_omp.f90:1): x, y lunk entries. */
+int heom_calcderiv(heom_ctx *ctx, double t, const double _Complex *x, double _Complex *y);
+/* y = A^H x, the adjoint of heom_calc_ax in the real inner product <u,v> = Re(u^H v)
+ * (the role calc_atrx_bicg_omp, bicg/calc_atrx_bicg_omp.f90:1, plays for the dense
+ * BiCG path, here on the sparse layout). x, y: ldim+1 complex. */
+int heom_calc_atrx(heom_ctx *ctx, int64_t ldim, const double _Complex *x, double _Complex *y);
+/* Device-pointer variants (pointers in the context's device memory space, stream 0 order). */
+int heom_calc_ax_dev(heom_ctx *ctx, const void *dx, void *dy);
+int heom_calc_atrx_dev(heom_ctx *ctx, const void *dx, void *dy);
+int heom_calc_ax_fp32_dev(heom_ctx *ctx, const void *dx, void *dy);
+
+/* Steady state by TFQMR (solve_tfqmr, tfqmr_double/solve_tfqmr.f90:1). */
+typedef struct {
+    double crit;              /* ||b - A x|| target (reference $converge crit) */
+    int32_t maxit0;           /* reference maxit0 (TFQMR limit = maxit0/2) */
+    int32_t precision;        /* HEOM_PREC_FP64 or HEOM_PREC_MIXED */
+    double inner_tol;         /* MIXED: relative residual of each FP32 inner solve */
+    int32_t max_refine;       /* MIXED: outer refinement rounds */
+} heom_solve_opts;
+
+typedef struct {
+    int32_t iters;            /* operator applies of the Krylov iterations */
+    int32_t ierr;             /* reference dutfx ierr of the last (inner) solve */
+    int32_t refinements;      /* MIXED: outer rounds used */
+    int32_t converged;
+    double resid;             /* final ||b - A x|| in FP64 (worst instance of a batch) */
+    double seconds;           /* device time of the solve */
+    int64_t launches;         /* kernels launched by the solve (graph nodes included) */
+} heom_solve_info;
+
+/* rho: lunk_spa complex (host), initial guess in, steady state out. */
+int heom_solve_tfqmr(heom_ctx *ctx, const heom_solve_opts *o, double _Complex *rho, heom_solve_info *info);
+
+/* Observables of a host rho (td/calcj.f90, main/calcocc.f90).
+ * jt: nalf*nspin (ialf fastest) in reference current units; occ: norbs*nspin. */
+int heom_current(heom_ctx *ctx, const double _Complex *rho, double *jt);
+int heom_occupation(heom_ctx *ctx, const double _Complex *rho, double *occ);
+
+/* Time propagation (td/intstp.f90 RK4; td/chebyshev.f90 Chebyshev, on the sparse
+ * layout).  rho (host, lunk) advanced from t0 by nstep steps of dt.  If jt_out is
+ * non-NULL it receives the current jt (nalf*nspin) at the start of every step
+ * (nstep rows), like curr.data. */
+enum { HEOM_PROP_RK4 = 0, HEOM_PROP_CHEBYSHEV = 1 };
+int heom_propagate(heom_ctx *ctx, int32_t method, double t0, double dt, int32_t nstep,
+                   double _Complex *rho, double *jt_out);
+
+/* Steady-state sensitivities by the adjoint method: for the lead-1 current
+ * I = sum_s jt(1,s), dI/dtheta for theta in {V (bias, engyshift = +-V/2),
+ * Gamma (all linewidths scaled together), U, eps} given as 4 partial derivatives
+ * of (eleadinfty, cb/cd, hs).  rho: converged steady state (host).  dI: 4 doubles.
+ * which: bitmask of the parameters wanted (bit k <-> theta k). */
+typedef struct {
+    const double *deshift;            /* (nalf,nspin) d eleadinfty / dV */
+    double gamma;                     /* current linewidth scale for dA/dGamma = A_lower / Gamma */
+    const double _Complex *dhs_du;    /* d hs / dU (nrho^2) */
+    const double _Complex *dhs_deps;  /* d hs / d eps (nrho^2) */
+    double crit;                      /* adjoint solve tolerance */
+    int32_t maxit0;
+} heom_grad_opts;
+int heom_steady_gradient(heom_ctx *ctx, const heom_grad_opts *o, const double _Complex *rho,
+                         int32_t which, double *dI, heom_solve_info *info);
+
+/* Time-dependent sensitivity: d/dA of int_0^{nstep dt} I_L(t) dt for a Chebyshev
+ * propagation under the step bias amplitude scale A (eshift = A * amps), by a
+ * reverse pass with checkpoints every k steps. rho0: initial state (host, lunk). */
+int heom_td_gradient(heom_ctx *ctx, double dt, int32_t nstep, int32_t checkpoint_every,
+                     const double _Complex *rho0, double *integral, double *dintegral);
+
+/* Batched steady states: many instances that share one table set and differ in
+ * hs and eleadinfty are solved together (one vector per instance, one launch per
+ * step for all of them).  hs_batch: nbatch * nrho^2, eshift_batch: nbatch*nalf*nspin.
+ * rho_batch: nbatch * lunk (host, in/out). */
+int heom_solve_batch(heom_ctx *ctx, int32_t nbatch, const double _Complex *hs_batch,
+                     const double *eshift_batch, const heom_solve_opts *o,
+                     double _Complex *rho_batch, heom_solve_info *info);
+
+/* The same batch with its parameters kept on the device between solves.
+ * heom_batch_solve_dev: x_dev holds nbatch FP64 complex vectors of stride
+ * heom_batch_stride() elements (entry lunk of each is the unused trace slot), with the
+ * initial guesses on entry and the steady states on return. */
+typedef struct heom_batch heom_batch;
+int heom_batch_create(heom_ctx *ctx, int32_t nbatch, const double _Complex *hs_batch, const double *eshift_batch,
+                      heom_batch **out);
+int64_t heom_batch_stride(const heom_batch *b);
+int heom_batch_solve_dev(heom_batch *b, const heom_solve_opts *o, void *x_dev, heom_solve_info *info);
+void heom_batch_destroy(heom_batch *b);
+
+/* Measurement hook: time `reps` back-to-back applies on `nbatch` instances on device
+ * (precision 0 FP64, 1 FP32x2 as used by the mixed solver, 2 plain FP32) and return the
+ * average kernel time in seconds and the algorithmic bytes of one launch. */
+int heom_bench_apply(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
+
+/* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs
+ * with entries, [2] pattern classes, [3] coupling records, [4] gather maps, [5] useful
+ * gathers (nonzero map halves), [6] same-tier terms, [7] lower-tier (complex-coefficient)
+ * gathers, [8] plan bytes read per apply (records, maps, per-entry and per-ADO arrays). */
+int heom_ctx_stats(const heom_ctx *ctx, double *out /* 9 */);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -114,7 +114,7 @@ static int orc_encode(int nspin, int norbs, int occ[][2])
 /* main/swapms.f90: exchange spin-s occupations of orbitals iorbs-1 and iorbs */
 static void orc_swapms(int nspin, int norbs, int irow, int icol, int iorbs, int ispin, int *orow, int *ocol, int *osgn)
 {
-    int occ[ORC_MAXORB][2], sgr, sgc, t;
+    int occ[ORC_MAXORB][2] = {{0}}, sgr, sgc, t;
     orc_decode(nspin, norbs, irow, occ);
     sgr = (occ[iorbs - 2][ispin - 1] == 1 && occ[iorbs - 1][ispin - 1] == 1) ? -1 : 1;
     t = occ[iorbs - 2][ispin - 1]; occ[iorbs - 2][ispin - 1] = occ[iorbs - 1][ispin - 1]; occ[iorbs - 1][ispin - 1] = t;
@@ -128,7 +128,7 @@ static void orc_swapms(int nspin, int norbs, int irow, int icol, int iorbs, int 
 /* main/swapspin.f90: exchange up/down occupations of orbital iorbs */
 static void orc_swapspin(int norbs, int irow, int icol, int iorbs, int *orow, int *ocol, int *osgn)
 {
-    int occ[ORC_MAXORB][2], sgr, sgc, t;
+    int occ[ORC_MAXORB][2] = {{0}}, sgr, sgc, t;
     orc_decode(2, norbs, irow, occ);
     sgr = (occ[iorbs - 1][0] == 1 && occ[iorbs - 1][1] == 1) ? -1 : 1;
     t = occ[iorbs - 1][0]; occ[iorbs - 1][0] = occ[iorbs - 1][1]; occ[iorbs - 1][1] = t;

@@ -1,48 +1,8 @@
-"""Synthetic impurity models of the benchmark, in the quantities of the reference
-input file (positional lines of main/evaluatepara.f90:71-84 plus namelists).
+"""Benchmark models used by the tests (the presets live in the library package)."""
+import os
+import sys
 
-Energies are in the input units (meV with funits=1); the library divides by hbar.
-"""
-import numpy as np
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "heom-quick2_gb300"))
+from heomq.models import siam, dqd, hund, iv_sweep, SIAM_L3, DQD_L4, HUND_L2  # noqa: E402,F401
 
-
-def siam(ntier=4, nmats=4, V=0.4, U=2.0, eps=-1.0, gamma=0.5, W=10.0, T=0.1):
-    """Single-orbital Anderson impurity, nd=4 ($para1 eup/edown/uu)."""
-    return dict(norbs=1, nspin=2, nalf=2, nmats=nmats, ntier=ntier, bandwidth=[W, W],
-                linewidth=[[gamma], [gamma]], temperature=[T, T],
-                engyshift=[[V / 2, V / 2], [-V / 2, -V / 2]], model=1, eup=eps, edown=eps, uu=U)
-
-
-def dqd(ntier=5, nmats=3, V=0.8, U=2.0, eps=-1.0, t=0.5, gamma=0.5, W=10.0, T=0.1):
-    """Serial double quantum dot, nd=16 ($para4, $ddots doubledot=T, lscreen=T)."""
-    return dict(norbs=2, nspin=2, nalf=2, nmats=nmats, ntier=ntier, bandwidth=[W, W],
-                linewidth=[[gamma, gamma], [gamma, gamma]], temperature=[T, T],
-                engyshift=[[V / 2, V / 2], [-V / 2, -V / 2]], model=4,
-                e1up=eps, e1down=eps, e2up=eps, e2down=eps, uu1=U, uu2=U, u12=0.0, t12=t,
-                doubledot=1, lscreen=1)
-
-
-def hund(ntier=3, nmats=6, V=0.2, U=3.0, J=0.3, gamma=0.25, W=10.0, T=0.05):
-    """Three-orbital Kanamori impurity, nd=64 ($hamil_sys lreadhs=T with a generated H)."""
-    return dict(norbs=3, nspin=2, nalf=2, nmats=nmats, ntier=ntier, bandwidth=[W, W],
-                linewidth=[[gamma] * 3, [gamma] * 3], temperature=[T, T],
-                engyshift=[[V / 2, V / 2], [-V / 2, -V / 2]], model=5,
-                kan_u=U, kan_j=J, kan_eps=-(5 * U - 10 * J) / 2)
-
-
-# BASELINE configs
-CFG0 = siam(ntier=4, nmats=4, V=0.4)               # SIAM L=3
-CFG1 = dqd(ntier=5, nmats=3, V=0.8)                # DQD L=4
-CFG4 = hund(ntier=3, nmats=6, V=0.2)               # Hund L=2
-
-
-def iv_sweep(n=128, seed=20261203):
-    """Config 2: n SIAM instances, V~U[-1,1], U in {1,2,3}, eps=-U/2, L in {2,3,4}."""
-    rng = np.random.default_rng(seed)
-    out = []
-    for _ in range(n):
-        V = float(rng.uniform(-1.0, 1.0))
-        U = float(rng.choice([1.0, 2.0, 3.0]))
-        L = int(rng.choice([2, 3, 4]))
-        out.append(siam(ntier=L + 1, nmats=4, V=V, U=U, eps=-U / 2))
-    return out
+CFG0, CFG1, CFG4 = SIAM_L3, DQD_L4, HUND_L2

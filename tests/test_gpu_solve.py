@@ -1,0 +1,40 @@
+"""Steady-state solves on the GPU against the oracle's TFQMR.
+
+crit follows the reference default ($converge crit = 1d-8, main/main.f90:856): the
+augmented HEOM system at T = 0.1 is ill-conditioned (slow Coulomb-blockade relaxation),
+and plain FP64 TFQMR stalls near relative residual 1e-10 on the double dot."""
+import numpy as np
+import pytest
+
+import configs as cf
+import heomq
+import oracle_ffi as of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cfg", [cf.siam(ntier=3), cf.CFG0, cf.dqd(ntier=3)], ids=["siam_L2", "siam_L3", "dqd_L2"])
+def test_fp64_solve_matches_oracle(cfg):
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m)
+    ref = of.Model(cfg)
+    rho, info = ctx.solve_tfqmr(crit=1e-8)
+    rho_ref, info_ref = ref.solve_tfqmr(crit=1e-8)
+    assert info.converged and info.resid <= 1e-8
+    j, j_ref = ctx.current(rho), ref.current(rho_ref)
+    assert np.max(np.abs(j - j_ref)) <= 1e-7 * np.max(np.abs(j_ref))
+    occ, occ_ref = ctx.occupation(rho), ref.occupation(rho_ref)
+    assert np.max(np.abs(occ - occ_ref)) <= 1e-7
+
+
+@pytest.mark.parametrize("cfg", [cf.CFG0, cf.dqd(ntier=3)], ids=["siam_L3", "dqd_L2"])
+def test_mixed_solve_matches_oracle(cfg):
+    """FP32x2 TFQMR with FP64 residual refinement reaches the FP64 criterion."""
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m)
+    ref = of.Model(cfg)
+    rho_ref, _ = ref.solve_tfqmr(crit=1e-8)
+    rho, info = ctx.solve_tfqmr(crit=1e-8, precision=heomq.PREC_MIXED)
+    assert info.converged and info.resid <= 1e-8
+    j, j_ref = ctx.current(rho), ref.current(rho_ref)
+    assert np.max(np.abs(j - j_ref)) <= 1e-7 * np.max(np.abs(j_ref))
