@@ -15,7 +15,10 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built():
+    """Build the oracle (the checker) and the product's CUDA library (no-op when current)."""
+    import build_lib
     import oracle_ffi
 
     oracle_ffi.build()
+    build_lib.build()
     yield

@@ -27,14 +27,16 @@ def test_fp64_solve_matches_oracle(cfg):
     assert np.max(np.abs(occ - occ_ref)) <= 1e-7
 
 
+@pytest.mark.parametrize("prec", [heomq.PREC_MIXED, heomq.PREC_MIXED_FP32X2], ids=["fp32", "fp32x2"])
 @pytest.mark.parametrize("cfg", [cf.CFG0, cf.dqd(ntier=3)], ids=["siam_L3", "dqd_L2"])
-def test_mixed_solve_matches_oracle(cfg):
-    """FP32x2 TFQMR with FP64 residual refinement reaches the FP64 criterion."""
+def test_mixed_solve_matches_oracle(cfg, prec):
+    """Inner TFQMR in FP32 (or FP32x2) on the regularised operator, refined with FP64
+    residuals, reaches the FP64 criterion."""
     m = heomq.Model(cfg)
     ctx = heomq.Context(m)
     ref = of.Model(cfg)
     rho_ref, _ = ref.solve_tfqmr(crit=1e-8)
-    rho, info = ctx.solve_tfqmr(crit=1e-8, precision=heomq.PREC_MIXED)
+    rho, info = ctx.solve_tfqmr(crit=1e-8, precision=prec)
     assert info.converged and info.resid <= 1e-8
     j, j_ref = ctx.current(rho), ref.current(rho_ref)
     assert np.max(np.abs(j - j_ref)) <= 1e-7 * np.max(np.abs(j_ref))
