@@ -31,7 +31,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=8, help="bias points per solve (per GPU)")
-    ap.add_argument("--crit", type=float, default=1e-8)
+    ap.add_argument("--crit", type=float, default=1e-9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiler run: warm-up solves, then one timed mixed solve; prints one short line")
@@ -185,10 +185,10 @@ def run_gb300(args, ws, rank, local, dist):
     x0[:, :L] = torch.from_numpy(x0h).to("cuda")
     x = torch.empty_like(x0)
 
-    def step(prec):
+    def step(prec, crit=None, refine=8):
         x.copy_(x0)
         torch.cuda.synchronize()
-        return batch.solve_dev(x.data_ptr(), crit=args.crit, precision=prec)
+        return batch.solve_dev(x.data_ptr(), crit=crit or args.crit, precision=prec, max_refine=refine)
 
     for _ in range(args.warmup):
         step(heomq.PREC_MIXED)
@@ -250,7 +250,12 @@ def run_gb300(args, ws, rank, local, dist):
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / sec / 1e9
     traffic = profile_traffic()
-    err = max(abs(a - b) / abs(b) for a, b in zip(curm, cur64))
+    # accuracy: both paths against a reference steady state solved to ||b - A x|| <= 1e-12
+    # (mixed refinement; FP64 TFQMR alone stalls near 2e-10 on this model)
+    step(heomq.PREC_MIXED, crit=1e-12, refine=16)
+    curt = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
+    err = max(abs(a - b) / abs(b) for a, b in zip(curm, curt))
+    err64 = max(abs(a - b) / abs(b) for a, b in zip(cur64, curt))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -266,14 +271,15 @@ def run_gb300(args, ws, rank, local, dist):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32x2+f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "batch": B, "bias_points_meV": [round(v, 4) for v in Vs],
-                       "crit": args.crit, "solver": "TFQMR, FP32x2 arithmetic, FP64 residual refinement",
+                       "crit": args.crit, "solver": "TFQMR in FP32x2 on the regularised operator, FP64 residual refinement",
                        "l2": f"inputs larger than L2: {B} x 9 solver vectors x {L * 16 / 1e6:.1f} MB",
                        "parallelism": f"replicas x{ws}", "wall_s": wall,
                        "applies_per_solve": infos[-1].iters, "refinements": infos[-1].refinements,
                        "fp64": {"solves_per_s": ws * B / t64, "applies_per_solve": info64.iters,
                                 "apply_us": sec64 * 1e6, "apply_gbs_alg": alg64 / sec64 / 1e9},
                        "speedup_mixed_vs_fp64": (ws * B / t_step) / (ws * B / t64),
-                       "current_rel_err_mixed_vs_fp64": err},
+                       "current_rel_err_mixed": err, "current_rel_err_fp64": err64,
+                       "current_reference": "mixed-precision steady state at ||b - A x|| <= 1e-12"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_apply<FP32x2> over the batch",
                          "apply_us": sec * 1e6, "alg_bytes_per_launch": alg_bytes},

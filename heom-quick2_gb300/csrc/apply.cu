@@ -9,11 +9,23 @@
 // The higher-tier couplings have coefficients +-i and cost only additions; the
 // lower-tier ones multiply by the bath residues cb, cd.  In FP64 the kernel is
 // bounded by the FP64 pipe; in FP32 and FP32x2 by gather latency and bandwidth.
+//
+// REG selects the regularised operator of the mixed-precision inner solves (see DevCoef):
+// reads of RDO entries (source offset 0) see the Hermitian part (x_q + conj x_q')/2.
+#include <algorithm>
+
 #include "device.cuh"
 
 namespace heom {
 
-template <typename T, bool ADJ>
+template <typename T>
+__device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V *__restrict__ x, const int32_t *pair, int q)
+{
+    using N = Num<T>;
+    return N::half(N::add(N::load(x[q]), N::conj(N::load(x[__ldg(pair + q)]))));
+}
+
+template <typename T, bool ADJ, bool REG>
 __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const typename Num<T>::V *__restrict__ x,
                                                typename Num<T>::V *__restrict__ y, int64_t vstride,
                                                const int *__restrict__ active)
@@ -29,7 +41,9 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
     if (t == P.lunk) {   // the trace slot
         A s = N::zero();
         if (!ADJ && C.trace_on)
-            for (int k = 0; k < P.ntrace; k++) s = N::add(s, N::load(x[P.trace_idx[k]]));
+            for (int k = 0; k < P.ntrace; k++)
+                s = N::add(s, REG ? herm_part<T>(x, C.rdo_pair, P.trace_idx[k]) : N::load(x[P.trace_idx[k]]));
+        if (REG) s = N::add(s, N::from_d(0.0, C.reg_scale * N::im(N::load(x[t]))));
         y[t] = N::store(s);
         return;
     }
@@ -40,14 +54,24 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
     const typename N::V *hv = C.hval + (int64_t)b * P.nh;
 
     // g = sum over the drawers of (cgamma + i dipm eshift)
-    const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
-    double es = 0;
+    A g;
+    if (C.gdiag) g = N::load(C.gdiag[(int64_t)b * P.nado + n]);
+    else {
+        const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
+        double es = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) es += (double)(int8_t)(cnt >> (8 * k)) * C.eshift[b * 4 + k];
-    A g = N::scale(N::load(C.g0[n]), C.g0_scale);
-    g = N::add(g, N::from_d(0.0, es));
+        for (int k = 0; k < 4; k++) es += (double)(int8_t)(cnt >> (8 * k)) * C.eshift[b * 4 + k];
+        g = N::add(N::scale(N::load(C.g0[n]), N::sc(C.g0_scale)), N::from_d(0.0, es));
+    }
     if (ADJ) g = N::conj(g);
-    A acc = N::mul(g, N::load(x[t]));
+    const bool rdo = REG && off == 0;   // output row and same-tier sources in the RDO block
+    A acc = N::mul(g, rdo ? herm_part<T>(x, C.rdo_pair, (int)t) : N::load(x[t]));
+    if (rdo) {
+        const int q = (int)t, qp = __ldg(C.rdo_pair + q);
+        const A xq = N::load(x[q]);
+        acc = N::add(acc, N::scale(N::sub(xq, N::conj(N::load(x[qp]))), N::sc(0.5 * C.reg_scale)));
+        if (qp == q) acc = N::add(acc, N::from_d(C.reg_scale * N::re(N::load(x[P.lunk])) / C.ndiag, 0.0));
+    }
 
     // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
     const int tb = __ldg(P.cls_tptr + c) + p;
@@ -57,8 +81,8 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
         const uint32_t w = __ldg(P.terms + k);
         A h = N::load(hv[(w >> 16) & 0x7FFF]);
         if (ADJ) h = N::conj(h);
-        const A xs = N::load(x[off + (int)(w & 0xFFFF)]);
-        const A hx = C.h_real ? N::scale(xs, N::re(h)) : N::mul(h, xs);
+        const A xs = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF)) : N::load(x[off + (int)(w & 0xFFFF)]);
+        const A hx = C.h_real ? N::scale(xs, N::re_s(h)) : N::mul(h, xs);
         if (w >> 31) sr = N::add(sr, hx); else sl = N::add(sl, hx);
     }
     // forward: acc += i (sr - sl); adjoint: acc += -i (sr - sl)
@@ -75,13 +99,14 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
         const bool cj = rec.z < 0;
         const uint32_t lo = mw & 0xFFFFu, hi = mw >> 16;
         A vl = N::zero(), vr = N::zero();
+        const bool src_rdo = REG && rec.x == 0;
         if (lo) {
-            vl = N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            vl = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
             if (cj) vl = N::conj(vl);
             if (lo & 0x8000u) vl = N::neg(vl);
         }
         if (hi) {
-            vr = N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            vr = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
             if (cj) vr = N::conj(vr);
             if (hi & 0x8000u) vr = N::neg(vr);
         }
@@ -95,10 +120,35 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
             const int cid = rec.z & 0x3FFFFFFF;
             if (lo) acc = N::add(acc, N::mul(N::load(C.cl[cid]), vl));
             if (hi) acc = N::add(acc, N::mul(N::load(C.cr[cid]), vr));
+            acc = N::norm(acc);
         }
+        ua = N::norm(ua);
     }
     acc = N::add(acc, N::mul_i(ua));
     y[t] = N::store(acc);
+}
+
+template <typename T>
+__global__ void k_fill_gdiag(DevPlan P, DevCoef<T> C, typename Num<T>::V *gdiag)
+{
+    using N = Num<T>;
+    const int b = blockIdx.y;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < P.nado; n += gridDim.x * blockDim.x) {
+        const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
+        double es = 0;
+        for (int k = 0; k < 4; k++) es += (double)(int8_t)(cnt >> (8 * k)) * C.eshift[b * 4 + k];
+        const typename N::A g0 = N::load(C.g0[n]);
+        gdiag[(int64_t)b * P.nado + n] = N::store(N::from_d(C.g0_scale * N::re(g0), C.g0_scale * N::im(g0) + es));
+    }
+}
+
+template <typename T>
+void fill_gdiag(const DevPlan &P, const DevCoef<T> &C, typename Num<T>::V *gdiag, int nbatch, cudaStream_t s)
+{
+    dim3 grid((unsigned)std::max(1, std::min(1024, (P.nado + 255) / 256)), (unsigned)nbatch);
+    DevCoef<T> K = C;
+    K.gdiag = nullptr;
+    k_fill_gdiag<T><<<grid, 256, 0, s>>>(P, K, gdiag);
 }
 
 template <typename T, bool ADJ>
@@ -106,9 +156,13 @@ void launch_apply(const DevPlan &P, const DevCoef<T> &C, const typename Num<T>::
                   int nbatch, int64_t vstride, const int *active, cudaStream_t s)
 {
     dim3 grid((unsigned)((P.lunk + 1 + 255) / 256), (unsigned)nbatch);
-    k_apply<T, ADJ><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
+    if (!ADJ && C.reg) k_apply<T, false, true><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
+    else k_apply<T, ADJ, false><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
 }
 
+template void fill_gdiag<double>(const DevPlan &, const DevCoef<double> &, double2 *, int, cudaStream_t);
+template void fill_gdiag<float>(const DevPlan &, const DevCoef<float> &, float2 *, int, cudaStream_t);
+template void fill_gdiag<DF>(const DevPlan &, const DevCoef<DF> &, float4 *, int, cudaStream_t);
 template void launch_apply<double, false>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
 template void launch_apply<double, true>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
 template void launch_apply<float, false>(const DevPlan &, const DevCoef<float> &, const float2 *, float2 *, int, int64_t, const int *, cudaStream_t);

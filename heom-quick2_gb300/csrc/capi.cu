@@ -4,6 +4,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <type_traits>
+
 #include "context.cuh"
 
 namespace heom {
@@ -55,7 +57,7 @@ void PlanDev::upload(const HostPlan &P)
     auto to32 = [](const std::vector<cd> &v) { std::vector<float2> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = make_float2((float)v[k].real(), (float)v[k].imag()); return o; };
     g0_64 = upload_vec(blocks, to64(P.g0)); cl_64 = upload_vec(blocks, to64(P.cl)); cr_64 = upload_vec(blocks, to64(P.cr));
     g0_32 = upload_vec(blocks, to32(P.g0)); cl_32 = upload_vec(blocks, to32(P.cl)); cr_32 = upload_vec(blocks, to32(P.cr));
-    auto todf = [](const std::vector<cd> &v) { std::vector<float4> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = Num<DF>::store(Num<DF>::from_d(v[k].real(), v[k].imag())); return o; };
+    auto todf = [](const std::vector<cd> &v) { std::vector<float4> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = Num<DF>::store_host(Num<DF>::from_d(v[k].real(), v[k].imag())); return o; };
     g0_df = upload_vec(blocks, todf(P.g0)); cl_df = upload_vec(blocks, todf(P.cl)); cr_df = upload_vec(blocks, todf(P.cr));
     ncoef = (int64_t)P.cl.size();
 }
@@ -78,7 +80,7 @@ heom_ctx::~heom_ctx()
 {
     dfwd.release();
     dadj.release();
-    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch};
+    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch, d_rdo_pair};
     for (void *p : ptrs) if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -89,12 +91,13 @@ struct heom_batch {
     int64_t vs = 0;
     double2 *h64 = nullptr;
     float4 *hdf = nullptr;
+    float2 *h32 = nullptr;
     double *e64 = nullptr;
     int h_real = 0;
-    ~heom_batch() { if (h64) cudaFree(h64); if (hdf) cudaFree(hdf); if (e64) cudaFree(e64); }
+    ~heom_batch() { if (h64) cudaFree(h64); if (hdf) cudaFree(hdf); if (h32) cudaFree(h32); if (e64) cudaFree(e64); }
 };
 
-namespace {
+namespace heom {
 
 // H values of the context's structure from a dense hs, in the three number types
 void hvalues(heom_ctx *c, const cd *hs, std::vector<double2> &h64, std::vector<float2> &h32, std::vector<float4> &hdf, int &real)
@@ -106,7 +109,7 @@ void hvalues(heom_ctx *c, const cd *hs, std::vector<double2> &h64, std::vector<f
         cd v = hs[(size_t)c->hst.rows[k] + (size_t)c->hst.cols[k] * c->nrho];
         h64[k] = make_double2(v.real(), v.imag());
         h32[k] = make_float2((float)v.real(), (float)v.imag());
-        hdf[k] = Num<DF>::store(Num<DF>::from_d(v.real(), v.imag()));
+        hdf[k] = Num<DF>::store_host(Num<DF>::from_d(v.real(), v.imag()));
         if (v.imag() != 0.0) real = 0;
     }
 }
@@ -142,6 +145,11 @@ template <typename T> DevCoef<T> ctx_coef(heom_ctx *c, bool adj)
     return k;
 }
 
+CoefSet ctx_coefs(heom_ctx *c, bool adj)
+{
+    return CoefSet{ctx_coef<double>(c, adj), ctx_coef<float>(c, adj), ctx_coef<DF>(c, adj)};
+}
+
 void require_ctx(heom_ctx *c) { if (!c) fail(HEOM_E_ARG, "null context"); }
 
 // Hermitise the RDO part of a host rho: upper triangle defines the lower one and the
@@ -159,6 +167,39 @@ void herm_rdo(heom_ctx *c, cd *rho)
 }
 
 __global__ void k_add_real(double2 *p, double v) { p->x += v; }
+
+// Replace the RDO block of every instance by its Hermitian part and clear the free trace
+// unknown x[lunk]; thread q handles the pair (q, q') with q <= q', so the update is in place.
+__global__ void k_herm_rdo(double2 *x, int64_t vstride, int64_t lunk, int nz0, const int32_t *pair)
+{
+    double2 *xb = x + (int64_t)blockIdx.y * vstride;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nz0; q += gridDim.x * blockDim.x) {
+        const int p = pair[q];
+        if (p < q) continue;
+        const double2 a = xb[q], b = xb[p];
+        if (p == q) { xb[q].y = 0.0; continue; }
+        const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+        xb[q] = h;
+        xb[p] = make_double2(h.x, -h.y);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) xb[lunk] = make_double2(0.0, 0.0);
+}
+
+void herm_rdo_dev(heom_ctx *c, double2 *x, int nbatch, int64_t vstride)
+{
+    dim3 g((unsigned)std::max(1, std::min(64, (c->nz0 + 255) / 256)), (unsigned)nbatch);
+    k_herm_rdo<<<g, 256, 0, c->stream>>>(x, vstride, c->lunk, c->nz0, c->d_rdo_pair);
+}
+
+template <typename T> DevCoef<T> regularised(heom_ctx *c, DevCoef<T> K)
+{
+    K.reg = 1;
+    K.nz0 = c->nz0;
+    K.ndiag = c->ndiag;
+    K.rdo_pair = c->d_rdo_pair;
+    K.reg_scale = c->reg_scale;
+    return K;
+}
 
 void drandn_stream(int64_t n, std::vector<double> &out)
 {
@@ -179,7 +220,7 @@ void upload_rt(heom_ctx *c, TfqWork<T> &W)
 {
     using V = typename Num<T>::V;
     std::vector<V> rt(W.N);
-    for (int64_t i = 0; i < W.N; i++) rt[i] = Num<T>::store(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
+    for (int64_t i = 0; i < W.N; i++) rt[i] = Num<T>::store_host(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
     CK(cudaMemcpyAsync(W.rt, rt.data(), sizeof(V) * W.N, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
 }
@@ -243,11 +284,129 @@ void residual64(heom_ctx *c, const DevCoef<double> &K, const double2 *x, double2
 // ----------------------------------------------------------------------------
 namespace heom {
 
+void hvalues64(heom_ctx *c, const cd *hs, std::vector<double2> &h64)
+{
+    std::vector<float2> a;
+    std::vector<float4> b;
+    int r;
+    hvalues(c, hs, h64, a, b, r);
+}
+
+double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b)
+{
+    return device_dot(n, a, b, c->dscratch, c->stream);
+}
+
+void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, double2 *x, double crit_abs, int maxit0,
+                    heom_solve_info &info)
+{
+    const int64_t N = c->lunk + 1;
+    const int nlim = std::max(1, maxit0 / 2);
+    info = heom_solve_info{};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    TfqWork<double> W;
+    tfq_alloc<double>(W, 1, N);
+    double resid = 0;
+    try {
+        upload_rt(c, W);
+        // restarted TFQMR: each round solves op d = rhs - op(x) from d = 0 and adds d to x;
+        // a restart clears the drift between TFQMR's recursive and true residuals
+        for (int round = 0;; round++) {
+            op(x, W.s, nullptr);
+            vec_axpby<double>(N, W.b, 1.0, rhs, -1.0, W.s, c->stream);
+            resid = device_norm2(N, W.b, c->dscratch, c->stream);
+            if (resid <= crit_abs || round == 8 || info.iters >= 2 * nlim) break;
+            tfq_start<double>(W, crit_abs / resid, nlim, crit_abs, 0.0, 8, c->stream);
+            int it = 0;
+            tfq_run<double>(c, W, op, nlim, it, info.launches);
+            vec_axpby<double>(N, x, 1.0, x, 1.0, W.x, c->stream);
+            TfqState st;
+            CK(cudaMemcpy(&st, W.st, sizeof(TfqState), cudaMemcpyDeviceToHost));
+            info.iters += st.axb;
+            info.ierr = st.ierr;
+            info.refinements = round + 1;
+        }
+    } catch (...) { tfq_free(W); cudaEventDestroy(e0); cudaEventDestroy(e1); throw; }
+    tfq_free(W);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    info.resid = resid;
+    info.converged = resid <= crit_abs;
+    info.seconds = ms * 1e-3;
+}
+
+// Mixed-precision refinement: rounds of (hermitise x, FP64 residual r = rhs - A x, inner
+// TFQMR on A~ d = r / ||r|| in the number type T, x += ||r|| d) until ||r|| <= crit.  A~ is
+// the regularised operator (DevCoef::reg): it agrees with A on vectors whose RDO block is
+// Hermitian and whose trace unknown is zero, and is nonsingular where A has the null space
+// spanned by the free trace unknown and the anti-Hermitian stationary RDO directions; the
+// inner Krylov solves then stay well conditioned in low precision.
+template <typename T>
+void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, const double2 *rhs,
+                  const DevCoef<double> &K64, const DevCoef<T> &KT, double2 *r64, std::vector<double> &norms,
+                  int nlim, int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
+                  const std::function<void(const double2 *, double2 *)> &residual,
+                  const std::function<void(const double2 *)> &batch_norms)
+{
+    const int64_t N = c->lunk + 1;
+    const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-6);
+    TfqWork<T> W;
+    tfq_alloc<T>(W, nbatch, N);
+    typename Num<T>::V *gd = nullptr;
+    try {
+        upload_rt(c, W);
+        DevCoef<T> KR = regularised<T>(c, KT);
+        // per-instance ADO diagonals, so the inner applies do no FP64 arithmetic
+        CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * std::max<int64_t>(1, (int64_t)c->dfwd.view.nado * nbatch)));
+        fill_gdiag<T>(c->dfwd.view, KR, gd, nbatch, c->stream);
+        KR.gdiag = gd;
+        aux++;
+        int round = 0;
+        for (; round < std::max(1, o.max_refine); round++) {
+            if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
+            residual(x, r64);
+            batch_norms(r64);
+            bool all_ok = true;
+            for (double v : norms) all_ok = all_ok && v <= o.crit;
+            if (all_ok) { converged = true; break; }
+            for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
+                vec_from_d<T>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride,
+                              norms[b] <= o.crit ? 0.0 : 1.0 / norms[b], c->stream);
+            // the scaled inner problem has ||b|| = 1: stop at max(itol, crit / ||r||) (the most
+            // demanding instance sets it), by TFQMR's own test or the every-50-applies test, or
+            // after 4 such tests without halving the residual
+            double tgt = 1.0;
+            for (double v : norms) if (v > o.crit) tgt = std::min(tgt, o.crit / v);
+            tgt = std::max(tgt, itol);
+            tfq_start<T>(W, tgt, nlim, tgt, 0.0, 4, c->stream);
+            aux += 1 + nbatch;
+            int it = 0;
+            tfq_run<T>(c, W, make_apply<T>(c, rhs ? KT : KR, nbatch, W.vstride, false), nlim, it, launches);
+            std::vector<TfqState> st(nbatch);
+            CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
+            int axb = 0;
+            for (auto &sv : st) { axb = std::max(axb, sv.axb); last_ierr = sv.ierr; }
+            total_iters += axb;
+            for (int b = 0; b < nbatch; b++)
+                if (norms[b] > o.crit) vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.x + (int64_t)b * W.vstride, c->stream), aux++;
+        }
+        if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
+        rounds = round;
+    } catch (...) { tfq_free(W); if (gd) cudaFree(gd); throw; }
+    tfq_free(W);
+    cudaFree(gd);
+}
+
 // Solve A x = rhs (rhs = e_trace when rhs == nullptr) for nbatch instances, in FP64 or
 // mixed precision.  x: device FP64, nbatch vectors with stride vstride (vstride >= lunk+1),
 // holding the initial guess on entry.
 void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, bool adj,
-                  const double2 *rhs, heom_solve_info &info, const DevCoef<double> &K64, const DevCoef<DF> &KDF)
+                  const double2 *rhs, heom_solve_info &info, const CoefSet &K)
 {
     const int64_t N = c->lunk + 1;
     int nlim = o.maxit0 / 2;
@@ -264,68 +423,48 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     bool converged = false;
     std::vector<double> norms(nbatch, 0.0);
     int64_t aux = 0;   // launches outside the TFQMR graphs
-    auto batch_norms = [&](const double2 *v) {
+    std::function<void(const double2 *)> batch_norms = [&](const double2 *v) {
         for (int b = 0; b < nbatch; b++) norms[b] = device_norm2(N, v + (int64_t)b * vstride, c->dscratch, c->stream);
         aux += nbatch;
     };
-    auto residual = [&](const double2 *xx, double2 *r) {
-        residual64(c, K64, xx, r, nbatch, vstride, adj, rhs);
+    std::function<void(const double2 *, double2 *)> residual = [&](const double2 *xx, double2 *r) {
+        residual64(c, K.k64, xx, r, nbatch, vstride, adj, rhs);
         aux += rhs ? 2 : 2 + nbatch;
     };
-    if (o.precision == HEOM_PREC_FP64) {
-        TfqWork<double> W;
-        tfq_alloc<double>(W, nbatch, N);
-        try {
-            upload_rt(c, W);
-            // b = rhs - A x0 per instance, stored with the workspace stride
-            residual(x, r64);
-            for (int b = 0; b < nbatch; b++)
-                CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, r64 + (int64_t)b * vstride, sizeof(double2) * N, cudaMemcpyDeviceToDevice, c->stream));
-            tfq_start<double>(W, o.crit * 1e-3, nlim, o.crit, c->stream);
-            aux++;
-            int it = 0;
-            tfq_run<double>(c, W, make_apply<double>(c, K64, nbatch, W.vstride, adj), nlim, it, info.launches);
-            total_iters = it;
-            for (int b = 0; b < nbatch; b++)
-                vec_axpby<double>(N, x + (int64_t)b * vstride, 1.0, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
-            std::vector<TfqState> st(nbatch);
-            CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
-            int axb = 0;
-            for (auto &s : st) { axb = std::max(axb, s.axb); last_ierr = s.ierr; }
-            total_iters = axb;
-        } catch (...) { tfq_free(W); for (void *p : tmp) cudaFree(p); throw; }
-        tfq_free(W);
-    } else {
-        // FP32x2 TFQMR on the FP64 residual, refined in FP64 until ||b - A x|| <= crit
-        TfqWork<DF> W;
-        tfq_alloc<DF>(W, nbatch, N);
-        try {
-            upload_rt(c, W);
-            int round = 0;
-            for (; round < std::max(1, o.max_refine); round++) {
+    try {
+        if (o.precision == HEOM_PREC_FP64) {
+            TfqWork<double> W;
+            tfq_alloc<double>(W, nbatch, N);
+            try {
+                upload_rt(c, W);
+                // b = rhs - A x0 per instance, stored with the workspace stride
                 residual(x, r64);
-                batch_norms(r64);
-                bool all_ok = true;
-                for (double v : norms) all_ok = all_ok && v <= o.crit;
-                if (all_ok) { converged = true; break; }
-                for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
-                    vec_from_d<DF>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride, norms[b] <= o.crit ? 0.0 : 1.0, c->stream);
-                tfq_start<DF>(W, o.crit * 1e-3, nlim, o.crit, c->stream);
-                aux += 1 + nbatch;
+                for (int b = 0; b < nbatch; b++)
+                    CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, r64 + (int64_t)b * vstride, sizeof(double2) * N, cudaMemcpyDeviceToDevice, c->stream));
+                tfq_start<double>(W, o.crit * 1e-3, nlim, o.crit, 0.0, 0, c->stream);
+                aux++;
                 int it = 0;
-                tfq_run<DF>(c, W, make_apply<DF>(c, KDF, nbatch, W.vstride, adj), nlim, it, info.launches);
+                tfq_run<double>(c, W, make_apply<double>(c, K.k64, nbatch, W.vstride, adj), nlim, it, info.launches);
+                for (int b = 0; b < nbatch; b++)
+                    vec_axpby<double>(N, x + (int64_t)b * vstride, 1.0, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
                 std::vector<TfqState> st(nbatch);
                 CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
                 int axb = 0;
-                for (auto &s : st) { axb = std::max(axb, s.axb); last_ierr = s.ierr; }
-                total_iters += axb;
-                for (int b = 0; b < nbatch; b++)
-                    if (norms[b] > o.crit) vec_axpy_to_d<DF>(N, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
-            }
-            info.refinements = round;
-        } catch (...) { tfq_free(W); for (void *p : tmp) cudaFree(p); throw; }
-        tfq_free(W);
-    }
+                for (auto &sv : st) { axb = std::max(axb, sv.axb); last_ierr = sv.ierr; }
+                total_iters = axb;
+            } catch (...) { tfq_free(W); throw; }
+            tfq_free(W);
+        } else {
+            if (adj) fail(HEOM_E_UNSUPPORTED, "mixed precision is implemented for the forward operator");
+            if (o.precision == HEOM_PREC_MIXED)
+                mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, K.k64, K.kdf, r64, norms, nlim, total_iters, last_ierr,
+                                 converged, info.refinements, info.launches, aux, residual, batch_norms);
+            else if (o.precision == HEOM_PREC_MIXED_FP32)
+                mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, K.k64, K.k32, r64, norms, nlim, total_iters, last_ierr,
+                                    converged, info.refinements, info.launches, aux, residual, batch_norms);
+            else fail(HEOM_E_ARG, "unknown precision");
+        }
+    } catch (...) { for (void *p : tmp) cudaFree(p); cudaEventDestroy(e0); cudaEventDestroy(e1); throw; }
     // final FP64 residual
     residual(x, r64);
     batch_norms(r64);
@@ -396,6 +535,39 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
         int nz0 = t->nnz_spa[0];
         c->rdo_rows.assign(t->irow_spa, t->irow_spa + nz0);
         c->rdo_cols.assign(t->icol_spa, t->icol_spa + nz0);
+        {
+            // transposed partner of every RDO entry (the pattern of exp(-0.314 H) is symmetric)
+            std::vector<int32_t> pos((size_t)t->nrho * t->nrho, -1), pair(nz0);
+            for (int q = 0; q < nz0; q++) pos[(t->irow_spa[q] - 1) + (size_t)(t->icol_spa[q] - 1) * t->nrho] = q;
+            for (int q = 0; q < nz0; q++) {
+                pair[q] = pos[(t->icol_spa[q] - 1) + (size_t)(t->irow_spa[q] - 1) * t->nrho];
+                if (pair[q] < 0) fail(HEOM_E_ARG, "RDO sparsity pattern is not symmetric");
+                if (pair[q] == q) c->ndiag++;
+            }
+            c->nz0 = nz0;
+            CK(cudaMalloc((void **)&c->d_rdo_pair, sizeof(int32_t) * std::max(1, nz0)));
+            CK(cudaMemcpy(c->d_rdo_pair, pair.data(), sizeof(int32_t) * nz0, cudaMemcpyHostToDevice));
+            // regularising weight: the largest bath decay rate |Re cgamma|, a typical diagonal
+            // magnitude of the operator
+            int nvar = 2 * t->norbs * t->nspin * t->nalf * t->ncor;
+            const cd *cg = reinterpret_cast<const cd *>(t->cgamma);
+            double m = 0;
+            for (int k = 0; k < nvar; k++) m = std::max(m, std::abs(cg[k].real()));
+            c->reg_scale = m > 0 ? m : 1.0;
+            // Chebyshev spectral width (td/prechebyshev.f90:56-110): spread of Re(sum of the
+            // drawers' cgamma) over every ADO of the index table, the RDO (0) included
+            double lo = 0.0, hi = 0.0;
+            for (int it = 2; it <= t->ntier; it++) {
+                const int nb = it - 1;
+                for (int64_t a = t->nfirst[it - 1]; a <= t->nlast[it - 1]; a++) {
+                    const int32_t *row = t->indextable + (t->ifirst[it - 1] - 1) + (a - t->nfirst[it - 1]) * nb;
+                    double g = 0;
+                    for (int k = 0; k < nb; k++) g += cg[row[k] - 1].real();
+                    lo = std::min(lo, g); hi = std::max(hi, g);
+                }
+            }
+            c->cheby_delta = hi - lo;
+        }
         const int n = t->nrho;
         for (int s = 1; s <= t->nspin; s++)
             for (int o = 1; o <= t->norbs; o++) {
@@ -536,7 +708,7 @@ int heom_solve_tfqmr(heom_ctx *c, const heom_solve_opts *o, double _Complex *rho
         herm_rdo(c, x.data());
         CK(cudaMemcpyAsync(c->dz, x.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
         heom_solve_info inf;
-        solve_device(c, *o, c->dz, 1, N, false, nullptr, inf, ctx_coef<double>(c, false), ctx_coef<DF>(c, false));
+        solve_device(c, *o, c->dz, 1, N, false, nullptr, inf, ctx_coefs(c));
         CK(cudaMemcpyAsync(rho, c->dz, sizeof(double2) * c->lunk, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         if (info) *info = inf;
@@ -582,6 +754,7 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
         size_t nh = c->hst.rows.size();
         std::vector<double2> h64(nh * nbatch);
         std::vector<float4> hdf(nh * nbatch);
+        std::vector<float2> h32(nh * nbatch);
         std::vector<double> e64(4 * (size_t)nbatch, 0.0);
         int all_real = 1;
         for (int b = 0; b < nbatch; b++) {
@@ -591,6 +764,7 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
             all_real = all_real && real;
             std::copy(a64.begin(), a64.end(), h64.begin() + b * nh);
             std::copy(adf.begin(), adf.end(), hdf.begin() + b * nh);
+            std::copy(a32.begin(), a32.end(), h32.begin() + b * nh);
             for (int a = 0; a < c->nalf; a++)
                 for (int s = 0; s < c->nspin; s++) {
                     int slot = a + s * c->nalf;
@@ -599,6 +773,8 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
         }
         CK(cudaMalloc((void **)&B->h64, sizeof(double2) * h64.size()));
         CK(cudaMalloc((void **)&B->hdf, sizeof(float4) * hdf.size()));
+        CK(cudaMalloc((void **)&B->h32, sizeof(float2) * h32.size()));
+        CK(cudaMemcpy(B->h32, h32.data(), sizeof(float2) * h32.size(), cudaMemcpyHostToDevice));
         CK(cudaMalloc((void **)&B->e64, sizeof(double) * e64.size()));
         CK(cudaMemcpy(B->h64, h64.data(), sizeof(double2) * h64.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(B->hdf, hdf.data(), sizeof(float4) * hdf.size(), cudaMemcpyHostToDevice));
@@ -619,8 +795,9 @@ int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, h
         heom_ctx *c = B->ctx;
         DevCoef<double> K64 = c->dfwd.coef<double>(); K64.hval = B->h64; K64.eshift = B->e64; K64.h_real = B->h_real;
         DevCoef<DF> KDF = c->dfwd.coef<DF>(); KDF.hval = B->hdf; KDF.eshift = B->e64; KDF.h_real = B->h_real;
+        DevCoef<float> K32 = c->dfwd.coef<float>(); K32.hval = B->h32; K32.eshift = B->e64; K32.h_real = B->h_real;
         heom_solve_info inf;
-        solve_device(c, *o, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, K64, KDF);
+        solve_device(c, *o, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, CoefSet{K64, K32, KDF});
         if (info) *info = inf;
         if (!inf.converged) fail(HEOM_E_NOCONV, "batched TFQMR did not reach crit");
     });
@@ -692,19 +869,31 @@ int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
                 else if (precision == HEOM_PREC_MIXED) CK(cudaMemcpyAsync((float4 *)hv + b * nh, hdf.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
                 else CK(cudaMemcpyAsync((float2 *)hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
             }
+            void *gdiag = nullptr;
+            CK(cudaMalloc(&gdiag, 16 * std::max<size_t>(1, (size_t)c->dfwd.view.nado * nbatch))); blocks.push_back(gdiag);
+            if (precision == HEOM_PREC_MIXED) {
+                DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = es;
+                fill_gdiag<DF>(c->dfwd.view, K, (float4 *)gdiag, nbatch, c->stream);
+            } else if (precision == HEOM_PREC_MIXED_FP32) {
+                DevCoef<float> K = main_coef<float>(c, false); K.eshift = es;
+                fill_gdiag<float>(c->dfwd.view, K, (float2 *)gdiag, nbatch, c->stream);
+            }
             CK(cudaStreamSynchronize(c->stream));
-            // precision: 0 FP64, 1 FP32x2 (the mixed solver's apply), 2 plain FP32
+            // the apply of each solver precision: FP64, and the regularised FP32 / FP32x2 applies
+            // of the mixed-precision inner solves
             auto run = [&] {
                 if (precision == HEOM_PREC_FP64) {
                     DevCoef<double> K = main_coef<double>(c, false); K.hval = (double2 *)hv; K.eshift = es;
                     launch_apply<double, false>(c->dfwd.view, K, (double2 *)xin, (double2 *)yout, nbatch, vs, nullptr, c->stream);
                 } else if (precision == HEOM_PREC_MIXED) {
-                    DevCoef<DF> K = main_coef<DF>(c, false); K.hval = (float4 *)hv; K.eshift = es;
+                    DevCoef<DF> K = regularised<DF>(c, main_coef<DF>(c, false)); K.hval = (float4 *)hv; K.eshift = es;
+                    K.gdiag = (const float4 *)gdiag;
                     launch_apply<DF, false>(c->dfwd.view, K, (float4 *)xin, (float4 *)yout, nbatch, vs, nullptr, c->stream);
-                } else {
-                    DevCoef<float> K = main_coef<float>(c, false); K.hval = (float2 *)hv; K.eshift = es;
+                } else if (precision == HEOM_PREC_MIXED_FP32) {
+                    DevCoef<float> K = regularised<float>(c, main_coef<float>(c, false)); K.hval = (float2 *)hv; K.eshift = es;
+                    K.gdiag = (const float2 *)gdiag;
                     launch_apply<float, false>(c->dfwd.view, K, (float2 *)xin, (float2 *)yout, nbatch, vs, nullptr, c->stream);
-                }
+                } else fail(HEOM_E_ARG, "unknown precision");
             };
             cudaEvent_t e0, e1;
             CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
@@ -720,7 +909,7 @@ int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
             if (seconds) *seconds = ms * 1e-3 / reps;
             double st[9];
             heom_ctx_stats(c, st);
-            double s = precision == 2 ? 8.0 : 16.0;
+            double s = precision == HEOM_PREC_MIXED_FP32 ? 8.0 : 16.0;
             // algorithmic bytes of one launch: x read once, y written once per instance, plus the plan
             if (bytes) *bytes = nbatch * 2.0 * (double)N * s + st[8];
             cleanup();

@@ -29,6 +29,32 @@ struct CurrentTerm {
     float sign;      // sign of the a_{ms} element
 };
 
+// The coefficient sets of one operator in the three number types.
+struct CoefSet {
+    DevCoef<double> k64;
+    DevCoef<float> k32;
+    DevCoef<DF> kdf;
+};
+
+}  // namespace heom
+
+struct heom_ctx;
+
+namespace heom {
+// Shared host helpers of the C-ABI translation units.
+CoefSet ctx_coefs(heom_ctx *c, bool adj = false);
+void require_ctx(heom_ctx *c);
+void herm_rdo(heom_ctx *c, cd *rho);
+void set_params(heom_ctx *c, const std::vector<cd> &hs, const double *es);
+void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, bool adj,
+                  const double2 *rhs, heom_solve_info &info, const CoefSet &K);
+// FP64 TFQMR on op(x) = rhs for one instance (x: initial guess in, solution out), stopping
+// at ||rhs - op(x)|| <= crit_abs.
+void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, double2 *x, double crit_abs, int maxit0,
+                    heom_solve_info &info);
+// Values of a full nrho x nrho matrix on the context's H structure (FP64).
+void hvalues64(heom_ctx *c, const cd *hs, std::vector<double2> &h64);
+double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b);
 }  // namespace heom
 
 struct heom_ctx {
@@ -54,6 +80,10 @@ struct heom_ctx {
     std::vector<heom::CurrentTerm> cur_terms;
     std::vector<int32_t> occ_entry, occ_slot;       // RDO diagonal entries contributing to occ(m,s)
     std::vector<int32_t> rdo_rows, rdo_cols;        // RDO pattern (1-based)
+    int32_t *d_rdo_pair = nullptr;                  // transposed RDO entry (device)
+    int32_t nz0 = 0, ndiag = 0;
+    double reg_scale = 1.0;                         // weight of the regularising blocks
+    double cheby_delta = 0.0;                       // spectral width of the Liouville diagonal
     heom::CurrentTerm *d_cur_terms = nullptr;
     int32_t n_cur_terms = 0;
     // scratch vectors (lunk + 1 complex)

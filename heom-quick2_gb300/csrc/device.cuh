@@ -28,14 +28,29 @@ struct DevCoef {
     const V *g0 = nullptr, *cl = nullptr, *cr = nullptr;
     const V *hval = nullptr;        // nh values per instance (instance stride nh)
     const double *eshift = nullptr; // 4 lead-shift slots per instance (FP64, converted in-kernel)
+    // optional per-instance ADO diagonal g (nado per instance) precomputed from g0, g0_scale
+    // and eshift: keeps FP64 arithmetic out of the FP32 / FP32x2 kernels
+    const V *gdiag = nullptr;
     double g0_scale = 1;            // 0 switches the sum of damping rates off (derivative applies)
     int unit_on = 1;                // 0 drops the unit (higher-tier / RDO) couplings (derivative applies)
     int trace_on = 1;               // forward plan: write Tr(rho0) into the trace slot
     int h_real = 0;                 // all H values real: cheaper same-tier products
+    // Regularised operator of the inner solves of mixed precision (forward plan only):
+    // A acts on the Hermitian part of the RDO block (entries 0 .. nz0-1); its anti-Hermitian
+    // part, scaled by reg_scale, goes to the anti-Hermitian part of the RDO output, and the
+    // free trace unknown x[lunk] goes to the RDO diagonal (real part) and to Im y[lunk].
+    int reg = 0;
+    int32_t nz0 = 0, ndiag = 0;
+    const int32_t *rdo_pair = nullptr;   // index of the transposed RDO entry
+    double reg_scale = 0;
 };
 
 // y = A x (ADJ = false) or y = A^H x (ADJ = true) for nbatch instances (gridDim.y);
 // vstride = complex elements between instance vectors; active[b] == 0 skips instance b.
+// gdiag[b * nado + n] = g0_scale g0[n] + i sum_k cnt_k(n) eshift[b][k]
+template <typename T>
+void fill_gdiag(const DevPlan &P, const DevCoef<T> &C, typename Num<T>::V *gdiag, int nbatch, cudaStream_t s);
+
 template <typename T, bool ADJ>
 void launch_apply(const DevPlan &P, const DevCoef<T> &C, const typename Num<T>::V *x, typename Num<T>::V *y,
                   int nbatch, int64_t vstride, const int *active, cudaStream_t s);

@@ -4,9 +4,13 @@
 // FP32x2 arithmetic uses error-free transformations: the two-sum of Knuth (TAOCP
 // vol. 2, 4.2.2) and the FMA-based exact product (p = a*b, e = fma(a, b, -p)),
 // combined as in Dekker (Numer. Math. 18 (1971) 224) "double-length" arithmetic.
-// A value is hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits; all
-// operations run on the FP32 pipe.  The intrinsics __fadd_rn/__fmul_rn keep the
-// compiler from contracting or reassociating the compensation terms.
+// A value is hi + lo, about 48 significant bits; all operations run on the FP32 pipe.
+// Intermediate results are kept unnormalised (the sum and product skip the final
+// renormalising fast-two-sum; the error terms collect in lo), and values are
+// renormalised to |lo| <= ulp(hi)/2 when stored.  Over the few dozen operations of one
+// apply this keeps the error near 2^-48 relative while cutting the instruction count
+// of an add from 11 to 8 and of a product from 7 to 4.  The intrinsics __fadd_rn /
+// __fmul_rn keep the compiler from contracting or reassociating the compensation terms.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -22,13 +26,18 @@ template <> struct Num<double> {
     using S = double;       // real scalar used in arithmetic
     static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
     static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
+    static __host__ __device__ __forceinline__ V store_host(const A &a) { return a; }
+    static __device__ __forceinline__ A norm(A a) { return a; }
     static __host__ __device__ __forceinline__ A zero() { return make_double2(0, 0); }
     static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_double2(re, im); }
     static __device__ __forceinline__ A add(A a, A b) { return make_double2(a.x + b.x, a.y + b.y); }
     static __device__ __forceinline__ A sub(A a, A b) { return make_double2(a.x - b.x, a.y - b.y); }
     static __device__ __forceinline__ A mul(A a, A b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-    // a * (r real)
-    static __device__ __forceinline__ A scale(A a, double r) { return make_double2(a.x * r, a.y * r); }
+    // a * (r real); sc converts an FP64 scalar once, outside element loops
+    static __host__ __device__ __forceinline__ S sc(double r) { return r; }
+    static __device__ __forceinline__ A scale(A a, S r) { return make_double2(a.x * r, a.y * r); }
+    static __device__ __forceinline__ A half(A a) { return make_double2(0.5 * a.x, 0.5 * a.y); }
+    static __device__ __forceinline__ S re_s(A a) { return a.x; }
     // i * a
     static __device__ __forceinline__ A mul_i(A a) { return make_double2(-a.y, a.x); }
     static __device__ __forceinline__ A neg(A a) { return make_double2(-a.x, -a.y); }
@@ -43,12 +52,17 @@ template <> struct Num<float> {
     using S = float;
     static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
     static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
+    static __host__ __device__ __forceinline__ V store_host(const A &a) { return a; }
+    static __device__ __forceinline__ A norm(A a) { return a; }
     static __host__ __device__ __forceinline__ A zero() { return make_float2(0, 0); }
     static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_float2((float)re, (float)im); }
     static __device__ __forceinline__ A add(A a, A b) { return make_float2(a.x + b.x, a.y + b.y); }
     static __device__ __forceinline__ A sub(A a, A b) { return make_float2(a.x - b.x, a.y - b.y); }
     static __device__ __forceinline__ A mul(A a, A b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-    static __device__ __forceinline__ A scale(A a, double r) { float f = (float)r; return make_float2(a.x * f, a.y * f); }
+    static __host__ __device__ __forceinline__ S sc(double r) { return (float)r; }
+    static __device__ __forceinline__ A scale(A a, S r) { return make_float2(a.x * r, a.y * r); }
+    static __device__ __forceinline__ A half(A a) { return make_float2(0.5f * a.x, 0.5f * a.y); }
+    static __device__ __forceinline__ S re_s(A a) { return a.x; }
     static __device__ __forceinline__ A mul_i(A a) { return make_float2(-a.y, a.x); }
     static __device__ __forceinline__ A neg(A a) { return make_float2(-a.x, -a.y); }
     static __device__ __forceinline__ A conj(A a) { return make_float2(a.x, -a.y); }
@@ -77,28 +91,38 @@ __device__ __forceinline__ f2r fast_two_sum(float a, float b)
     float s = __fadd_rn(a, b);
     return {s, __fadd_rn(b, -__fadd_rn(s, -a))};
 }
+// unnormalised sum: exact two-sum of the high parts, low parts and error added in FP32
 __device__ __forceinline__ f2r f2r_add(f2r a, f2r b)
 {
     f2r s = two_sum(a.hi, b.hi);
-    float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
-    return fast_two_sum(s.hi, e);
+    return {s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
 }
 __device__ __forceinline__ f2r f2r_neg(f2r a) { return {-a.hi, -a.lo}; }
+// unnormalised product: exact product of the high parts plus the cross terms
 __device__ __forceinline__ f2r f2r_mul(f2r a, f2r b)
 {
     float p = __fmul_rn(a.hi, b.hi);
     float e = __fmaf_rn(a.hi, b.hi, -p);
     e = __fmaf_rn(a.hi, b.lo, e);
     e = __fmaf_rn(a.lo, b.hi, e);
-    return fast_two_sum(p, e);
+    return {p, e};
 }
+// renormalise to |lo| <= ulp(hi)/2
+__device__ __forceinline__ f2r f2r_norm(f2r a) { return two_sum(a.hi, a.lo); }
 
 template <> struct Num<DF> {
     using V = float4;    // (re_hi, im_hi, re_lo, im_lo)
     using A = f2c;
     using S = f2r;
     static __host__ __device__ __forceinline__ A load(const V &v) { return {{v.x, v.z}, {v.y, v.w}}; }
-    static __host__ __device__ __forceinline__ V store(const A &a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+    static __device__ __forceinline__ V store(const A &a)
+    {
+        const f2r r = f2r_norm(a.re), i = f2r_norm(a.im);
+        return make_float4(r.hi, i.hi, r.lo, i.lo);
+    }
+    static __host__ __device__ __forceinline__ V store_host(const A &a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+    // renormalise an accumulator (keeps long sums near 2^-48 relative)
+    static __device__ __forceinline__ A norm(A a) { return {two_sum(a.re.hi, a.re.lo), two_sum(a.im.hi, a.im.lo)}; }
     static __host__ __device__ __forceinline__ A zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
     static __host__ __device__ __forceinline__ A from_d(double re, double im) { return {f2r_from_d(re), f2r_from_d(im)}; }
     static __device__ __forceinline__ A add(A a, A b) { return {f2r_add(a.re, b.re), f2r_add(a.im, b.im)}; }
@@ -107,7 +131,14 @@ template <> struct Num<DF> {
     {
         return {f2r_add(f2r_mul(a.re, b.re), f2r_neg(f2r_mul(a.im, b.im))), f2r_add(f2r_mul(a.re, b.im), f2r_mul(a.im, b.re))};
     }
-    static __device__ __forceinline__ A scale(A a, double r) { f2r f = f2r_from_d(r); return {f2r_mul(a.re, f), f2r_mul(a.im, f)}; }
+    static __host__ __device__ __forceinline__ S sc(double r) { return f2r_from_d(r); }
+    static __device__ __forceinline__ A scale(A a, S r) { return {f2r_mul(a.re, r), f2r_mul(a.im, r)}; }
+    // exact halving of both parts
+    static __device__ __forceinline__ A half(A a)
+    {
+        return {{0.5f * a.re.hi, 0.5f * a.re.lo}, {0.5f * a.im.hi, 0.5f * a.im.lo}};
+    }
+    static __device__ __forceinline__ S re_s(A a) { return a.re; }
     static __device__ __forceinline__ A mul_i(A a) { return {f2r_neg(a.im), a.re}; }
     static __device__ __forceinline__ A neg(A a) { return {f2r_neg(a.re), f2r_neg(a.im)}; }
     static __device__ __forceinline__ A conj(A a) { return {a.re, f2r_neg(a.im)}; }

@@ -1,0 +1,39 @@
+// Device time propagation: shared pieces of the forward steps and the reverse pass.
+#pragma once
+#include <vector>
+
+#include "context.cuh"
+
+namespace heom {
+
+// Step counter and pulse parameters read by the device at every stage.
+struct PropClock {
+    int64_t n;          // step index (forward: 0, 1, ...; reverse: counts down)
+    int64_t dir;        // +1 forward, -1 reverse
+    double t0, dt;
+    double amp_scale;   // bias amplitude scale A (eshift = A * amps * onset(t))
+    double amps[4], tchar[4];
+};
+
+struct PropBuffers {
+    int64_t N = 0;
+    double dt = 0;
+    void *mem = nullptr;
+    std::vector<double2 *> vec;   // nvec FP64 vectors of lunk + 1 elements
+    double *es = nullptr;         // 4 lead shifts of the current stage (+4 spare)
+    PropClock *clk = nullptr;
+    double *jt = nullptr;         // recorded currents
+    PropBuffers(heom_ctx *c, int nvec, int64_t njt);
+    ~PropBuffers();
+    PropBuffers(const PropBuffers &) = delete;
+    PropBuffers &operator=(const PropBuffers &) = delete;
+};
+
+double bessel_j(int n, double x);
+double cheby_width(heom_ctx *c);
+int cheby_terms(double delta, double dt, double dpre);
+void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale);
+void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &K, PropBuffers &B, double2 *rho, double delta,
+                  const std::vector<double> &bes, bool record_current);
+
+}  // namespace heom

@@ -4,7 +4,7 @@
 // algorithm of R. W. Freund (SIAM J. Sci. Comput. 14 (1993) 470) in the column
 // roles and tolerances of tfqmr_double/dutfx.f90: 1 x, 2 b, 3 shadow r~, 4 v, 5 w,
 // 6 y, 7 d, 8 A y (u), 9 scratch (t).  Vector arithmetic runs in the number type T
-// (FP64 or FP32x2); inner products accumulate in FP64.  Each reduction ends in its
+// (FP64, FP32 or FP32x2); inner products are summed in FP64 across threads.  Each reduction ends in its
 // last thread block, which updates that instance's scalars (deterministic: partials
 // are summed in a fixed order).  Vector kernels skip instances that have finished, so
 // one launch sequence serves a batch of independent solves and can be captured in a
@@ -98,10 +98,25 @@ __device__ void advance(TfqState &S)
     schedule_check(S);
 }
 
-template <typename T> __device__ __forceinline__ double rdot(typename Num<T>::A a, typename Num<T>::A b)
-{
-    return Num<T>::re(a) * Num<T>::re(b) + Num<T>::im(a) * Num<T>::im(b);
-}
+// Per-thread accumulation of the real inner product Re(a^H b): FP64 for FP64 vectors,
+// FP32 for FP32 vectors, FP32x2 (on the FP32 pipe) for FP32x2 vectors; the per-thread
+// values are summed in FP64 across the grid.
+template <typename T> struct DotAcc {
+    double v = 0;
+    __device__ __forceinline__ void add(typename Num<T>::A a, typename Num<T>::A b)
+    { v += Num<T>::re(a) * Num<T>::re(b) + Num<T>::im(a) * Num<T>::im(b); }
+    __device__ __forceinline__ double val() const { return v; }
+};
+template <> struct DotAcc<float> {   // a few elements per thread: FP32 partial sums
+    float v = 0.f;
+    __device__ __forceinline__ void add(float2 a, float2 b) { v = fmaf(a.x, b.x, fmaf(a.y, b.y, v)); }
+    __device__ __forceinline__ double val() const { return (double)v; }
+};
+template <> struct DotAcc<DF> {
+    f2r v{0.f, 0.f};
+    __device__ __forceinline__ void add(f2c a, f2c b) { v = f2r_add(v, f2r_add(f2r_mul(a.re, b.re), f2r_mul(a.im, b.im))); }
+    __device__ __forceinline__ double val() const { return (double)v.hi + (double)v.lo; }
+};
 
 #define INST_SETUP                                  \
     using NN = Num<T>;                              \
@@ -112,24 +127,26 @@ template <typename T> __device__ __forceinline__ double rdot(typename Num<T>::A 
     const int64_t i0 = (int64_t)blockIdx.x * NT + threadIdx.x, di = (int64_t)W.nblk * NT;
 
 template <typename T>
-__global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit)
+__global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit, double rel_crit, int stag_window)
 {
     INST_SETUP
-    double bb = 0, rb = 0;
+    DotAcc<T> bb, rb;
     for (int64_t i = i0; i < W.N; i += di) {
         const AA bv = NN::load(W.b[o + i]), r = NN::load(W.rt[i]);
         const typename NN::V z = NN::store(NN::zero());
         W.x[o + i] = z; W.v[o + i] = z; W.y[o + i] = z; W.d[o + i] = z; W.u[o + i] = z;
         W.w[o + i] = NN::store(bv);
-        bb += rdot<T>(bv, bv);
-        rb += rdot<T>(r, bv);
+        bb.add(bv, bv);
+        rb.add(r, bv);
     }
     double tb, trb;
-    if (finish_reduce(W, b, bb, rb, tb, trb)) {
+    if (finish_reduce(W, b, bb.val(), rb.val(), tb, trb)) {
         TfqState s = {};
-        s.tol = tol; s.nlim = nlim; s.crit = crit;
         s.r0 = sqrt(tb);
+        s.tol = tol; s.nlim = nlim; s.stag_window = stag_window;
+        s.crit = fmax(crit, rel_crit * s.r0);
         s.ext_resid = s.r0;
+        s.best = s.r0;
         if (tol >= 1.0 || s.r0 == 0.0) { s.done = 1; s.ierr = 0; }
         else {
             s.n = 1; s.resn = 1; s.rho = 1; s.var = 0; s.eta = 0; s.tau = s.r0 * s.r0; s.ierr = 8;
@@ -148,7 +165,7 @@ __global__ void k_p1(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
-    const double beta = S->beta, xe = S->xpend;
+    const auto beta = NN::sc(S->beta), xe = NN::sc(S->xpend);
     for (int64_t i = i0; i < W.N; i += di) {
         const AA d = NN::load(W.d[o + i]);
         W.x[o + i] = NN::store(NN::add(NN::load(W.x[o + i]), NN::scale(d, xe)));
@@ -163,17 +180,23 @@ __global__ void k_chk(TfqWork<T> W)
 {
     INST_SETUP
     if (!W.act_chk[b]) return;
-    double ss = 0;
+    DotAcc<T> ss;
     for (int64_t i = i0; i < W.N; i += di) {
         const AA e = NN::sub(NN::load(W.s[o + i]), NN::load(W.b[o + i]));
-        ss += rdot<T>(e, e);
+        ss.add(e, e);
     }
     double t, dummy;
-    if (finish_reduce(W, b, ss, 0.0, t, dummy)) {
+    if (finish_reduce(W, b, ss.val(), 0.0, t, dummy)) {
         TfqState st = *S;
         st.ext_resid = sqrt(t);
         st.chk = 0;
         if (st.ext_resid <= st.crit) { st.done = 1; st.conv_ext = 1; }
+        else if (st.stag_window) {
+            // inner solve of a refinement: stop once stag_window consecutive tests fail to halve the
+            // best true residual (the arithmetic's floor), and hand back to the FP64 refinement
+            if (st.ext_resid < 0.5 * st.best) { st.best = st.ext_resid; st.stag = 0; }
+            else if (++st.stag >= st.stag_window) { st.done = 1; st.ierr = 4; }
+        }
         *S = st;
         set_flags(st, W.act_main, W.act_tres, W.act_chk, b);
     }
@@ -185,15 +208,15 @@ __global__ void k_p2(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
-    const double beta = S->beta;
-    double sg = 0;
+    const auto beta = NN::sc(S->beta);
+    DotAcc<T> sg;
     for (int64_t i = i0; i < W.N; i += di) {
         const AA v = NN::add(NN::scale(NN::load(W.v[o + i]), beta), NN::load(W.t[o + i]));
         W.v[o + i] = NN::store(v);
-        sg += rdot<T>(NN::load(W.rt[i]), v);
+        sg.add(NN::load(W.rt[i]), v);
     }
     double sigma, dummy;
-    if (finish_reduce(W, b, sg, 0.0, sigma, dummy)) {
+    if (finish_reduce(W, b, sg.val(), 0.0, sigma, dummy)) {
         TfqState s = *S;
         s.axb += 1;
         if (sigma == 0.0 || s.rho == 0.0) { s.ierr = 8; s.done = 1; }
@@ -209,16 +232,16 @@ __global__ void k_p3(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
-    const double dd = S->dd, al = S->alpha;
-    double ww = 0;
+    const auto dd = NN::sc(S->dd), al = NN::sc(S->alpha);
+    DotAcc<T> ww;
     for (int64_t i = i0; i < W.N; i += di) {
         W.d[o + i] = NN::store(NN::add(NN::load(W.y[o + i]), NN::scale(NN::load(W.d[o + i]), dd)));
         const AA w = NN::sub(NN::load(W.w[o + i]), NN::scale(NN::load(W.t[o + i]), al));
         W.w[o + i] = NN::store(w);
-        ww += rdot<T>(w, w);
+        ww.add(w, w);
     }
     double tw, dummy;
-    if (finish_reduce(W, b, ww, 0.0, tw, dummy)) {
+    if (finish_reduce(W, b, ww.val(), 0.0, tw, dummy)) {
         TfqState s = *S;
         s.var = tw / s.tau; s.cosv = 1.0 / (1.0 + s.var); s.tau = tw * s.cosv; s.eta = s.alpha * s.cosv;
         s.xpend = s.eta;
@@ -237,7 +260,7 @@ __global__ void k_tx(TfqWork<T> W)
 {
     INST_SETUP
     if (!W.act_tres[b]) return;
-    const double xe = S->xpend;
+    const auto xe = NN::sc(S->xpend);
     for (int64_t i = i0; i < W.N; i += di)
         W.x[o + i] = NN::store(NN::add(NN::load(W.x[o + i]), NN::scale(NN::load(W.d[o + i]), xe)));
 }
@@ -248,14 +271,14 @@ __global__ void k_tr(TfqWork<T> W, int second_half)
 {
     INST_SETUP
     if (!W.act_tres[b]) return;
-    double ss = 0;
+    DotAcc<T> ss;
     for (int64_t i = i0; i < W.N; i += di) {
         const AA s = NN::sub(NN::load(W.b[o + i]), NN::load(W.s[o + i]));
         W.s[o + i] = NN::store(s);
-        ss += rdot<T>(s, s);
+        ss.add(s, s);
     }
     double t, dummy;
-    if (finish_reduce(W, b, ss, 0.0, t, dummy)) {
+    if (finish_reduce(W, b, ss.val(), 0.0, t, dummy)) {
         TfqState st = *S;
         st.xpend = 0; st.axb += 1; st.tres = 0;
         st.resn = sqrt(t) / st.r0;
@@ -275,7 +298,7 @@ __global__ void k_p4(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
-    const double xe = S->xpend, al = S->alpha, vc = S->var * S->cosv;
+    const auto xe = NN::sc(S->xpend), al = NN::sc(S->alpha), vc = NN::sc(S->var * S->cosv);
     for (int64_t i = i0; i < W.N; i += di) {
         const AA d = NN::load(W.d[o + i]);
         W.x[o + i] = NN::store(NN::add(NN::load(W.x[o + i]), NN::scale(d, xe)));
@@ -291,16 +314,16 @@ __global__ void k_p5(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
-    const double al = S->alpha;
-    double ww = 0, rw = 0;
+    const auto al = NN::sc(S->alpha);
+    DotAcc<T> ww, rw;
     for (int64_t i = i0; i < W.N; i += di) {
         const AA w = NN::sub(NN::load(W.w[o + i]), NN::scale(NN::load(W.u[o + i]), al));
         W.w[o + i] = NN::store(w);
-        ww += rdot<T>(w, w);
-        rw += rdot<T>(NN::load(W.rt[i]), w);
+        ww.add(w, w);
+        rw.add(NN::load(W.rt[i]), w);
     }
     double tw, trw;
-    if (finish_reduce(W, b, ww, rw, tw, trw)) {
+    if (finish_reduce(W, b, ww.val(), rw.val(), tw, trw)) {
         TfqState s = *S;
         s.axb += 1;
         s.var = tw / s.tau; s.cosv = 1.0 / (1.0 + s.var); s.tau = tw * s.cosv; s.eta = s.alpha * s.cosv;
@@ -323,8 +346,9 @@ __global__ void k_axpby(int64_t n, typename Num<T>::V *z, double a, const typena
                         const typename Num<T>::V *y)
 {
     using NN = Num<T>;
+    const auto as = NN::sc(a), bs = NN::sc(bb);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        z[i] = NN::store(NN::add(NN::scale(NN::load(x[i]), a), NN::scale(NN::load(y[i]), bb)));
+        z[i] = NN::store(NN::add(NN::scale(NN::load(x[i]), as), NN::scale(NN::load(y[i]), bs)));
 }
 
 // conversions between FP64 vectors and the number type of a solver
@@ -349,6 +373,15 @@ __global__ void k_norm2(int64_t n, const double2 *x, double *out)
     double s = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         s += x[i].x * x[i].x + x[i].y * x[i].y;
+    double2 r = block_sum2(s, 0.0);
+    if (threadIdx.x == 0) out[blockIdx.x] = r.x;
+}
+
+__global__ void k_dot(int64_t n, const double2 *a, const double2 *b, double *out)
+{
+    double s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i].x * b[i].x + a[i].y * b[i].y;
     double2 r = block_sum2(s, 0.0);
     if (threadIdx.x == 0) out[blockIdx.x] = r.x;
 }
@@ -398,10 +431,10 @@ void tfq_free(TfqWork<T> &W)
 }
 
 template <typename T>
-void tfq_start(TfqWork<T> &W, double tol, int nlim, double crit, cudaStream_t s)
+void tfq_start(TfqWork<T> &W, double tol, int nlim, double crit, double rel_crit, int stag_window, cudaStream_t s)
 {
     dim3 g(W.nblk, W.nbatch);
-    k_init<T><<<g, NT, 0, s>>>(W, tol, nlim, crit);
+    k_init<T><<<g, NT, 0, s>>>(W, tol, nlim, crit, rel_crit, stag_window);
 }
 
 template <typename T>
@@ -457,10 +490,23 @@ double device_norm2(int64_t n, const double2 *x, double *scratch, cudaStream_t s
     return std::sqrt(t);
 }
 
+double device_dot(int64_t n, const double2 *a, const double2 *b, double *scratch, cudaStream_t s)
+{
+    int g = grid_for(n);
+    if (g > 1024) g = 1024;
+    k_dot<<<g, NT, 0, s>>>(n, a, b, scratch);
+    std::vector<double> h(g);
+    cudaMemcpyAsync(h.data(), scratch, sizeof(double) * g, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    double t = 0;
+    for (double v : h) t += v;
+    return t;
+}
+
 #define INST(T)                                                                                                 \
     template void tfq_alloc<T>(TfqWork<T> &, int, int64_t);                                                     \
     template void tfq_free<T>(TfqWork<T> &);                                                                    \
-    template void tfq_start<T>(TfqWork<T> &, double, int, double, cudaStream_t);                                \
+    template void tfq_start<T>(TfqWork<T> &, double, int, double, double, int, cudaStream_t);                   \
     template void tfq_iteration<T>(TfqWork<T> &, const ApplyFn<T> &, cudaStream_t);                             \
     template void vec_axpby<T>(int64_t, Num<T>::V *, double, const Num<T>::V *, double, const Num<T>::V *,      \
                                cudaStream_t);                                                                   \

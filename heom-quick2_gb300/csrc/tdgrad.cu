@@ -1,0 +1,206 @@
+// Gradient of a time integral of the lead current through the Chebyshev propagation
+// (td/chebyshev.f90 steps on the sparse derivative), by a reverse pass with checkpoints.
+//
+// J(A) = dt sum_{n=0}^{N-1} I_1(rho_n), rho_{n+1} = U_n rho_n, where the lead shift of step
+// n is A * amps * onset(t_n) and I_1 = Re<c, rho> is the lead-1 current.  One Chebyshev step
+// is out = sum_k a_k Q_k with Q_0 = rho, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1}
+// (a_0 = J_0, a_k = 2 J_k).  Backwards through it, with lambda = dJ/d(out):
+//     mu_{K-1} = a_{K-1} lambda,  mu_k = a_k lambda + s_{k+1} L^H mu_{k+1} + mu_{k+2},
+//     dJ/d rho = mu_0,   dJ/dA += sum_{j>=1} s_j Re<mu_j, (dL/dA) Q_{j-1}>,
+// s_1 = 1/delta, s_j = 2/delta.  dL/dA is diagonal: i sum_k cnt_k(ado) amps_k onset_k(t).
+// The forward pass stores rho every `checkpoint_every` steps; the reverse pass recomputes
+// the states of one segment from its checkpoint, then walks it backwards.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.cuh"
+#include "propagate.cuh"
+
+namespace heom {
+namespace {
+constexpr int NT = 256;
+int grid_for(int64_t n) { int64_t g = (n + NT - 1) / NT; return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g)); }
+
+// Q_k = (first ? 0 : Q_{k-2}) + s lq
+__global__ void k_qstep(int64_t n, const double2 *qm2, const double2 *lq, double2 *q, double s, int first)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 l = lq[i];
+        const double2 b = first ? make_double2(0, 0) : qm2[i];
+        q[i] = make_double2(b.x + s * l.x, b.y + s * l.y);
+    }
+}
+
+// mu_j = a lam + s_next lh + mu_{j+2} (terms present when the pointers are non-null), then
+// acc[e] += s_j d_e Re(conj(mu_j) i Q_{j-1}) with d_e = sum_k cnt_k es_k (when qprev != null)
+__global__ void k_mu(int64_t n, const DevPlan P, const double *es, const double2 *lam, double a, const double2 *lh,
+                     double s_next, const double2 *mu2, double2 *mu, const double2 *qprev, double s_j, double *acc)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 l = lam[i];
+        double2 m = make_double2(a * l.x, a * l.y);
+        if (lh) { m.x += s_next * lh[i].x; m.y += s_next * lh[i].y; }
+        if (mu2) { m.x += mu2[i].x; m.y += mu2[i].y; }
+        mu[i] = m;
+        if (qprev) {
+            const unsigned cnt = (unsigned)P.ado_cnt[P.ent_ado[i]];
+            double d = 0;
+            for (int k = 0; k < 4; k++) d += (double)(int8_t)(cnt >> (8 * k)) * es[k];
+            const double2 q = qprev[i];
+            // Re(conj(m) * i q) = m.x * (-q.y) + m.y * q.x
+            acc[i] += s_j * d * (m.y * q.x - m.x * q.y);
+        }
+    }
+}
+
+// lam = dt c + mu0
+__global__ void k_lambda(int64_t n, const double2 *c, double dt, const double2 *mu0, double2 *lam)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        lam[i] = make_double2(dt * c[i].x + mu0[i].x, dt * c[i].y + mu0[i].y);
+}
+
+__global__ void k_set_step(PropClock *clk, int64_t n) { clk->n = n; }
+
+__global__ void k_sum(int64_t n, const double *a, double *out)
+{
+    __shared__ double red[NT];
+    double s = 0;
+    for (int64_t i = threadIdx.x; i < n; i += NT) s += a[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = NT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+}  // namespace
+}  // namespace heom
+
+using namespace heom;
+
+extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t checkpoint_every,
+                                const double _Complex *rho0, double *integral, double *dintegral)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!rho0 || !integral || !dintegral || nstep < 1 || !(dt > 0)) fail(HEOM_E_ARG, "bad arguments");
+        if (!c->has_adj) fail(HEOM_E_ARG, "the context was created without the adjoint plan");
+        CK(cudaSetDevice(c->device));
+        const int ck = checkpoint_every > 0 ? checkpoint_every : 32;
+        const int64_t N = c->lunk + 1, L = c->lunk;
+        const int ns = c->nalf * c->nspin;
+        const double delta = cheby_width(c);
+        if (!(delta > 0)) fail(HEOM_E_ARG, "Chebyshev propagation needs a nonzero spectral width");
+        const int K = std::max(2, cheby_terms(delta, dt, 1e-21));
+        std::vector<double> bes(K);
+        for (int k = 0; k < K; k++) bes[k] = bessel_j(k, delta * dt);
+        const int ncp = (nstep + ck - 1) / ck;
+        // buffers: 5 propagation vectors; checkpoints; one segment of states; Q_0..Q_{K-1};
+        // 3 mu; lambda; L^H output; the current functional; the per-entry accumulator
+        PropBuffers B(c, 5, (int64_t)nstep * ns);
+        B.dt = dt;
+        std::vector<void *> blocks;
+        auto dalloc = [&](size_t bytes) { void *p = nullptr; CK(cudaMalloc(&p, bytes)); blocks.push_back(p); CK(cudaMemsetAsync(p, 0, bytes, c->stream)); return p; };
+        try {
+            const size_t vb = sizeof(double2) * (size_t)N;
+            char *cps = (char *)dalloc(vb * ncp);
+            char *seg = (char *)dalloc(vb * (ck + 1));
+            char *qs = (char *)dalloc(vb * K);
+            double2 *mu[3] = {(double2 *)dalloc(vb), (double2 *)dalloc(vb), (double2 *)dalloc(vb)};
+            double2 *lam = (double2 *)dalloc(vb), *lh = (double2 *)dalloc(vb), *cv = (double2 *)dalloc(vb);
+            double *acc = (double *)dalloc(sizeof(double) * N);
+            double *dsum = (double *)dalloc(sizeof(double));
+            auto cp = [&](int i) { return (double2 *)(cps + vb * i); };
+            auto st = [&](int i) { return (double2 *)(seg + vb * i); };
+            auto Q = [&](int k) { return (double2 *)(qs + vb * k); };
+            std::vector<cd> ch(N, 0.0);
+            for (const CurrentTerm &tm : c->cur_terms)
+                if (tm.slot % c->nalf == 0) ch[tm.entry] += cd(0.0, -2.0 * kJconst * tm.sign);
+            CK(cudaMemcpyAsync(cv, ch.data(), vb, cudaMemcpyHostToDevice, c->stream));
+            double2 *x = B.vec[4];
+            CK(cudaMemcpyAsync(x, rho0, sizeof(double2) * L, cudaMemcpyHostToDevice, c->stream));
+            PropClock h;
+            prop_clock_init(c, h, 0.0, dt, 1.0);
+            CK(cudaMemcpyAsync(B.clk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+            const CoefSet Kf = ctx_coefs(c, false), Ka = ctx_coefs(c, true);
+            // forward pass: checkpoints and currents
+            {
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t ge = nullptr;
+                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, true);
+                CK(cudaStreamEndCapture(c->stream, &g));
+                CK(cudaGraphInstantiate(&ge, g, 0));
+                cudaError_t err = cudaSuccess;
+                for (int n = 0; n < nstep && err == cudaSuccess; n++) {
+                    if (n % ck == 0) err = cudaMemcpyAsync(cp(n / ck), x, vb, cudaMemcpyDeviceToDevice, c->stream);
+                    if (err == cudaSuccess) err = cudaGraphLaunch(ge, c->stream);
+                }
+                cudaGraphExecDestroy(ge);
+                cudaGraphDestroy(g);
+                CK(err);
+            }
+            std::vector<double> jt((size_t)nstep * ns);
+            CK(cudaMemcpyAsync(jt.data(), B.jt, sizeof(double) * jt.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            double J = 0;
+            for (int n = 0; n < nstep; n++)
+                for (int s = 0; s < ns; s++)
+                    if (s % c->nalf == 0) J += dt * jt[(size_t)n * ns + s];
+            *integral = J;
+            // reverse pass
+            const DevPlan &P = c->dfwd.view, &PA = c->dadj.view;
+            DevCoef<double> KF = Kf.k64, KA = Ka.k64;
+            KF.trace_on = 0; KA.trace_on = 0;
+            KF.eshift = B.es; KA.eshift = B.es;
+            cudaStream_t s = c->stream;
+            const int gL = grid_for(L);
+            for (int sg = ncp - 1; sg >= 0; sg--) {
+                const int n0 = sg * ck, n1 = std::min(nstep, n0 + ck);
+                // recompute rho_{n0} .. rho_{n1-1}
+                CK(cudaMemcpyAsync(st(0), cp(sg), vb, cudaMemcpyDeviceToDevice, s));
+                for (int n = n0; n < n1 - 1; n++) {
+                    CK(cudaMemcpyAsync(x, st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                    k_set_step<<<1, 1, 0, s>>>(B.clk, n);
+                    enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, false);
+                    CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
+                }
+                for (int n = n1 - 1; n >= n0; n--) {
+                    k_set_step<<<1, 1, 0, s>>>(B.clk, n);
+                    k_stage_shift_ext(B.clk, 0.0, B.es, s);
+                    // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1}
+                    CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                    for (int k = 1; k < K; k++) {
+                        launch_apply<double, false>(P, KF, Q(k - 1), lh, 1, N, nullptr, s);
+                        k_qstep<<<gL, NT, 0, s>>>(L, k >= 2 ? Q(k - 2) : nullptr, lh, Q(k), k == 1 ? 1.0 / delta : 2.0 / delta, k == 1);
+                    }
+                    // mu recurrence, lambda = dJ/d rho_{n+1} (zero at n = nstep - 1)
+                    const double2 *m2 = nullptr, *m1 = nullptr;
+                    int slot = 0;
+                    for (int j = K - 1; j >= 0; j--) {
+                        double2 *mj = mu[slot];
+                        slot = (slot + 1) % 3;
+                        const double a = j == 0 ? bes[0] : 2.0 * bes[j];
+                        const double s_next = (j + 1 == 1) ? 1.0 / delta : 2.0 / delta;
+                        if (m1) launch_apply<double, true>(PA, KA, m1, lh, 1, N, nullptr, s);
+                        k_mu<<<gL, NT, 0, s>>>(L, P, B.es, lam, a, m1 ? lh : nullptr, s_next, m2, mj,
+                                               j >= 1 ? Q(j - 1) : nullptr, j == 1 ? 1.0 / delta : 2.0 / delta, acc);
+                        m2 = m1;
+                        m1 = mj;
+                    }
+                    k_lambda<<<gL, NT, 0, s>>>(L, cv, dt, m1, lam);
+                }
+                CK(cudaGetLastError());
+            }
+            k_sum<<<1, NT, 0, s>>>(L, acc, dsum);
+            double dJ = 0;
+            CK(cudaMemcpyAsync(&dJ, dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            *dintegral = dJ;
+            for (void *p : blocks) cudaFree(p);
+        } catch (...) { for (void *p : blocks) cudaFree(p); throw; }
+    });
+}

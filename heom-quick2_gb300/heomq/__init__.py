@@ -20,7 +20,7 @@ from . import models  # noqa: F401
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libheom_gb300.so")
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_FP32 = 0, 1, 2
 PROP_RK4, PROP_CHEBYSHEV = 0, 1
 ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "out of memory", -4: "unsupported",
           -5: "TFQMR breakdown", -6: "not converged", -7: "device wait timed out"}
@@ -244,6 +244,8 @@ class Context:
         o.device = device
         o.build_adjoint = int(adjoint)
         self._keep = []
+        if amps is None and tchar is None:   # the model's own pulse (getengyshift, fieldtype 0)
+            amps, tchar = model.field()
         if amps is not None:
             a = np.ascontiguousarray(amps, dtype=np.float64)
             self._keep.append(a)
@@ -288,7 +290,7 @@ class Context:
         _check(lib().heom_calc_atrx(self.h, self.lunk, x.ctypes.data, y.ctypes.data))
         return y
 
-    def solve_tfqmr(self, rho=None, crit=1e-10, maxit0=20000, precision=PREC_FP64, inner_tol=1e-4, max_refine=8,
+    def solve_tfqmr(self, rho=None, crit=1e-10, maxit0=20000, precision=PREC_FP64, inner_tol=0.0, max_refine=8,
                     check=True):
         if rho is None:
             rho = self.model.initial_guess()
@@ -301,7 +303,7 @@ class Context:
         return rho, info
 
     def solve_batch(self, rhos, hs_batch=None, eshift_batch=None, crit=1e-10, maxit0=20000, precision=PREC_FP64,
-                    inner_tol=1e-4, max_refine=8):
+                    inner_tol=0.0, max_refine=8):
         rhos = np.ascontiguousarray(rhos, dtype=np.complex128).copy()
         nb = rhos.shape[0]
         hs = None if hs_batch is None else _c128(hs_batch)
@@ -384,8 +386,8 @@ class Batch:
         self.h = h
         self.stride = lib().heom_batch_stride(h)
 
-    def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, max_refine=3, check=True):
-        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=0.0, max_refine=max_refine)
+    def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True):
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine)
         info = SolveInfo()
         rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
         if check:

@@ -37,7 +37,12 @@ enum {
 };
 
 /* Precision of the steady-state solver. */
-enum { HEOM_PREC_FP64 = 0, HEOM_PREC_MIXED = 1 };
+/* Solver precision.  MIXED: inner TFQMR in FP32x2 (double-float, about 48 significant
+ * bits, on the FP32 pipe) on a regularised operator, refined with FP64 residuals.
+ * MIXED_FP32: the same with plain FP32 inner arithmetic; it converges only where the
+ * operator's conditioning times 6e-8 stays well below one (the single-orbital model at
+ * T = 0.1 does, the double dot does not). */
+enum { HEOM_PREC_FP64 = 0, HEOM_PREC_MIXED = 1, HEOM_PREC_MIXED_FP32 = 2 };
 
 /* View of the module data the reference keeps for the sparse path
  * (module/matmod.f90:4-52, module/sparsemod.f90:34-42, include/common).  The
@@ -141,8 +146,10 @@ int heom_calc_ax_fp32_dev(heom_ctx *ctx, const void *dx, void *dy);
 typedef struct {
     double crit;              /* ||b - A x|| target (reference $converge crit) */
     int32_t maxit0;           /* reference maxit0 (TFQMR limit = maxit0/2) */
-    int32_t precision;        /* HEOM_PREC_FP64 or HEOM_PREC_MIXED */
-    double inner_tol;         /* MIXED: relative residual of each FP32 inner solve */
+    int32_t precision;        /* HEOM_PREC_FP64, HEOM_PREC_MIXED or HEOM_PREC_MIXED_FP32 */
+    double inner_tol;         /* MIXED*: an inner solve stops at ||r|| <= max(crit, inner_tol ||r0||),
+                                 r0 its FP64 right-hand side; <= 0 selects the default
+                                 (1e-6 for MIXED, 1e-2 for MIXED_FP32) */
     int32_t max_refine;       /* MIXED: outer refinement rounds */
 } heom_solve_opts;
 
@@ -213,9 +220,10 @@ int64_t heom_batch_stride(const heom_batch *b);
 int heom_batch_solve_dev(heom_batch *b, const heom_solve_opts *o, void *x_dev, heom_solve_info *info);
 void heom_batch_destroy(heom_batch *b);
 
-/* Measurement hook: time `reps` back-to-back applies on `nbatch` instances on device
- * (precision 0 FP64, 1 FP32x2 as used by the mixed solver, 2 plain FP32) and return the
- * average kernel time in seconds and the algorithmic bytes of one launch. */
+/* Measurement hook: time `reps` back-to-back applies on `nbatch` instances on device, in
+ * the form each solver precision uses (HEOM_PREC_FP64: the FP64 apply; HEOM_PREC_MIXED and
+ * HEOM_PREC_MIXED_FP32: the regularised FP32x2 / FP32 apply of the inner solves), and
+ * return the average kernel time in seconds and the algorithmic bytes of one launch. */
 int heom_bench_apply(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
 
 /* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs

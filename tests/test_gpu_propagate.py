@@ -1,0 +1,62 @@
+"""Time propagation on the GPU against the oracle: RK4 (td/intstp.f90) and Chebyshev
+(td/chebyshev.f90) steps of the sparse derivative (calcderiv_spa_omp) under a step bias
+switched on at t = 0+, with the lead currents of td/calcj.f90 at every step."""
+import numpy as np
+import pytest
+
+import configs as cf
+import heomq
+import oracle_ffi as of
+
+pytestmark = pytest.mark.gpu
+
+CASES = {"siam_L2": cf.siam(ntier=3, nmats=2), "dqd_L2": cf.dqd(ntier=3, nmats=2),
+         "siam_L2_onset": cf.siam(ntier=3, nmats=2, tchar=0.3)}
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_rk4_matches_oracle(name):
+    cfg = CASES[name]
+    m, ref = heomq.Model(cfg), of.Model(cfg)
+    ctx = heomq.Context(m)
+    rho0 = m.initial_guess()
+    dt, nstep = 0.05, 6
+    rho, jt = ctx.propagate(rho0, 0.0, dt, nstep, method=heomq.PROP_RK4, currents=True)
+    r = rho0.copy()
+    for n in range(nstep):
+        np.testing.assert_allclose(jt[n], ref.current(r).T.reshape(-1), rtol=1e-11, atol=1e-9)
+        r = ref.rk4_step(n * dt, dt, r)
+    assert _rel(rho, r) < 1e-12
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_chebyshev_matches_oracle(name):
+    cfg = CASES[name]
+    m, ref = heomq.Model(cfg), of.Model(cfg)
+    ctx = heomq.Context(m)
+    rho0 = m.initial_guess()
+    dt, nstep = 0.05, 4
+    delta = ref.cheby_delta()
+    nterms = of.cheby_nterms(delta, dt)
+    rho, jt = ctx.propagate(rho0, 0.0, dt, nstep, method=heomq.PROP_CHEBYSHEV, currents=True)
+    r = rho0.copy()
+    for n in range(nstep):
+        np.testing.assert_allclose(jt[n], ref.current(r).T.reshape(-1), rtol=1e-11, atol=1e-9)
+        r = ref.cheby_step(n * dt, delta, nterms, dt, r)
+    assert _rel(rho, r) < 1e-11
+
+
+def test_long_chebyshev_run_relaxes_to_the_steady_state():
+    """After the bias step the current relaxes to the TFQMR steady-state value."""
+    cfg = cf.siam(ntier=3, nmats=2, V=0.4)
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m)
+    rho_ss, _ = ctx.solve_tfqmr(crit=1e-10)
+    rho, jt = ctx.propagate(m.initial_guess(), 0.0, 0.05, 800, method=heomq.PROP_CHEBYSHEV, currents=True)
+    i_ss = ctx.current(rho_ss)[0].sum()
+    i_t = ctx.current(rho)[0].sum()
+    assert abs(i_t / i_ss - 1) < 1e-3

@@ -134,3 +134,20 @@ def test_coupling_rows_link_neighbouring_tiers():
                 assert n + 1 in rows[tgt]
                 direct += 1
     assert direct > 0
+
+
+@pytest.mark.parametrize("cfg, nunk, lall", [
+    (cf.siam(ntier=3, nmats=4), 481, None),
+    (cf.CFG0, 6221, 37360),
+    (cf.siam(ntier=5, nmats=4), 70251, 523080),
+    (cf.CFG1, 30453, 223904),
+    (cf.CFG4, 7477, 28980),
+], ids=["siam_L2", "siam_L3", "siam_L4", "dqd_L4", "hund_L2"])
+def test_stored_sizes_match_an_independent_count(cfg, nunk, lall):
+    """Stored ADO and coupling-entry counts of the reference's table rules, as counted by
+    a separate restatement of ball2drawer / buildcoefindex (Hermitian-conjugate halves
+    kept once, repeated drawers kept, lscreen dropping decoupled operators)."""
+    m = heomq.Model(cfg)
+    assert m.nunk == nunk
+    if lall is not None:
+        assert m.lall == lall
