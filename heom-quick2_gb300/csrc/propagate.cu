@@ -119,6 +119,11 @@ int cheby_terms(double delta, double dt, double dpre)
     return n;
 }
 
+void stage_shift(const PropClock *clk, double frac, double *es, cudaStream_t s)
+{
+    k_stage_shift<<<1, 32, 0, s>>>(clk, frac, es);
+}
+
 void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale)
 {
     h.n = 0;

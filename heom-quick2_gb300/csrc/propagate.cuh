@@ -33,6 +33,8 @@ double bessel_j(int n, double x);
 double cheby_width(heom_ctx *c);
 int cheby_terms(double delta, double dt, double dpre);
 void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale);
+// es = eshift at t0 + (n + frac) dt, n read from the device clock
+void stage_shift(const PropClock *clk, double frac, double *es, cudaStream_t s);
 void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &K, PropBuffers &B, double2 *rho, double delta,
                   const std::vector<double> &bes, bool record_current);
 

@@ -170,7 +170,7 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
                 }
                 for (int n = n1 - 1; n >= n0; n--) {
                     k_set_step<<<1, 1, 0, s>>>(B.clk, n);
-                    k_stage_shift_ext(B.clk, 0.0, B.es, s);
+                    stage_shift(B.clk, 0.0, B.es, s);
                     // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1}
                     CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
                     for (int k = 1; k < K; k++) {
