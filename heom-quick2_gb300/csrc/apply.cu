@@ -13,6 +13,7 @@
 // REG selects the regularised operator of the mixed-precision inner solves (see DevCoef):
 // reads of RDO entries (source offset 0) see the Hermitian part (x_q + conj x_q')/2.
 #include <algorithm>
+#include <type_traits>
 
 #include "device.cuh"
 
@@ -36,8 +37,9 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
     if (active && !active[b]) return;
     x += (int64_t)b * vstride;
     y += (int64_t)b * vstride;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t > P.lunk) return;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid > P.lunk) return;
+    const int64_t t = (tid < P.lunk && P.order) ? (int64_t)__ldg(P.order + tid) : tid;
     if (t == P.lunk) {   // the trace slot
         A s = N::zero();
         if (!ADJ && C.trace_on)
@@ -156,8 +158,12 @@ void launch_apply(const DevPlan &P, const DevCoef<T> &C, const typename Num<T>::
                   int nbatch, int64_t vstride, const int *active, cudaStream_t s)
 {
     dim3 grid((unsigned)((P.lunk + 1 + 255) / 256), (unsigned)nbatch);
-    if (!ADJ && C.reg) k_apply<T, false, true><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
-    else k_apply<T, ADJ, false><<<grid, 256, 0, s>>>(P, C, x, y, vstride, active);
+    // the work-profile order pays in FP64 (FP64-pipe bound: divergence costs issue slots);
+    // the FP32 / FP32x2 kernels keep entry order for coalesced entry, map and output access
+    DevPlan Q = P;
+    if (!std::is_same<T, double>::value) Q.order = nullptr;
+    if (!ADJ && C.reg) k_apply<T, false, true><<<grid, 256, 0, s>>>(Q, C, x, y, vstride, active);
+    else k_apply<T, ADJ, false><<<grid, 256, 0, s>>>(Q, C, x, y, vstride, active);
 }
 
 template void fill_gdiag<double>(const DevPlan &, const DevCoef<double> &, double2 *, int, cudaStream_t);

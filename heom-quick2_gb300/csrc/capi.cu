@@ -1,4 +1,5 @@
 // extern "C" entry points of the GB300 HEOM library (declared in include/heom_gb300.h).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -53,6 +54,25 @@ void PlanDev::upload(const HostPlan &P)
     std::vector<int4> coup(P.coup.size());
     for (size_t k = 0; k < coup.size(); k++) coup[k] = make_int4(P.coup[k].src_off, P.coup[k].map_base, P.coup[k].cid, 0);
     view.coup = upload_vec(blocks, coup);
+    {
+        // work profile of every entry: couplings of its ADO, nonzero gather words, same-tier
+        // terms; a stable sort by profile (then class and position) makes warps uniform
+        std::vector<uint64_t> key(P.lunk);
+        for (int64_t e = 0; e < P.lunk; e++) {
+            const int32_t a = P.ent_ado[e], p = (int32_t)(e - P.ado_off[a]), c = P.ado_cls[a];
+            const int32_t ncp = P.coup_ptr[a + 1] - P.coup_ptr[a];
+            int32_t used = 0;
+            for (int32_t k = P.coup_ptr[a]; k < P.coup_ptr[a + 1]; k++) used += P.maps[P.coup[k].map_base + p] != 0;
+            const int32_t tb = P.cls_tptr[c] + p;
+            const int32_t nt = P.term_ptr[tb + 1] - P.term_ptr[tb];
+            key[e] = ((uint64_t)std::min(ncp, 255) << 56) | ((uint64_t)std::min(used, 255) << 48) |
+                     ((uint64_t)std::min(nt, 255) << 40) | ((uint64_t)std::min(c, 65535) << 24) | (uint64_t)std::min(p, 16777215);
+        }
+        std::vector<int32_t> order(P.lunk);
+        for (int64_t e = 0; e < P.lunk; e++) order[e] = (int32_t)e;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+        view.order = upload_vec(blocks, order);
+    }
     auto to64 = [](const std::vector<cd> &v) { std::vector<double2> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = make_double2(v[k].real(), v[k].imag()); return o; };
     auto to32 = [](const std::vector<cd> &v) { std::vector<float2> o(v.size()); for (size_t k = 0; k < v.size(); k++) o[k] = make_float2((float)v[k].real(), (float)v[k].imag()); return o; };
     g0_64 = upload_vec(blocks, to64(P.g0)); cl_64 = upload_vec(blocks, to64(P.cl)); cr_64 = upload_vec(blocks, to64(P.cr));
@@ -251,7 +271,7 @@ void tfq_run(heom_ctx *c, TfqWork<T> &W, const ApplyFn<T> &apply, int nlim, int 
     cudaGraphExecDestroy(ge);
     cudaGraphDestroy(g);
     iters_out = launched;
-    launches += (int64_t)launched * 15;   // kernels of one tfq_iteration
+    launches += (int64_t)launched * kTfqIterationLaunches;
 }
 
 template <typename T>
@@ -383,8 +403,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             double tgt = 1.0;
             for (double v : norms) if (v > o.crit) tgt = std::min(tgt, o.crit / v);
             tgt = std::max(tgt, itol);
-            tfq_start<T>(W, tgt, nlim, tgt, 0.0, 4, c->stream);
-            aux += 1 + nbatch;
+            tfq_start<T>(W, tgt, nlim, tgt, 0.0, o.stag_window > 0 ? o.stag_window : 4, c->stream);
+            aux += kTfqStartLaunches + nbatch;
             int it = 0;
             tfq_run<T>(c, W, make_apply<T>(c, rhs ? KT : KR, nbatch, W.vstride, false), nlim, it, launches);
             std::vector<TfqState> st(nbatch);
@@ -442,7 +462,7 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                 for (int b = 0; b < nbatch; b++)
                     CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, r64 + (int64_t)b * vstride, sizeof(double2) * N, cudaMemcpyDeviceToDevice, c->stream));
                 tfq_start<double>(W, o.crit * 1e-3, nlim, o.crit, 0.0, 0, c->stream);
-                aux++;
+                aux += kTfqStartLaunches;
                 int it = 0;
                 tfq_run<double>(c, W, make_apply<double>(c, K.k64, nbatch, W.vstride, adj), nlim, it, info.launches);
                 for (int b = 0; b < nbatch; b++)
@@ -459,6 +479,9 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             if (o.precision == HEOM_PREC_MIXED)
                 mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, K.k64, K.kdf, r64, norms, nlim, total_iters, last_ierr,
                                  converged, info.refinements, info.launches, aux, residual, batch_norms);
+            else if (o.precision == HEOM_PREC_FP64_REFINED)
+                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, K.k64, K.k64, r64, norms, nlim, total_iters, last_ierr,
+                                     converged, info.refinements, info.launches, aux, residual, batch_norms);
             else if (o.precision == HEOM_PREC_MIXED_FP32)
                 mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, K.k64, K.k32, r64, norms, nlim, total_iters, last_ierr,
                                     converged, info.refinements, info.launches, aux, residual, batch_norms);

@@ -19,6 +19,9 @@ struct DevPlan {
     const int32_t *coup_ptr = nullptr, *cls_tptr = nullptr, *term_ptr = nullptr, *trace_idx = nullptr;
     const int4 *coup = nullptr;
     const uint32_t *maps = nullptr, *terms = nullptr;
+    // thread -> entry order: entries grouped by their work profile (couplings, useful
+    // gathers, same-tier terms) so that the threads of a warp follow the same trip counts
+    const int32_t *order = nullptr;
 };
 
 // Parameter set of one apply: coefficient tables, per-instance H values and lead shifts.

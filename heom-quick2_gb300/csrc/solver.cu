@@ -43,35 +43,30 @@ __device__ __forceinline__ double2 block_sum2(double a, double c)
     return r;   // valid in thread 0
 }
 
-// Returns true in thread 0 of the last block of instance b, with the grand totals.
+// Per-block partial sums of a reduction (written by thread 0; no atomics, no fences).
 template <typename T>
-__device__ bool finish_reduce(const TfqWork<T> &W, int b, double a, double c, double &ta, double &tc)
+__device__ void write_partial(const TfqWork<T> &W, int b, double a, double c)
 {
-    __shared__ int am_last;
-    double2 r = block_sum2(a, c);
+    const double2 r = block_sum2(a, c);
     if (threadIdx.x == 0) {
         double *pp = W.part + 2 * ((size_t)b * W.nblk + blockIdx.x);
         pp[0] = r.x;
         pp[1] = r.y;
-        __threadfence();
-        unsigned tk = atomicAdd(W.cnt + b, 1u);
-        am_last = (tk == (unsigned)W.nblk - 1);
     }
-    __syncthreads();
-    if (!am_last) return false;
-    __threadfence();
+}
+
+// In the one-block-per-instance kernel that follows a reduction: the grand totals, summed
+// in a fixed order (deterministic), valid in thread 0.
+template <typename T>
+__device__ bool gather_partials(const TfqWork<T> &W, int b, double &ta, double &tc)
+{
     double sa = 0, sc = 0;
     for (int k = threadIdx.x; k < W.nblk; k += NT) {
-        sa += __ldcg(W.part + 2 * ((size_t)b * W.nblk + k));
-        sc += __ldcg(W.part + 2 * ((size_t)b * W.nblk + k) + 1);
+        sa += W.part[2 * ((size_t)b * W.nblk + k)];
+        sc += W.part[2 * ((size_t)b * W.nblk + k) + 1];
     }
-    r = block_sum2(sa, sc);
-    if (threadIdx.x == 0) {
-        W.cnt[b] = 0;
-        ta = r.x;
-        tc = r.y;
-        return true;
-    }
+    const double2 r = block_sum2(sa, sc);
+    if (threadIdx.x == 0) { ta = r.x; tc = r.y; return true; }
     return false;
 }
 
@@ -126,6 +121,16 @@ template <> struct DotAcc<DF> {
     const int64_t o = (int64_t)b * W.vstride;       \
     const int64_t i0 = (int64_t)blockIdx.x * NT + threadIdx.x, di = (int64_t)W.nblk * NT;
 
+// restrict-qualified views of this instance's vectors: lets the compiler overlap the loads
+// of successive elements with the stores of earlier ones
+#define VIEWS                                                               \
+    using VV = typename NN::V;                                              \
+    VV *__restrict__ x_ = W.x + o, *__restrict__ v_ = W.v + o, *__restrict__ w_ = W.w + o; \
+    VV *__restrict__ y_ = W.y + o, *__restrict__ d_ = W.d + o, *__restrict__ s_ = W.s + o; \
+    const VV *__restrict__ u_ = W.u + o, *__restrict__ t_ = W.t + o;      \
+    const VV *__restrict__ b_ = W.b + o, *__restrict__ rt_ = W.rt;        \
+    (void)x_; (void)v_; (void)w_; (void)y_; (void)d_; (void)s_; (void)u_; (void)t_; (void)b_; (void)rt_;
+
 template <typename T>
 __global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit, double rel_crit, int stag_window)
 {
@@ -139,8 +144,17 @@ __global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit, double r
         bb.add(bv, bv);
         rb.add(r, bv);
     }
+    write_partial(W, b, bb.val(), rb.val());
+}
+
+template <typename T>
+__global__ void k_init_fin(TfqWork<T> W, double tol, int nlim, double crit, double rel_crit, int stag_window)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
     double tb, trb;
-    if (finish_reduce(W, b, bb.val(), rb.val(), tb, trb)) {
+    if (gather_partials(W, b, tb, trb)) {
         TfqState s = {};
         s.r0 = sqrt(tb);
         s.tol = tol; s.nlim = nlim; s.stag_window = stag_window;
@@ -159,18 +173,19 @@ __global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit, double r
     }
 }
 
-// x += xpend d; v = beta v + u; y = w + beta y
+// x += xpend d; y = w + beta y   (the v update of this half step is done in k_p2)
 template <typename T>
 __global__ void k_p1(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
+    VIEWS
     const auto beta = NN::sc(S->beta), xe = NN::sc(S->xpend);
+#pragma unroll 2
     for (int64_t i = i0; i < W.N; i += di) {
-        const AA d = NN::load(W.d[o + i]);
-        W.x[o + i] = NN::store(NN::add(NN::load(W.x[o + i]), NN::scale(d, xe)));
-        W.v[o + i] = NN::store(NN::add(NN::scale(NN::load(W.v[o + i]), beta), NN::load(W.u[o + i])));
-        W.y[o + i] = NN::store(NN::add(NN::load(W.w[o + i]), NN::scale(NN::load(W.y[o + i]), beta)));
+        const AA d = NN::load(d_[i]);
+        x_[i] = NN::store(NN::add(NN::load(x_[i]), NN::scale(d, xe)));
+        y_[i] = NN::store(NN::add(NN::load(w_[i]), NN::scale(NN::load(y_[i]), beta)));
     }
 }
 
@@ -185,8 +200,18 @@ __global__ void k_chk(TfqWork<T> W)
         const AA e = NN::sub(NN::load(W.s[o + i]), NN::load(W.b[o + i]));
         ss.add(e, e);
     }
+    write_partial(W, b, ss.val(), 0.0);
+}
+
+template <typename T>
+__global__ void k_chk_fin(TfqWork<T> W)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
+    if (!W.act_chk[b]) return;
     double t, dummy;
-    if (finish_reduce(W, b, ss.val(), 0.0, t, dummy)) {
+    if (gather_partials(W, b, t, dummy)) {
         TfqState st = *S;
         st.ext_resid = sqrt(t);
         st.chk = 0;
@@ -202,21 +227,34 @@ __global__ void k_chk(TfqWork<T> W)
     }
 }
 
-// v = beta v + t; sigma = <r~, v>
+// v = beta (beta v + u) + t; sigma = <r~, v>   (u = A y of the previous half step)
 template <typename T>
 __global__ void k_p2(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
+    VIEWS
     const auto beta = NN::sc(S->beta);
     DotAcc<T> sg;
+#pragma unroll 2
     for (int64_t i = i0; i < W.N; i += di) {
-        const AA v = NN::add(NN::scale(NN::load(W.v[o + i]), beta), NN::load(W.t[o + i]));
-        W.v[o + i] = NN::store(v);
-        sg.add(NN::load(W.rt[i]), v);
+        const AA vu = NN::add(NN::scale(NN::load(v_[i]), beta), NN::load(u_[i]));
+        const AA v = NN::add(NN::scale(vu, beta), NN::load(t_[i]));
+        v_[i] = NN::store(v);
+        sg.add(NN::load(rt_[i]), v);
     }
+    write_partial(W, b, sg.val(), 0.0);
+}
+
+template <typename T>
+__global__ void k_p2_fin(TfqWork<T> W)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
+    if (S->done) return;
     double sigma, dummy;
-    if (finish_reduce(W, b, sg.val(), 0.0, sigma, dummy)) {
+    if (gather_partials(W, b, sigma, dummy)) {
         TfqState s = *S;
         s.axb += 1;
         if (sigma == 0.0 || s.rho == 0.0) { s.ierr = 8; s.done = 1; }
@@ -232,16 +270,28 @@ __global__ void k_p3(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
+    VIEWS
     const auto dd = NN::sc(S->dd), al = NN::sc(S->alpha);
     DotAcc<T> ww;
+#pragma unroll 2
     for (int64_t i = i0; i < W.N; i += di) {
-        W.d[o + i] = NN::store(NN::add(NN::load(W.y[o + i]), NN::scale(NN::load(W.d[o + i]), dd)));
-        const AA w = NN::sub(NN::load(W.w[o + i]), NN::scale(NN::load(W.t[o + i]), al));
-        W.w[o + i] = NN::store(w);
+        d_[i] = NN::store(NN::add(NN::load(y_[i]), NN::scale(NN::load(d_[i]), dd)));
+        const AA w = NN::sub(NN::load(w_[i]), NN::scale(NN::load(t_[i]), al));
+        w_[i] = NN::store(w);
         ww.add(w, w);
     }
+    write_partial(W, b, ww.val(), 0.0);
+}
+
+template <typename T>
+__global__ void k_p3_fin(TfqWork<T> W)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
+    if (S->done) return;
     double tw, dummy;
-    if (finish_reduce(W, b, ww.val(), 0.0, tw, dummy)) {
+    if (gather_partials(W, b, tw, dummy)) {
         TfqState s = *S;
         s.var = tw / s.tau; s.cosv = 1.0 / (1.0 + s.var); s.tau = tw * s.cosv; s.eta = s.alpha * s.cosv;
         s.xpend = s.eta;
@@ -277,8 +327,18 @@ __global__ void k_tr(TfqWork<T> W, int second_half)
         W.s[o + i] = NN::store(s);
         ss.add(s, s);
     }
+    write_partial(W, b, ss.val(), 0.0);
+}
+
+template <typename T>
+__global__ void k_tr_fin(TfqWork<T> W, int second_half)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
+    if (!W.act_tres[b]) return;
     double t, dummy;
-    if (finish_reduce(W, b, ss.val(), 0.0, t, dummy)) {
+    if (gather_partials(W, b, t, dummy)) {
         TfqState st = *S;
         st.xpend = 0; st.axb += 1; st.tres = 0;
         st.resn = sqrt(t) / st.r0;
@@ -298,13 +358,15 @@ __global__ void k_p4(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
+    VIEWS
     const auto xe = NN::sc(S->xpend), al = NN::sc(S->alpha), vc = NN::sc(S->var * S->cosv);
+#pragma unroll 2
     for (int64_t i = i0; i < W.N; i += di) {
-        const AA d = NN::load(W.d[o + i]);
-        W.x[o + i] = NN::store(NN::add(NN::load(W.x[o + i]), NN::scale(d, xe)));
-        const AA y = NN::sub(NN::load(W.y[o + i]), NN::scale(NN::load(W.v[o + i]), al));
-        W.y[o + i] = NN::store(y);
-        W.d[o + i] = NN::store(NN::add(y, NN::scale(d, vc)));
+        const AA d = NN::load(d_[i]);
+        x_[i] = NN::store(NN::add(NN::load(x_[i]), NN::scale(d, xe)));
+        const AA y = NN::sub(NN::load(y_[i]), NN::scale(NN::load(v_[i]), al));
+        y_[i] = NN::store(y);
+        d_[i] = NN::store(NN::add(y, NN::scale(d, vc)));
     }
 }
 
@@ -314,16 +376,28 @@ __global__ void k_p5(TfqWork<T> W)
 {
     INST_SETUP
     if (S->done) return;
+    VIEWS
     const auto al = NN::sc(S->alpha);
     DotAcc<T> ww, rw;
+#pragma unroll 2
     for (int64_t i = i0; i < W.N; i += di) {
-        const AA w = NN::sub(NN::load(W.w[o + i]), NN::scale(NN::load(W.u[o + i]), al));
-        W.w[o + i] = NN::store(w);
+        const AA w = NN::sub(NN::load(w_[i]), NN::scale(NN::load(u_[i]), al));
+        w_[i] = NN::store(w);
         ww.add(w, w);
-        rw.add(NN::load(W.rt[i]), w);
+        rw.add(NN::load(rt_[i]), w);
     }
+    write_partial(W, b, ww.val(), rw.val());
+}
+
+template <typename T>
+__global__ void k_p5_fin(TfqWork<T> W)
+{
+    const int b = blockIdx.x;
+    TfqState *S = W.st + b;
+    (void)S;
+    if (S->done) return;
     double tw, trw;
-    if (finish_reduce(W, b, ww.val(), rw.val(), tw, trw)) {
+    if (gather_partials(W, b, tw, trw)) {
         TfqState s = *S;
         s.axb += 1;
         s.var = tw / s.tau; s.cosv = 1.0 / (1.0 + s.var); s.tau = tw * s.cosv; s.eta = s.alpha * s.cosv;
@@ -397,6 +471,7 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N)
     W.nbatch = nbatch;
     W.N = N;
     W.vstride = (N + 63) / 64 * 64;
+    // about four elements per thread and instance, at most 296 blocks (2 per SM) per instance
     int64_t nb = (N + 4 * NT - 1) / (4 * NT);
     W.nblk = (int)(nb < 1 ? 1 : (nb > 296 ? 296 : nb));
     size_t vbytes = sizeof(V) * (size_t)W.vstride * nbatch;
@@ -435,27 +510,35 @@ void tfq_start(TfqWork<T> &W, double tol, int nlim, double crit, double rel_crit
 {
     dim3 g(W.nblk, W.nbatch);
     k_init<T><<<g, NT, 0, s>>>(W, tol, nlim, crit, rel_crit, stag_window);
+    k_init_fin<T><<<W.nbatch, NT, 0, s>>>(W, tol, nlim, crit, rel_crit, stag_window);
 }
 
 template <typename T>
 void tfq_iteration(TfqWork<T> &W, const ApplyFn<T> &apply, cudaStream_t s)
 {
     dim3 g(W.nblk, W.nbatch);
+    const unsigned nb = (unsigned)W.nbatch;
     k_p1<T><<<g, NT, 0, s>>>(W);
     apply(W.x, W.s, W.act_chk);            // residual test every 50 applies
     k_chk<T><<<g, NT, 0, s>>>(W);
+    k_chk_fin<T><<<nb, NT, 0, s>>>(W);
     apply(W.y, W.t, W.act_main);           // t = A y_{2n-1}
     k_p2<T><<<g, NT, 0, s>>>(W);
+    k_p2_fin<T><<<nb, NT, 0, s>>>(W);
     k_p3<T><<<g, NT, 0, s>>>(W);
+    k_p3_fin<T><<<nb, NT, 0, s>>>(W);
     k_tx<T><<<g, NT, 0, s>>>(W);
     apply(W.x, W.s, W.act_tres);
     k_tr<T><<<g, NT, 0, s>>>(W, 0);
+    k_tr_fin<T><<<nb, NT, 0, s>>>(W, 0);
     k_p4<T><<<g, NT, 0, s>>>(W);
     apply(W.y, W.u, W.act_main);           // u = A y_{2n}
     k_p5<T><<<g, NT, 0, s>>>(W);
+    k_p5_fin<T><<<nb, NT, 0, s>>>(W);
     k_tx<T><<<g, NT, 0, s>>>(W);
     apply(W.x, W.s, W.act_tres);
     k_tr<T><<<g, NT, 0, s>>>(W, 1);
+    k_tr_fin<T><<<nb, NT, 0, s>>>(W, 1);
 }
 
 template <typename T>

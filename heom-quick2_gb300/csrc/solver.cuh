@@ -34,6 +34,10 @@ template <typename T> void tfq_free(TfqWork<T> &W);
 template <typename T>
 using ApplyFn = std::function<void(const typename Num<T>::V *, typename Num<T>::V *, const int *)>;
 
+// Kernel launches of tfq_start and of one tfq_iteration (including guarded no-op launches).
+constexpr int kTfqStartLaunches = 2;
+constexpr int kTfqIterationLaunches = 21;
+
 // Initialise the solve: expects W.b filled (right-hand side), W.rt filled (drandn stream).
 // The every-50-applies test stops an instance at ||A x - b|| <= max(crit, rel_crit ||b||);
 // stag_window > 0 also stops it after that many tests without halving the best residual.

@@ -20,7 +20,7 @@ from . import models  # noqa: F401
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libheom_gb300.so")
 
-PREC_FP64, PREC_MIXED, PREC_MIXED_FP32 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_MIXED_FP32, PREC_FP64_REFINED = 0, 1, 2, 3
 PROP_RK4, PROP_CHEBYSHEV = 0, 1
 ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "out of memory", -4: "unsupported",
           -5: "TFQMR breakdown", -6: "not converged", -7: "device wait timed out"}
@@ -71,7 +71,7 @@ class CtxOpts(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32), ("inner_tol", C.c_double),
-                ("max_refine", C.c_int32)]
+                ("max_refine", C.c_int32), ("stag_window", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -386,8 +386,10 @@ class Batch:
         self.h = h
         self.stride = lib().heom_batch_stride(h)
 
-    def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True):
-        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine)
+    def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True,
+                  stag_window=0):
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine,
+                      stag_window=stag_window)
         info = SolveInfo()
         rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
         if check:

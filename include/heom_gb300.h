@@ -42,7 +42,9 @@ enum {
  * MIXED_FP32: the same with plain FP32 inner arithmetic; it converges only where the
  * operator's conditioning times 6e-8 stays well below one (the single-orbital model at
  * T = 0.1 does, the double dot does not). */
-enum { HEOM_PREC_FP64 = 0, HEOM_PREC_MIXED = 1, HEOM_PREC_MIXED_FP32 = 2 };
+enum { HEOM_PREC_FP64 = 0, HEOM_PREC_MIXED = 1, HEOM_PREC_MIXED_FP32 = 2, HEOM_PREC_FP64_REFINED = 3 };
+/* FP64_REFINED: the refinement of MIXED with FP64 inner solves; slower, for reference
+ * solutions below the FP64 TFQMR floor (||b - A x|| down to about 1e-13). */
 
 /* View of the module data the reference keeps for the sparse path
  * (module/matmod.f90:4-52, module/sparsemod.f90:34-42, include/common).  The
@@ -151,6 +153,8 @@ typedef struct {
                                  r0 its FP64 right-hand side; <= 0 selects the default
                                  (1e-6 for MIXED, 1e-2 for MIXED_FP32) */
     int32_t max_refine;       /* MIXED: outer refinement rounds */
+    int32_t stag_window;      /* MIXED: an inner solve also stops after this many every-50-applies
+                                 tests without halving its residual; <= 0 selects 4 */
 } heom_solve_opts;
 
 typedef struct {

@@ -25,7 +25,7 @@ def make_cfg(name, **over):
 def steady_current(cfg):
     m = heomq.Model(cfg)
     ctx = heomq.Context(m)
-    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_MIXED, max_refine=16)
+    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
     assert info.converged
     return ctx.current(rho)[0].sum()
 
@@ -37,7 +37,7 @@ def test_adjoint_gradient_matches_central_differences(name):
     cfg = make_cfg(name)
     m = heomq.Model(cfg)
     ctx = heomq.Context(m, dhs=(m.get("dhs_du", m.nrho ** 2, np.complex128), m.get("dhs_deps", m.nrho ** 2, np.complex128)))
-    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_MIXED, max_refine=16)
+    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
     assert info.converged
     # d eleadinfty / dV: +1/2 for lead 1, -1/2 for lead 2, in the operator's units (1/hbar)
     deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / HB
@@ -61,7 +61,7 @@ def test_adjoint_identity_of_the_regularised_solve():
     cfg = make_cfg("siam_L2")
     m = heomq.Model(cfg)
     ctx = heomq.Context(m)
-    rho, _ = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_MIXED, max_refine=16)
+    rho, _ = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
     deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / HB
     d1, _ = ctx.steady_gradient(rho, deshift=deshift, which=1, crit=1e-12)
     d2, _ = ctx.steady_gradient(rho, deshift=2 * deshift, which=1, crit=1e-12)
@@ -77,7 +77,7 @@ def test_td_gradient_matches_central_differences(name, nstep, ck):
     cfg0 = make_cfg(name, V=0.0)
     m0 = heomq.Model(cfg0)
     ctx0 = heomq.Context(m0)
-    rho_eq, _ = ctx0.solve_tfqmr(crit=1e-12, precision=heomq.PREC_MIXED, max_refine=16)
+    rho_eq, _ = ctx0.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
     cfg = make_cfg(name)
     m = heomq.Model(cfg)
     amps, tchar = m.field()
@@ -93,3 +93,31 @@ def test_td_gradient_matches_central_differences(name, nstep, ck):
     h = 1e-5
     fd = (integral(1 + h) - integral(1 - h)) / (2 * h)
     assert abs(dJ - fd) <= 1e-6 * abs(fd), (dJ, fd)
+
+
+def test_autograd_wrappers_match_the_entry_points():
+    import torch
+
+    from heomq import autograd as hag
+
+    theta = torch.tensor([0.6, 0.5, 2.0, -0.7], dtype=torch.float64, requires_grad=True)
+    base = dict(ntier=3, nmats=2)
+    current = hag.steady_current(theta, "siam", **base)
+    current.backward()
+    h = 1e-5
+    for k in range(4):
+        tp, tm = theta.detach().clone(), theta.detach().clone()
+        tp[k] += h
+        tm[k] -= h
+        fd = (hag.steady_current(tp, "siam", **base) - hag.steady_current(tm, "siam", **base)).item() / (2 * h)
+        assert abs(theta.grad[k].item() - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(current.item()))
+    m0 = heomq.Model(make_cfg("siam_L2", V=0.0))
+    rho_eq, _ = heomq.Context(m0).solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    m = heomq.Model(make_cfg("siam_L2"))
+    amp = torch.tensor(1.3, dtype=torch.float64, requires_grad=True)
+    J = hag.chebyshev_current_integral(amp, m, rho_eq, 0.05, 40, 8)
+    J.backward()
+    h = 1e-5
+    jp = hag.chebyshev_current_integral(torch.tensor(1.3 + h, dtype=torch.float64), m, rho_eq, 0.05, 40, 8).item()
+    jm = hag.chebyshev_current_integral(torch.tensor(1.3 - h, dtype=torch.float64), m, rho_eq, 0.05, 40, 8).item()
+    assert abs(amp.grad.item() - (jp - jm) / (2 * h)) <= 1e-6 * abs((jp - jm) / (2 * h))

@@ -125,3 +125,29 @@ def test_chebyshev_term_count_grows_with_the_spectral_width():
     n1 = of.cheby_nterms(10.0, 0.05)
     n2 = of.cheby_nterms(100.0, 0.05)
     assert 0 < n1 < n2
+
+
+def test_augmented_system_null_space():
+    """The reference's augmented steady-state system [L; Tr] x = e is singular but
+    consistent: its real null space holds the free trace unknown x[lunk] (2 real
+    directions) and nd - 1 anti-Hermitian stationary RDO directions, which change the
+    current.  The mixed-precision solver regularises exactly these directions."""
+    m = of.Model(cf.siam(ntier=3, nmats=2, V=0.4))
+    n = m.lunk + 1
+    M = np.zeros((2 * n, 2 * n))
+    for k in range(n):
+        for part in (0, 1):
+            x = np.zeros(n, complex)
+            x[k] = 1.0 if part == 0 else 1j
+            y = m.calc_ax(x, nthreads=1)
+            M[:n, part * n + k] = y.real
+            M[n:, part * n + k] = y.imag
+    u, s, vt = np.linalg.svd(M)
+    null = np.where(s < 1e-11 * s[0])[0]
+    assert len(null) == 2 + (m.nrho - 1)
+    assert s[null[0] - 1] > 1e-4 * s[0]                       # a clear gap above the null space
+    b = np.zeros(2 * n)
+    b[n - 1] = 1.0
+    assert np.sqrt(sum((u[:, j] @ b) ** 2 for j in null)) < 1e-13   # consistent
+    currents = [np.abs(m.current(vt[j][: n - 1] + 1j * vt[j][n: 2 * n - 1])).max() for j in null]
+    assert max(currents) > 1.0                                 # the null space moves the current
