@@ -115,6 +115,7 @@ SIGNATURES = {
     "heom_batch_stride": (C.c_int64, [C.c_void_p]),
     "heom_batch_solve_dev": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_batch_destroy": (None, [C.c_void_p]),
+    "heom_batch_current_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
 }
 
 _lib = None
@@ -395,6 +396,15 @@ class Batch:
         if check:
             _check(rc)
         return info
+
+    def currents_static(self, x_dev, nbatch=None, vstride=None):
+        """Lead currents jt[b, ialf, ispin] of device states, without device allocation."""
+        n = self.nbatch if nbatch is None else nbatch
+        ns = self.ctx.model.nalf * self.ctx.model.nspin
+        jt = np.zeros(n * ns)
+        _check(lib().heom_batch_current_static(self.ctx.h, C.c_void_p(x_dev), n,
+                                                self.stride if vstride is None else vstride, jt.ctypes.data))
+        return jt.reshape(n, self.ctx.model.nspin, self.ctx.model.nalf).transpose(0, 2, 1)
 
     def close(self):
         if getattr(self, "h", None) and _lib is not None:

@@ -224,6 +224,17 @@ int64_t heom_batch_stride(const heom_batch *b);
 int heom_batch_solve_dev(heom_batch *b, const heom_solve_opts *o, void *x_dev, heom_solve_info *info);
 void heom_batch_destroy(heom_batch *b);
 
+/* Lead currents jt[b][ialf + nalf*ispin] (b < nbatch) of nbatch device-resident states
+ * x_dev (FP64 complex, instance stride vstride >= lunk + 1 elements, e.g. the vectors of
+ * heom_batch_solve_dev), without any device allocation: the sums go through a file-scope
+ * device array of 4096 x 4 doubles (128 KiB), so nbatch > 4096 is rejected.  It has no
+ * counterpart in the reference (calcj, td/calcj.f90:40-85, works on one host state).  It
+ * serves callers that must not allocate between solver rounds or time steps (cudaFree
+ * synchronises the whole device).  The first call on a device does a one-time address
+ * lookup and should come before any stream capture; calls that overlap in time share the
+ * scratch and race. */
+int heom_batch_current_static(heom_ctx *ctx, const void *x_dev, int32_t nbatch, int64_t vstride, double *jt);
+
 /* Measurement hook: time `reps` back-to-back applies on `nbatch` instances on device, in
  * the form each solver precision uses (HEOM_PREC_FP64: the FP64 apply; HEOM_PREC_MIXED and
  * HEOM_PREC_MIXED_FP32: the regularised FP32x2 / FP32 apply of the inner solves), and
