@@ -374,7 +374,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   const std::function<void(const double2 *)> &batch_norms)
 {
     const int64_t N = c->lunk + 1;
-    const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-6);
+    const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 3e-7);
     TfqWork<T> W;
     tfq_alloc<T>(W, nbatch, N);
     typename Num<T>::V *gd = nullptr;
