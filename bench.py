@@ -241,13 +241,15 @@ def run_gb300(args, ws, rank, local, dist):
     # FP64 timing beside (one step, after the timed region)
     t64 = info64.seconds
     # end to end through the C ABI with host buffers
-    rhos = np.tile(x0h, (B, 1))
+    pinned = torch.empty((B, L), dtype=torch.complex128, pin_memory=True)
+    rhos = pinned.numpy()
     hs_b = None
     e2e_times = []
     for _ in range(max(1, min(args.steps, 3))):
+        rhos[:] = x0h
         t0 = time.perf_counter()
         out, info_e = ctx.solve_batch(rhos, hs_batch=hs_b, eshift_batch=es_cm, crit=args.crit,
-                                      precision=heomq.PREC_MIXED)
+                                      precision=heomq.PREC_MIXED, inplace=True)
         jt = [ctx.current(out[b])[0].sum() for b in range(B)]
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = ws * B / statistics.median(e2e_times)

@@ -100,7 +100,7 @@ heom_ctx::~heom_ctx()
 {
     dfwd.release();
     dadj.release();
-    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch, d_rdo_pair};
+    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch, d_rdo_pair, d_rdo_upper};
     for (void *p : ptrs) if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -203,6 +203,24 @@ __global__ void k_herm_rdo(double2 *x, int64_t vstride, int64_t lunk, int nz0, c
         xb[p] = make_double2(h.x, -h.y);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) xb[lunk] = make_double2(0.0, 0.0);
+}
+
+// The reference's hermitisation of an input RDO block (utility/zmat_herm_coo.f90, uplo 'u'):
+// the upper triangle defines the lower one and the diagonal is made real.
+__global__ void k_herm_rdo_upper(double2 *x, int64_t vstride, int nz0, const int32_t *pair, const int32_t *upper)
+{
+    double2 *xb = x + (int64_t)blockIdx.y * vstride;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nz0; q += gridDim.x * blockDim.x) {
+        const int p = pair[q];
+        if (p == q) xb[q].y = 0.0;
+        else if (upper[q]) xb[p] = make_double2(xb[q].x, -xb[q].y);
+    }
+}
+
+void herm_rdo_upper_dev(heom_ctx *c, double2 *x, int nbatch, int64_t vstride)
+{
+    dim3 g((unsigned)std::max(1, std::min(64, (c->nz0 + 255) / 256)), (unsigned)nbatch);
+    k_herm_rdo_upper<<<g, 256, 0, c->stream>>>(x, vstride, c->nz0, c->d_rdo_pair, c->d_rdo_upper);
 }
 
 void herm_rdo_dev(heom_ctx *c, double2 *x, int nbatch, int64_t vstride)
@@ -568,8 +586,12 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
                 if (pair[q] == q) c->ndiag++;
             }
             c->nz0 = nz0;
+            std::vector<int32_t> upper(nz0);
+            for (int q = 0; q < nz0; q++) upper[q] = t->icol_spa[q] > t->irow_spa[q];
             CK(cudaMalloc((void **)&c->d_rdo_pair, sizeof(int32_t) * std::max(1, nz0)));
             CK(cudaMemcpy(c->d_rdo_pair, pair.data(), sizeof(int32_t) * nz0, cudaMemcpyHostToDevice));
+            CK(cudaMalloc((void **)&c->d_rdo_upper, sizeof(int32_t) * std::max(1, nz0)));
+            CK(cudaMemcpy(c->d_rdo_upper, upper.data(), sizeof(int32_t) * nz0, cudaMemcpyHostToDevice));
             // regularising weight: the largest bath decay rate |Re cgamma|, a typical diagonal
             // magnitude of the operator
             int nvar = 2 * t->norbs * t->nspin * t->nalf * t->ncor;
@@ -835,27 +857,22 @@ int heom_solve_batch(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batc
     void *dxb = nullptr;
     rc = guarded([&] {
         if (!o || !rho_batch) fail(HEOM_E_ARG, "null argument");
-        int64_t N = c->lunk + 1, vs = B->vs;
+        const int64_t vs = B->vs;
         CK(cudaMalloc(&dxb, sizeof(double2) * (size_t)vs * nbatch));
         CK(cudaMemsetAsync(dxb, 0, sizeof(double2) * (size_t)vs * nbatch, c->stream));
-        std::vector<cd> x((size_t)vs * nbatch, 0.0);
-        for (int b = 0; b < nbatch; b++) {
-            cd *xb = x.data() + (size_t)b * vs;
-            std::memcpy(xb, reinterpret_cast<cd *>(rho_batch) + (size_t)b * c->lunk, sizeof(cd) * c->lunk);
-            herm_rdo(c, xb);
-        }
-        CK(cudaMemcpyAsync(dxb, x.data(), sizeof(double2) * x.size(), cudaMemcpyHostToDevice, c->stream));
+        // one strided copy straight from the caller's buffer (DMA at full speed when it is
+        // pinned), then the reference's hermitisation of the RDO block on the device
+        CK(cudaMemcpy2DAsync(dxb, sizeof(double2) * vs, rho_batch, sizeof(double2) * c->lunk, sizeof(double2) * c->lunk,
+                             nbatch, cudaMemcpyHostToDevice, c->stream));
+        herm_rdo_upper_dev(c, (double2 *)dxb, nbatch, vs);
         CK(cudaStreamSynchronize(c->stream));
-        (void)N;
     });
     if (rc == 0) rc = heom_batch_solve_dev(B, o, dxb, info);
     if (rc == 0 || rc == HEOM_E_NOCONV) {
         int rc2 = guarded([&] {
-            std::vector<cd> x((size_t)B->vs * nbatch);
-            CK(cudaMemcpyAsync(x.data(), dxb, sizeof(double2) * x.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaMemcpy2DAsync(rho_batch, sizeof(double2) * c->lunk, dxb, sizeof(double2) * B->vs, sizeof(double2) * c->lunk,
+                                 nbatch, cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
-            for (int b = 0; b < nbatch; b++)
-                std::memcpy(reinterpret_cast<cd *>(rho_batch) + (size_t)b * c->lunk, x.data() + (size_t)b * B->vs, sizeof(cd) * c->lunk);
         });
         if (rc == 0) rc = rc2;
     }

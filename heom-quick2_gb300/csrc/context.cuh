@@ -81,6 +81,7 @@ struct heom_ctx {
     std::vector<int32_t> occ_entry, occ_slot;       // RDO diagonal entries contributing to occ(m,s)
     std::vector<int32_t> rdo_rows, rdo_cols;        // RDO pattern (1-based)
     int32_t *d_rdo_pair = nullptr;                  // transposed RDO entry (device)
+    int32_t *d_rdo_upper = nullptr;                 // 1 for entries above the diagonal (device)
     int32_t nz0 = 0, ndiag = 0;
     double reg_scale = 1.0;                         // weight of the regularising blocks
     double cheby_delta = 0.0;                       // spectral width of the Liouville diagonal

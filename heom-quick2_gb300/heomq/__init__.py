@@ -304,8 +304,15 @@ class Context:
         return rho, info
 
     def solve_batch(self, rhos, hs_batch=None, eshift_batch=None, crit=1e-10, maxit0=20000, precision=PREC_FP64,
-                    inner_tol=0.0, max_refine=8):
-        rhos = np.ascontiguousarray(rhos, dtype=np.complex128).copy()
+                    inner_tol=0.0, max_refine=8, inplace=False):
+        """Steady states of a batch; rhos (nbatch, lunk) holds the initial guesses.  With
+        inplace=True a C-contiguous complex128 rhos (e.g. a view of pinned memory) is solved
+        in place."""
+        if inplace:
+            if rhos.dtype != np.complex128 or not rhos.flags.c_contiguous:
+                raise ValueError("inplace needs a C-contiguous complex128 array")
+        else:
+            rhos = np.ascontiguousarray(rhos, dtype=np.complex128).copy()
         nb = rhos.shape[0]
         hs = None if hs_batch is None else _c128(hs_batch)
         es = None if eshift_batch is None else np.ascontiguousarray(eshift_batch, dtype=np.float64)
