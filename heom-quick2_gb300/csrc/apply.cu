@@ -8,7 +8,8 @@
 // where every gather is a precomputed index into the source ADO's stored entries.
 // The higher-tier couplings have coefficients +-i and cost only additions; the
 // lower-tier ones multiply by the bath residues cb, cd.  In FP64 the kernel is
-// bounded by the FP64 pipe; in FP32 and FP32x2 by gather latency and bandwidth.
+// bounded by the FP64 pipe; in FP32x2 by instruction issue on the FP32 / ALU pipes
+// (double-float arithmetic, about 1 400 instructions per entry); in FP32 by gather latency.
 //
 // REG selects the regularised operator of the mixed-precision inner solves (see DevCoef):
 // reads of RDO entries (source offset 0) see the Hermitian part (x_q + conj x_q')/2.
@@ -78,17 +79,18 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
     // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
     const int tb = __ldg(P.cls_tptr + c) + p;
     const int k0 = __ldg(P.term_ptr + tb), k1 = __ldg(P.term_ptr + tb + 1);
-    A sl = N::zero(), sr = N::zero();   // sum H x over left terms and over right terms
+    // one signed sum: right terms (x H) count +, left terms (H x) count - (no divergent branch)
+    A sd = N::zero();
     for (int k = k0; k < k1; k++) {
         const uint32_t w = __ldg(P.terms + k);
         A h = N::load(hv[(w >> 16) & 0x7FFF]);
         if (ADJ) h = N::conj(h);
         const A xs = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF)) : N::load(x[off + (int)(w & 0xFFFF)]);
         const A hx = C.h_real ? N::scale(xs, N::re_s(h)) : N::mul(h, xs);
-        if (w >> 31) sr = N::add(sr, hx); else sl = N::add(sl, hx);
+        sd = N::add(sd, (w >> 31) ? hx : N::neg(hx));
     }
-    // forward: acc += i (sr - sl); adjoint: acc += -i (sr - sl)
-    A dlt = N::mul_i(N::sub(sr, sl));
+    // forward: acc += i (sum_right - sum_left); adjoint: acc += -i (...)
+    const A dlt = N::mul_i(N::norm(sd));
     acc = N::add(acc, ADJ ? N::neg(dlt) : dlt);
 
     // couplings to the neighbouring tiers
@@ -122,9 +124,9 @@ __global__ void __launch_bounds__(256) k_apply(DevPlan P, DevCoef<T> C, const ty
             const int cid = rec.z & 0x3FFFFFFF;
             if (lo) acc = N::add(acc, N::mul(N::load(C.cl[cid]), vl));
             if (hi) acc = N::add(acc, N::mul(N::load(C.cr[cid]), vr));
-            acc = N::norm(acc);
+            if ((e - e0) & 1) acc = N::norm(acc);
         }
-        ua = N::norm(ua);
+        if (((e - e0) & 3) == 3) ua = N::norm(ua);
     }
     acc = N::add(acc, N::mul_i(ua));
     y[t] = N::store(acc);

@@ -1,6 +1,8 @@
 """Adjoint steady-state sensitivities of the lead-1 current against central finite
-differences (h = 1e-5 relative to the parameter scale, steady states solved to a residual
-of 1e-12 by the mixed-precision refinement)."""
+differences.  Steady states are refined to a residual of 1e-12, which leaves about 1e-11
+relative noise in the current; the steady-state differences therefore use h = 1e-4 (the
+truncation error h^2 stays near 1e-8) so that the noise of (I+ - I-)/2h stays well below the
+1e-6 bar.  The time-dependent runs are deterministic and use h = 1e-5."""
 import numpy as np
 import pytest
 
@@ -45,7 +47,7 @@ def test_adjoint_gradient_matches_central_differences(name):
                                     dhs_du=m.get("dhs_du", m.nrho ** 2, np.complex128),
                                     dhs_deps=m.get("dhs_deps", m.nrho ** 2, np.complex128), which=0xF, crit=1e-12)
     for k, key in enumerate(("V", "gamma", "U", "eps")):
-        h = 1e-5 * max(1.0, abs(p0[key]))
+        h = 1e-4 * max(1.0, abs(p0[key]))
         if key == "gamma":
             ip = steady_current(make_cfg(name, gamma=p0[key] + h))
             im = steady_current(make_cfg(name, gamma=p0[key] - h))
@@ -104,7 +106,7 @@ def test_autograd_wrappers_match_the_entry_points():
     base = dict(ntier=3, nmats=2)
     current = hag.steady_current(theta, "siam", **base)
     current.backward()
-    h = 1e-5
+    h = 1e-4
     for k in range(4):
         tp, tm = theta.detach().clone(), theta.detach().clone()
         tp[k] += h
