@@ -345,7 +345,7 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, c->stream));
     TfqWork<double> W;
-    tfq_alloc<double>(W, 1, N);
+    tfq_alloc<double>(W, 1, N, c->stream);
     double resid = 0;
     try {
         upload_rt(c, W);
@@ -394,7 +394,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     const int64_t N = c->lunk + 1;
     const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 3e-7);
     TfqWork<T> W;
-    tfq_alloc<T>(W, nbatch, N);
+    tfq_alloc<T>(W, nbatch, N, c->stream);
     typename Num<T>::V *gd = nullptr;
     try {
         upload_rt(c, W);
@@ -421,7 +421,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             double tgt = 1.0;
             for (double v : norms) if (v > o.crit) tgt = std::min(tgt, o.crit / v);
             tgt = std::max(tgt, itol);
-            tfq_start<T>(W, tgt, nlim, tgt, 0.0, o.stag_window > 0 ? o.stag_window : 4, c->stream);
+            tfq_start<T>(W, tgt, nlim, tgt, 0.0, o.stag_window > 0 ? o.stag_window : 16, c->stream);
             aux += kTfqStartLaunches + nbatch;
             int it = 0;
             tfq_run<T>(c, W, make_apply<T>(c, rhs ? KT : KR, nbatch, W.vstride, false), nlim, it, launches);
@@ -472,7 +472,7 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     try {
         if (o.precision == HEOM_PREC_FP64) {
             TfqWork<double> W;
-            tfq_alloc<double>(W, nbatch, N);
+            tfq_alloc<double>(W, nbatch, N, c->stream);
             try {
                 upload_rt(c, W);
                 // b = rhs - A x0 per instance, stored with the workspace stride
@@ -648,7 +648,7 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
         CK(cudaMalloc((void **)&c->fy, sizeof(float2) * N));
         CK(cudaMalloc((void **)&c->dscratch, sizeof(double) * 2048));
         drandn_stream(2 * N, c->rt_host);
-        CK(cudaDeviceSynchronize());
+        CK(cudaStreamSynchronize(c->stream));
         *out = c.release();
     });
 }

@@ -4,11 +4,11 @@
 // algorithm of R. W. Freund (SIAM J. Sci. Comput. 14 (1993) 470) in the column
 // roles and tolerances of tfqmr_double/dutfx.f90: 1 x, 2 b, 3 shadow r~, 4 v, 5 w,
 // 6 y, 7 d, 8 A y (u), 9 scratch (t).  Vector arithmetic runs in the number type T
-// (FP64, FP32 or FP32x2); inner products are summed in FP64 across threads.  Each reduction ends in its
-// last thread block, which updates that instance's scalars (deterministic: partials
-// are summed in a fixed order).  Vector kernels skip instances that have finished, so
-// one launch sequence serves a batch of independent solves and can be captured in a
-// CUDA graph.
+// (FP64, FP32 or FP32x2); inner products are summed in FP64 across threads.  A reduction
+// kernel writes one partial per block; a one-block-per-instance finaliser (k_*_fin) sums
+// them in a fixed order (deterministic) and updates that instance's scalars.  Vector
+// kernels skip instances that have finished, so one launch sequence serves a batch of
+// independent solves and can be captured in a CUDA graph.
 #include <cstdio>
 
 #include "solver.cuh"
@@ -217,9 +217,12 @@ __global__ void k_chk_fin(TfqWork<T> W)
         st.chk = 0;
         if (st.ext_resid <= st.crit) { st.done = 1; st.conv_ext = 1; }
         else if (st.stag_window) {
-            // inner solve of a refinement: stop once stag_window consecutive tests fail to halve the
-            // best true residual (the arithmetic's floor), and hand back to the FP64 refinement
-            if (st.ext_resid < 0.5 * st.best) { st.best = st.ext_resid; st.stag = 0; }
+            // inner solve of a refinement: hand back to the FP64 refinement once the arithmetic's
+            // floor is reached, seen either as the true residual running 10x above TFQMR's own
+            // bound sqrt(2n+1) tau (the recursion has drifted from the true residual), or as
+            // stag_window consecutive tests that fail to halve the best true residual
+            if (st.n > 2 && st.ext_resid > 10.0 * st.unrm * st.r0) { st.done = 1; st.ierr = 4; }
+            else if (st.ext_resid < 0.5 * st.best) { st.best = st.ext_resid; st.stag = 0; }
             else if (++st.stag >= st.stag_window) { st.done = 1; st.ierr = 4; }
         }
         *S = st;
@@ -465,7 +468,7 @@ int grid_for(int64_t n) { int64_t g = (n + NT - 1) / NT; return (int)(g < 1 ? 1 
 }  // namespace
 
 template <typename T>
-void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N)
+void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
 {
     using V = typename Num<T>::V;
     W.nbatch = nbatch;
@@ -479,8 +482,9 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N)
                    sizeof(double) * 2 * (size_t)nbatch * W.nblk + sizeof(unsigned) * nbatch + 3 * sizeof(int) * nbatch + 4096;
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the TFQMR workspace failed");
-    // the solver runs on a non-blocking stream: finish the clear before any use
-    if (cudaMemset(p, 0, total) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+    // cleared on the solver's stream (no device-wide synchronisation, which would collide with
+    // graph captures of other contexts), finished before first use
+    if (cudaMemsetAsync(p, 0, total, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
         cudaFree(p);
         fail(HEOM_E_CUDA, "clearing the TFQMR workspace failed");
     }
@@ -587,7 +591,7 @@ double device_dot(int64_t n, const double2 *a, const double2 *b, double *scratch
 }
 
 #define INST(T)                                                                                                 \
-    template void tfq_alloc<T>(TfqWork<T> &, int, int64_t);                                                     \
+    template void tfq_alloc<T>(TfqWork<T> &, int, int64_t, cudaStream_t);                                      \
     template void tfq_free<T>(TfqWork<T> &);                                                                    \
     template void tfq_start<T>(TfqWork<T> &, double, int, double, double, int, cudaStream_t);                   \
     template void tfq_iteration<T>(TfqWork<T> &, const ApplyFn<T> &, cudaStream_t);                             \

@@ -27,7 +27,7 @@ struct TfqWork {
     void *mem = nullptr;          // single allocation backing everything above
 };
 
-template <typename T> void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N);
+template <typename T> void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s);
 template <typename T> void tfq_free(TfqWork<T> &W);
 
 // apply(x, y, active): y = A x for the instances whose active flag is set

