@@ -137,10 +137,13 @@ void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp
 PropBuffers::PropBuffers(heom_ctx *c, int nvec, int64_t njt)
 {
     N = c->lunk + 1;
-    size_t bytes = sizeof(double2) * (size_t)N * nvec + sizeof(double) * 8 + sizeof(PropClock) + sizeof(double) * std::max<int64_t>(njt, 1) + 1024;
+    // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
+    auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t bytes = rounded(sizeof(double2) * (size_t)N) * nvec + rounded(sizeof(double) * 8) +
+                         rounded(sizeof(PropClock)) + rounded(sizeof(double) * std::max<int64_t>(njt, 1));
     CK(cudaMalloc(&mem, bytes));
     char *p = (char *)mem;
-    auto take = [&](size_t b) { char *q = p; p += (b + 255) / 256 * 256; return (void *)q; };
+    auto take = [&](size_t b) { char *q = p; p += rounded(b); return (void *)q; };
     for (int k = 0; k < nvec; k++) vec.push_back((double2 *)take(sizeof(double2) * N));
     es = (double *)take(sizeof(double) * 8);
     clk = (PropClock *)take(sizeof(PropClock));

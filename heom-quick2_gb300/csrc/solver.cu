@@ -478,8 +478,11 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     int64_t nb = (N + 4 * NT - 1) / (4 * NT);
     W.nblk = (int)(nb < 1 ? 1 : (nb > 296 ? 296 : nb));
     size_t vbytes = sizeof(V) * (size_t)W.vstride * nbatch;
-    size_t total = vbytes * 9 + sizeof(V) * (size_t)W.vstride + sizeof(TfqState) * nbatch +
-                   sizeof(double) * 2 * (size_t)nbatch * W.nblk + sizeof(unsigned) * nbatch + 3 * sizeof(int) * nbatch + 4096;
+    // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
+    auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(TfqState) * nbatch) +
+                         rounded(sizeof(double) * 2 * (size_t)nbatch * W.nblk) + rounded(sizeof(unsigned) * nbatch) +
+                         3 * rounded(sizeof(int) * nbatch);
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the TFQMR workspace failed");
     // cleared on the solver's stream (no device-wide synchronisation, which would collide with
@@ -489,7 +492,7 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
         fail(HEOM_E_CUDA, "clearing the TFQMR workspace failed");
     }
     W.mem = p;
-    auto take = [&](size_t bytes) { char *q = p; p += (bytes + 255) / 256 * 256; return q; };
+    auto take = [&](size_t bytes) { char *q = p; p += rounded(bytes); return q; };
     W.x = (V *)take(vbytes); W.b = (V *)take(vbytes); W.v = (V *)take(vbytes); W.w = (V *)take(vbytes);
     W.y = (V *)take(vbytes); W.d = (V *)take(vbytes); W.u = (V *)take(vbytes); W.t = (V *)take(vbytes);
     W.s = (V *)take(vbytes);

@@ -60,3 +60,16 @@ def test_long_chebyshev_run_relaxes_to_the_steady_state():
     i_ss = ctx.current(rho_ss)[0].sum()
     i_t = ctx.current(rho)[0].sum()
     assert abs(i_t / i_ss - 1) < 1e-3
+
+
+@pytest.mark.parametrize("method", [heomq.PROP_RK4, heomq.PROP_CHEBYSHEV], ids=["rk4", "chebyshev"])
+def test_full_size_propagation_buffers(method):
+    """The double dot at tier 4 (393 812 entries): the device buffers of a propagation with
+    current recording are laid out without overlap (the recorded first-step current equals
+    the host current of the initial state, and the run completes)."""
+    m = heomq.Model(cf.CFG1)
+    ctx = heomq.Context(m, adjoint=False)
+    rho0 = m.initial_guess()
+    rho, jt = ctx.propagate(rho0, 0.0, 0.05, 3, method=method, currents=True)
+    np.testing.assert_allclose(jt[0], ctx.current(rho0).T.reshape(-1), rtol=1e-12, atol=1e-9)
+    assert np.isfinite(rho).all() and np.isfinite(jt).all()
