@@ -481,7 +481,7 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
     auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(TfqState) * nbatch) +
-                         rounded(sizeof(double) * 2 * (size_t)nbatch * W.nblk) + rounded(sizeof(unsigned) * nbatch) +
+                         rounded(sizeof(double) * 2 * (size_t)nbatch * W.nblk) +
                          3 * rounded(sizeof(int) * nbatch);
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the TFQMR workspace failed");
@@ -499,7 +499,6 @@ void tfq_alloc(TfqWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     W.rt = (V *)take(sizeof(V) * (size_t)W.vstride);
     W.st = (TfqState *)take(sizeof(TfqState) * nbatch);
     W.part = (double *)take(sizeof(double) * 2 * (size_t)nbatch * W.nblk);
-    W.cnt = (unsigned *)take(sizeof(unsigned) * nbatch);
     W.act_main = (int *)take(sizeof(int) * nbatch);
     W.act_tres = (int *)take(sizeof(int) * nbatch);
     W.act_chk = (int *)take(sizeof(int) * nbatch);

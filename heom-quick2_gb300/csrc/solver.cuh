@@ -22,7 +22,6 @@ struct TfqWork {
       *t = nullptr, *s = nullptr;
     TfqState *st = nullptr;       // device, nbatch
     double *part = nullptr;       // nbatch * nblk * 2
-    unsigned *cnt = nullptr;      // nbatch
     int *act_main = nullptr, *act_tres = nullptr, *act_chk = nullptr;
     void *mem = nullptr;          // single allocation backing everything above
 };
