@@ -45,6 +45,24 @@ def bias_points(n):
     return [0.8] if n == 1 else [0.4 + 0.8 * b / (n - 1) for b in range(n)]
 
 
+def rank_bias_points(batch, rank, world_size):
+    """Replicas (weak scaling): rank r solves its own batch of bias points out of one sweep of
+    batch * world_size points, so every rank does the same amount of distinct work."""
+    pts = bias_points(batch * world_size)
+    return pts[rank * batch:(rank + 1) * batch]
+
+
+def max_over_ranks(x, dist, device="cpu"):
+    """The largest per-rank value (the job's time), through an all-reduce; x itself without dist."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -170,7 +188,7 @@ def run_gb300(args, ws, rank, local, dist):
     dev = local
     torch.cuda.set_device(dev)
     B = args.batch
-    Vs = bias_points(B)
+    Vs = rank_bias_points(B, rank, ws)
     cfg = heomq.models.dqd(ntier=5, nmats=3, V=0.8)
     model = heomq.Model(cfg)
     ctx = heomq.Context(model, device=dev, adjoint=False)
@@ -231,11 +249,7 @@ def run_gb300(args, ws, rank, local, dist):
         dist.barrier()
     clocks = clocks_stop(clk, dev) if rank == 0 else None
     curm = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
-    t_step = dev_s / args.steps
-    if dist:
-        t = torch.tensor([t_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
+    t_step = max_over_ranks(dev_s / args.steps, dist, device="cuda")
     value = ws * B / t_step
 
     # FP64 timing beside (one step, after the timed region)
@@ -295,6 +309,8 @@ def run_gb300(args, ws, rank, local, dist):
                        "current_reference_resid": info_ref.resid},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_apply<FP32x2> over the batch",
+                         "note": "issue-bound on the FP32/ALU pipes (double-float arithmetic, ~75% issue "
+                                 "utilisation), not HBM-bound: profiles/apply_fp32x2_dqd_L4_batch8.md",
                          "apply_us": sec * 1e6, "alg_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
