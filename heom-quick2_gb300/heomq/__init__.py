@@ -158,7 +158,8 @@ def make_params(cfg):
             p.linewidth[a][o] = cfg["linewidth"][a][o]
         for s in range(cfg["nspin"]):
             p.engyshift[a][s] = cfg["engyshift"][a][s]
-            p.tchar[a][s] = cfg.get("tchar", 0.0)
+            tc = cfg.get("tchar", 0.0)
+            p.tchar[a][s] = tc[a][s] if isinstance(tc, (list, tuple)) else tc
     p.lscreen = int(cfg.get("lscreen", 0))
     p.doubledot = int(cfg.get("doubledot", 0))
     p.model = cfg["model"]

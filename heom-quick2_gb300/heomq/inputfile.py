@@ -1,0 +1,257 @@
+"""The reference's input file and its sparse state files, for drop-in workflows.
+
+Input file (read on unit 5 by the reference):
+- 12 list-directed records in the order of main/evaluatepara.f90:71-84:
+  init, ntier, nmats, norbs, nspin, nalf, bandwidth(nalf), linewidth(norbs, per lead),
+  temperature(nalf), engyshift(nspin, per lead), tmax, dt;
+- Fortran namelist groups anywhere after them ($name ... $end or &name ... /), each read by
+  name (main/main.f90:119-147, main/calchs.f90:17-27, main/evaluatepara.f90:27-28);
+- after the $field group, the record of tchar(nspin, per lead) for fieldtype 0
+  (main/evaluatepara.f90:2299-2330).
+
+Supported subset: the Lorentzian PSD sparse path (psdjob = T, lsparse = T, methodss = 2,
+fieldtype = 0) with $para1 (one orbital), $para4 (two orbitals, $ddots), or
+$hamil_sys lreadhs = T (H from hamil_sys.data, internal units).  Anything else raises.
+
+State files (Intel form='binary', i.e. raw streams without record markers):
+  rho_spa.st / .gr / .sav / .chk : int32 norbs, nspin, ncor, ntier0, nalf; int64 nunk;
+                                   then the nnz_spa(n) complex128 entries of every ADO n with
+                                   entries, in ADO order (main/main.f90:1087-1105,
+                                   fermion/initialize2_spa.f90:24-110).
+hamil_sys.data (form='unformatted', sequential): one record of nrho^2 complex128, column-major
+                                   (main/calchs.f90:78-82).
+"""
+import re
+import struct
+
+import numpy as np
+
+from . import models
+
+_NUM = re.compile(r"^[+-]?(\d+\.?\d*|\.\d+)([eEdD][+-]?\d+)?$")
+
+
+def _value(tok):
+    t = tok.strip().strip(",")
+    low = t.lower()
+    if low in (".true.", "t", ".t.", "true"):
+        return True
+    if low in (".false.", "f", ".f.", "false"):
+        return False
+    if len(t) >= 2 and t[0] == t[-1] and t[0] in "'\"":
+        return t[1:-1]
+    if _NUM.match(t):
+        v = float(t.replace("d", "e").replace("D", "e"))
+        return int(v) if re.match(r"^[+-]?\d+$", t) else v
+    raise ValueError(f"cannot read value {tok!r}")
+
+
+def _tokens(line):
+    """List-directed items of one record (r*value repeats expanded; '!' starts a comment)."""
+    line = line.split("!")[0]
+    out = []
+    for tok in re.split(r"[\s,]+", line.strip()):
+        if not tok:
+            continue
+        m = re.match(r"^(\d+)\*(.+)$", tok)
+        if m:
+            out += [m.group(2)] * int(m.group(1))
+        else:
+            out.append(tok)
+    return out
+
+
+def _namelists(text):
+    groups = {}
+    for m in re.finditer(r"[$&](\w+)(.*?)(?:[$&]end\b|/)", text, re.S | re.I):
+        name, body = m.group(1).lower(), m.group(2)
+        if name == "end":
+            continue
+        vals = {}
+        for a in re.finditer(r"(\w+)\s*=\s*('[^']*'|\"[^\"]*\"|[^\s,=]+)", body):
+            vals[a.group(1).lower()] = _value(a.group(2))
+        groups[name] = vals
+    return groups
+
+
+def parse(text):
+    """The positional records, the namelist groups and the record after $field."""
+    lines = text.splitlines()
+    pos = {}
+    li = 0
+
+    def read(count):
+        nonlocal li
+        vals = []
+        while len(vals) < count:
+            if li >= len(lines):
+                raise ValueError("input file ends inside the positional records")
+            toks = _tokens(lines[li])
+            li += 1
+            vals += [_value(t) for t in toks]
+        return vals[:count]
+
+    for key in ("init", "ntier", "nmats", "norbs", "nspin", "nalf"):
+        pos[key] = int(read(1)[0])
+    nalf, norbs, nspin = pos["nalf"], pos["norbs"], pos["nspin"]
+    pos["bandwidth"] = [float(v) for v in read(nalf)]
+    lw = read(nalf * norbs)
+    pos["linewidth"] = [[float(v) for v in lw[a * norbs:(a + 1) * norbs]] for a in range(nalf)]
+    pos["temperature"] = [float(v) for v in read(nalf)]
+    es = read(nalf * nspin)
+    pos["engyshift"] = [[float(v) for v in es[a * nspin:(a + 1) * nspin]] for a in range(nalf)]
+    pos["tmax"] = float(read(1)[0])
+    pos["dt"] = float(read(1)[0])
+    rest = "\n".join(lines[li:])
+    groups = _namelists(rest)
+    tchar = None
+    m = re.search(r"[$&]field\b.*?(?:[$&]end\b|/)[^\n]*\n(.*)", rest, re.S | re.I)
+    if m:
+        after = m.group(1).splitlines()
+        toks = []
+        for ln in after:
+            toks += _tokens(ln)
+            if len(toks) >= nalf * nspin:
+                break
+        if len(toks) >= nalf * nspin:
+            vals = [float(_value(t)) for t in toks[: nalf * nspin]]
+            tchar = [[vals[a * nspin + s] for s in range(nspin)] for a in range(nalf)]
+    return pos, groups, tchar
+
+
+def to_config(text, hamil_sys=None):
+    """Model configuration (heomq.Model argument) and solver options of an input file.
+    hamil_sys: H (nrho x nrho, internal units) when $hamil_sys lreadhs = T."""
+    pos, g, tchar = parse(text)
+    job = g.get("jobinfo", {})
+    if not job.get("lsparse", False):
+        raise ValueError("only the sparse path (lsparse = T) is supported")
+    if not job.get("psdjob", False):
+        raise ValueError("only the Pade spectrum decomposition (psdjob = T) is supported")
+    for flag in ("mfdjob", "pfdjob", "psfjob", "psdlor", "psdfff", "lsimple", "ltrun_der"):
+        if job.get(flag, False):
+            raise ValueError(f"{flag} = T is not supported")
+    if g.get("adiabatic", {}).get("lad", False):
+        raise ValueError("lad = T is not supported")
+    if g.get("method", {}).get("methodss", 2) != 2:
+        raise ValueError("only methodss = 2 (TFQMR) is supported")
+    if g.get("field", {}).get("fieldtype", 0) != 0:
+        raise ValueError("only fieldtype = 0 is supported")
+    cfg = dict(norbs=pos["norbs"], nspin=pos["nspin"], nalf=pos["nalf"], nmats=pos["nmats"], ntier=pos["ntier"],
+               bandwidth=pos["bandwidth"], linewidth=pos["linewidth"], temperature=pos["temperature"],
+               engyshift=pos["engyshift"], lscreen=int(bool(job.get("lscreen", False))),
+               doubledot=int(bool(g.get("ddots", {}).get("doubledot", False))),
+               tchar=(tchar if tchar else 0.0))
+    hs = None
+    if g.get("hamil_sys", {}).get("lreadhs", False):
+        if hamil_sys is None:
+            raise ValueError("lreadhs = T needs the hamil_sys.data matrix")
+        hs = np.asarray(hamil_sys, dtype=np.complex128)
+        cfg["model"] = 9
+    elif pos["norbs"] == 1 and pos["nspin"] == 2:
+        p = g.get("para1", {})
+        cfg.update(model=1, eup=p.get("eup", 0.0), edown=p.get("edown", 0.0), uu=p.get("uu", 0.0))
+    elif pos["norbs"] == 2 and pos["nspin"] == 2:
+        p = g.get("para4", {})
+        cfg.update(model=4, **{k: float(p.get(k, 0.0)) for k in ("e1up", "e1down", "e2up", "e2down", "uu1", "uu2",
+                                                                  "u12", "t12")})
+    else:
+        raise ValueError("this orbital/spin count needs $hamil_sys lreadhs = T")
+    conv = g.get("converge", {})
+    opts = dict(init=pos["init"], crit=float(conv.get("crit", 1e-8)), maxit0=int(conv.get("maxit0", 20000)),
+                tmax=pos["tmax"], dt=pos["dt"])
+    return cfg, hs, opts
+
+
+def model_from_input(text, hamil_sys=None):
+    """heomq.Model of an input file, with its solver options."""
+    from . import Model
+
+    cfg, hs, opts = to_config(text, hamil_sys)
+    return Model(cfg, hs=hs), opts
+
+
+# ---- state files -----------------------------------------------------------------
+def write_rho_spa(path, model, rho):
+    """rho_spa.st layout: header, then the entries of every ADO in ADO order."""
+    rho = np.ascontiguousarray(rho, dtype=np.complex128)
+    if rho.size != model.lunk:
+        raise ValueError("rho must hold lunk entries")
+    with open(path, "wb") as f:
+        f.write(struct.pack("<5i", model.norbs, model.nspin, model.ncor, model.ntier, model.nalf))
+        f.write(struct.pack("<q", model.nunk))
+        f.write(rho.tobytes())
+
+
+def read_rho_spa(path, model):
+    """A saved state as the initial guess of `model` (fermion/initialize2_spa.f90 without the
+    changed-pattern branch): header fields must match; a state saved at a lower tier fills the
+    ADOs it holds and leaves the rest zero."""
+    with open(path, "rb") as f:
+        norbs, nspin, ncor, jtier, nalf = struct.unpack("<5i", f.read(20))
+        (nunk_saved,) = struct.unpack("<q", f.read(8))
+        data = np.frombuffer(f.read(), dtype=np.complex128)
+    if (norbs, nspin, ncor, nalf) != (model.norbs, model.nspin, model.ncor, model.nalf) or jtier <= 1:
+        raise ValueError("state file does not match the model (norbs, nspin, ncor, nalf)")
+    nnz = model.array("nnz_spa").astype(np.int64)
+    if jtier >= model.ntier and nunk_saved != model.nunk:
+        raise ValueError("incompatible state file: ADO count differs")
+    count = int(nnz[: min(nunk_saved, model.nunk)].sum())
+    if data.size < count:
+        raise ValueError("state file is truncated")
+    rho = np.zeros(model.lunk, dtype=np.complex128)
+    rho[:count] = data[:count]
+    return rho
+
+
+def write_hamil_sys(path, hs):
+    """hamil_sys.data: one sequential unformatted record (4-byte length markers)."""
+    h = np.asfortranarray(np.asarray(hs, dtype=np.complex128))
+    body = h.reshape(-1, order="F").tobytes()
+    with open(path, "wb") as f:
+        f.write(struct.pack("<i", len(body)))
+        f.write(body)
+        f.write(struct.pack("<i", len(body)))
+
+
+def read_hamil_sys(path, nrho):
+    with open(path, "rb") as f:
+        (n,) = struct.unpack("<i", f.read(4))
+        if n != 16 * nrho * nrho:
+            raise ValueError(f"record of {n} bytes, expected {16 * nrho * nrho}")
+        body = f.read(n)
+        (n2,) = struct.unpack("<i", f.read(4))
+    if n2 != n:
+        raise ValueError("record markers differ")
+    return np.frombuffer(body, dtype=np.complex128).reshape(nrho, nrho, order="F")
+
+
+def write_input(cfg, crit=1e-8, maxit0=20000, init=2, tmax=0.0, dt=0.05):
+    """Input-file text of a model configuration (the inverse of to_config for its subset)."""
+    nalf, norbs, nspin = cfg["nalf"], cfg["norbs"], cfg["nspin"]
+    lines = [str(init), str(cfg["ntier"]), str(cfg["nmats"]), str(norbs), str(nspin), str(nalf),
+             " ".join(repr(float(w)) for w in cfg["bandwidth"][:nalf]),
+             " ".join(repr(float(cfg["linewidth"][a][o])) for a in range(nalf) for o in range(norbs)),
+             " ".join(repr(float(t)) for t in cfg["temperature"][:nalf]),
+             " ".join(repr(float(cfg["engyshift"][a][s])) for a in range(nalf) for s in range(nspin)),
+             repr(float(tmax)), repr(float(dt))]
+    job = f"$jobinfo lsparse=T psdjob=T lscreen={'T' if cfg.get('lscreen') else 'F'} $end"
+    lines += [job, "$method methodss=2 $end", f"$converge crit={crit!r} maxit0={maxit0} $end"]
+    if cfg.get("model") == 1:
+        lines.append(f"$para1 eup={cfg['eup']!r} edown={cfg['edown']!r} uu={cfg['uu']!r} $end")
+    elif cfg.get("model") == 4:
+        keys = ("e1up", "e1down", "e2up", "e2down", "uu1", "uu2", "u12", "t12")
+        lines.append("$para4 " + " ".join(f"{k}={float(cfg.get(k, 0.0))!r}" for k in keys) + " $end")
+        if cfg.get("doubledot"):
+            lines.append("$ddots doubledot=T $end")
+    else:
+        lines.append("$hamil_sys lreadhs=T $end")
+    lines.append("$field fieldtype=0 $end")
+    tc = cfg.get("tchar", 0.0)
+    lines.append(" ".join(repr(float(tc[a][s] if isinstance(tc, (list, tuple)) else tc))
+                          for a in range(nalf) for s in range(nspin)))
+    return "\n".join(lines) + "\n"
+
+
+__all__ = ["parse", "to_config", "model_from_input", "write_rho_spa", "read_rho_spa", "write_hamil_sys",
+           "read_hamil_sys", "write_input", "models"]
