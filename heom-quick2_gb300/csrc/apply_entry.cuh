@@ -1,0 +1,125 @@
+// One output entry of the sparse HEOM Liouvillian apply, shared by the plain apply kernel
+// and by the fused inner-solver kernels.
+//
+// Role: tfqmr_double/calc_ax_tfqmr_spa_omp.f90 (steady, with the Tr rho0 row),
+// td/calcderiv_spa_omp.f90 (time-dependent lead shifts, no trace row) and the
+// adjoint of the former.  For entry t the value is
+//   g x  +  same-tier commutator terms of its pattern class  +  one or two signed
+//   gathers per coupled ADO (left and right operator products),
+// where every gather is a precomputed index into the source ADO's stored entries.
+// The higher-tier couplings have coefficients +-i and cost only additions; the
+// lower-tier ones multiply by the bath residues cb, cd.
+//
+// REG selects the regularised operator of the mixed-precision inner solves (see DevCoef):
+// reads of RDO entries (source offset 0) see the Hermitian part (x_q + conj x_q')/2.
+#pragma once
+#include "device.cuh"
+
+namespace heom {
+
+template <typename T>
+__device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V *__restrict__ x, const int32_t *pair, int q)
+{
+    using N = Num<T>;
+    return N::half(N::add(N::load(x[q]), N::conj(N::load(x[__ldg(pair + q)]))));
+}
+
+// y[t] of instance b (x: that instance's vector); t in [0, lunk], lunk = the trace slot
+template <typename T, bool ADJ, bool REG>
+__device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, const DevCoef<T> &C,
+                                                          const typename Num<T>::V *__restrict__ x, int64_t t, int b)
+{
+    using N = Num<T>;
+    using A = typename N::A;
+    if (t == P.lunk) {   // the trace slot
+        A s = N::zero();
+        if (!ADJ && C.trace_on)
+            for (int k = 0; k < P.ntrace; k++)
+                s = N::add(s, REG ? herm_part<T>(x, C.rdo_pair, P.trace_idx[k]) : N::load(x[P.trace_idx[k]]));
+        if (REG) s = N::add(s, N::from_d(0.0, C.reg_scale * N::im(N::load(x[t]))));
+        return s;
+    }
+    const int n = __ldg(P.ent_ado + t);
+    const int off = __ldg(P.ado_off + n);
+    const int p = (int)(t - off);
+    const int c = __ldg(P.ado_cls + n);
+    const typename N::V *hv = C.hval + (int64_t)b * P.nh;
+
+    // g = sum over the drawers of (cgamma + i dipm eshift)
+    A g;
+    if (C.gdiag) g = N::load(C.gdiag[(int64_t)b * P.nado + n]);
+    else {
+        const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
+        double es = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) es += (double)(int8_t)(cnt >> (8 * k)) * C.eshift[b * 4 + k];
+        g = N::add(N::scale(N::load(C.g0[n]), N::sc(C.g0_scale)), N::from_d(0.0, es));
+    }
+    if (ADJ) g = N::conj(g);
+    const bool rdo = REG && off == 0;   // output row and same-tier sources in the RDO block
+    A acc = N::mul(g, rdo ? herm_part<T>(x, C.rdo_pair, (int)t) : N::load(x[t]));
+    if (rdo) {
+        const int q = (int)t, qp = __ldg(C.rdo_pair + q);
+        const A xq = N::load(x[q]);
+        acc = N::add(acc, N::scale(N::sub(xq, N::conj(N::load(x[qp]))), N::sc(0.5 * C.reg_scale)));
+        if (qp == q) acc = N::add(acc, N::from_d(C.reg_scale * N::re(N::load(x[P.lunk])) / C.ndiag, 0.0));
+    }
+
+    // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
+    const int tb = __ldg(P.cls_tptr + c) + p;
+    const int k0 = __ldg(P.term_ptr + tb), k1 = __ldg(P.term_ptr + tb + 1);
+    // one signed sum: right terms (x H) count +, left terms (H x) count - (no divergent branch)
+    A sd = N::zero();
+    for (int k = k0; k < k1; k++) {
+        const uint32_t w = __ldg(P.terms + k);
+        A h = N::load(hv[(w >> 16) & 0x7FFF]);
+        if (ADJ) h = N::conj(h);
+        const A xs = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF)) : N::load(x[off + (int)(w & 0xFFFF)]);
+        const A hx = C.h_real ? N::scale(xs, N::re_s(h)) : N::mul(h, xs);
+        sd = N::add(sd, (w >> 31) ? hx : N::neg(hx));
+    }
+    // forward: acc += i (sum_right - sum_left); adjoint: acc += -i (...)
+    const A dlt = N::mul_i(N::norm(sd));
+    acc = N::add(acc, ADJ ? N::neg(dlt) : dlt);
+
+    // couplings to the neighbouring tiers
+    const int e0 = __ldg(P.coup_ptr + n), e1 = __ldg(P.coup_ptr + n + 1);
+    A ua = N::zero();   // sum of unit-coefficient contributions (times -i at the end)
+    for (int e = e0; e < e1; e++) {
+        const int4 rec = __ldg(P.coup + e);
+        const uint32_t mw = __ldg(P.maps + rec.y + p);
+        if (!mw) continue;
+        const bool cj = rec.z < 0;
+        const uint32_t lo = mw & 0xFFFFu, hi = mw >> 16;
+        A vl = N::zero(), vr = N::zero();
+        const bool src_rdo = REG && rec.x == 0;
+        if (lo) {
+            vl = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            if (cj) vl = N::conj(vl);
+            if (lo & 0x8000u) vl = N::neg(vl);
+        }
+        if (hi) {
+            vr = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            if (cj) vr = N::conj(vr);
+            if (hi & 0x8000u) vr = N::neg(vr);
+        }
+        if (rec.z & kCoefUnit) {
+            // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
+            if (C.unit_on) {
+                ua = N::add(ua, (rec.z & 1) ? N::neg(vl) : vl);
+                ua = N::add(ua, (rec.z & 2) ? N::neg(vr) : vr);
+            }
+        } else {
+            const int cid = rec.z & 0x3FFFFFFF;
+            if (lo) acc = N::add(acc, N::mul(N::load(C.cl[cid]), vl));
+            if (hi) acc = N::add(acc, N::mul(N::load(C.cr[cid]), vr));
+            if ((e - e0) & 1) acc = N::norm(acc);
+        }
+        if (((e - e0) & 3) == 3) ua = N::norm(ua);
+    }
+    acc = N::add(acc, N::mul_i(ua));
+    return acc;
+}
+
+
+}  // namespace heom

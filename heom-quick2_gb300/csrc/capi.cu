@@ -8,6 +8,7 @@
 #include <type_traits>
 
 #include "context.cuh"
+#include "inner.cuh"
 
 namespace heom {
 
@@ -254,14 +255,17 @@ void drandn_stream(int64_t n, std::vector<double> &out)
 }
 
 template <typename T>
-void upload_rt(heom_ctx *c, TfqWork<T> &W)
+void upload_rt_to(heom_ctx *c, typename Num<T>::V *dst, int64_t n)
 {
     using V = typename Num<T>::V;
-    std::vector<V> rt(W.N);
-    for (int64_t i = 0; i < W.N; i++) rt[i] = Num<T>::store_host(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
-    CK(cudaMemcpyAsync(W.rt, rt.data(), sizeof(V) * W.N, cudaMemcpyHostToDevice, c->stream));
+    std::vector<V> rt(n);
+    for (int64_t i = 0; i < n; i++) rt[i] = Num<T>::store_host(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
+    CK(cudaMemcpyAsync(dst, rt.data(), sizeof(V) * n, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
 }
+
+template <typename T>
+void upload_rt(heom_ctx *c, TfqWork<T> &W) { upload_rt_to<T>(c, W.rt, W.N); }
 
 // Run TFQMR iterations until every instance finished; graph-captured chunks of `chunk`
 // iterations, host polls the done flags between chunks.
@@ -383,7 +387,9 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
 // the regularised operator (DevCoef::reg): it agrees with A on vectors whose RDO block is
 // Hermitian and whose trace unknown is zero, and is nonsingular where A has the null space
 // spanned by the free trace unknown and the anti-Hermitian stationary RDO directions; the
-// inner Krylov solves then stay well conditioned in low precision.
+// inner Krylov solves then stay well conditioned in low precision.  The inner solves run
+// the fused TFQMR of inner.cuh from one CUDA graph of kInnerChunk iterations plus a
+// residual check, instantiated once and replayed for every round.
 template <typename T>
 void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, const double2 *rhs,
                   const DevCoef<double> &K64, const DevCoef<T> &KT, double2 *r64, std::vector<double> &norms,
@@ -391,19 +397,34 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   const std::function<void(const double2 *, double2 *)> &residual,
                   const std::function<void(const double2 *)> &batch_norms)
 {
+    constexpr int kInnerChunk = 25;   // 50 applies between residual checks, as in the reference driver
     const int64_t N = c->lunk + 1;
     const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 3e-7);
-    TfqWork<T> W;
-    tfq_alloc<T>(W, nbatch, N, c->stream);
+    InnerWork<T> W;
+    inner_alloc<T>(W, nbatch, N, c->stream);
     typename Num<T>::V *gd = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    auto release = [&] {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        inner_free(W);
+        if (gd) cudaFree(gd);
+    };
     try {
-        upload_rt(c, W);
+        upload_rt_to<T>(c, W.rt, N);
         DevCoef<T> KR = regularised<T>(c, KT);
         // per-instance ADO diagonals, so the inner applies do no FP64 arithmetic
         CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * std::max<int64_t>(1, (int64_t)c->dfwd.view.nado * nbatch)));
         fill_gdiag<T>(c->dfwd.view, KR, gd, nbatch, c->stream);
         KR.gdiag = gd;
         aux++;
+        const DevCoef<T> KI = rhs ? KT : KR;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        inner_chunk<T>(W, c->dfwd.view, KI, kInnerChunk, c->stream);
+        CK(cudaStreamEndCapture(c->stream, &graph));
+        CK(cudaGraphInstantiate(&gexec, graph, 0));
+        std::vector<InnerState> st(nbatch);
         int round = 0;
         for (; round < std::max(1, o.max_refine); round++) {
             if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
@@ -415,29 +436,34 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
                 vec_from_d<T>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride,
                               norms[b] <= o.crit ? 0.0 : 1.0 / norms[b], c->stream);
+            aux += nbatch;
             // the scaled inner problem has ||b|| = 1: stop at max(itol, crit / ||r||) (the most
-            // demanding instance sets it), by TFQMR's own test or the every-50-applies test, or
-            // after 4 such tests without halving the residual
+            // demanding instance sets it), or at the arithmetic's floor
             double tgt = 1.0;
             for (double v : norms) if (v > o.crit) tgt = std::min(tgt, o.crit / v);
             tgt = std::max(tgt, itol);
-            tfq_start<T>(W, tgt, nlim, tgt, 0.0, o.stag_window > 0 ? o.stag_window : 16, c->stream);
-            aux += kTfqStartLaunches + nbatch;
-            int it = 0;
-            tfq_run<T>(c, W, make_apply<T>(c, rhs ? KT : KR, nbatch, W.vstride, false), nlim, it, launches);
-            std::vector<TfqState> st(nbatch);
-            CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
-            int axb = 0;
-            for (auto &sv : st) { axb = std::max(axb, sv.axb); last_ierr = sv.ierr; }
-            total_iters += axb;
+            inner_start<T>(W, tgt, nlim, o.stag_window > 0 ? o.stag_window : 16, c->stream);
+            aux += kInnerStartLaunches;
+            for (int iters = 0;;) {
+                CK(cudaGraphLaunch(gexec, c->stream));
+                iters += kInnerChunk;
+                launches += (int64_t)kInnerChunk * kInnerIterationLaunches + kInnerCheckLaunches;
+                CK(cudaMemcpyAsync(st.data(), W.st, sizeof(InnerState) * nbatch, cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                bool any = false;
+                for (const auto &sv : st) any = any || !sv.done;
+                if (!any || iters > nlim + kInnerChunk) break;
+            }
+            int applies = 0;
+            for (const auto &sv : st) { applies = std::max(applies, 2 * sv.n + sv.checks); last_ierr = sv.ierr; }
+            total_iters += applies;
             for (int b = 0; b < nbatch; b++)
-                if (norms[b] > o.crit) vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.x + (int64_t)b * W.vstride, c->stream), aux++;
+                if (norms[b] > o.crit) vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.xs + (int64_t)b * W.vstride, c->stream), aux++;
         }
         if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
         rounds = round;
-    } catch (...) { tfq_free(W); if (gd) cudaFree(gd); throw; }
-    tfq_free(W);
-    cudaFree(gd);
+    } catch (...) { release(); throw; }
+    release();
 }
 
 // Solve A x = rhs (rhs = e_trace when rhs == nullptr) for nbatch instances, in FP64 or
@@ -592,13 +618,15 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
             CK(cudaMemcpy(c->d_rdo_pair, pair.data(), sizeof(int32_t) * nz0, cudaMemcpyHostToDevice));
             CK(cudaMalloc((void **)&c->d_rdo_upper, sizeof(int32_t) * std::max(1, nz0)));
             CK(cudaMemcpy(c->d_rdo_upper, upper.data(), sizeof(int32_t) * nz0, cudaMemcpyHostToDevice));
-            // regularising weight: the largest bath decay rate |Re cgamma|, a typical diagonal
-            // magnitude of the operator
+            // regularising weight: minus the largest bath decay rate |Re cgamma|, a typical
+            // diagonal magnitude of the operator; the negative sign puts the regularised
+            // directions on the decaying side of the spectrum with the physical ones (about
+            // 12 % fewer inner applies than the positive sign on the double-dot models)
             int nvar = 2 * t->norbs * t->nspin * t->nalf * t->ncor;
             const cd *cg = reinterpret_cast<const cd *>(t->cgamma);
             double m = 0;
             for (int k = 0; k < nvar; k++) m = std::max(m, std::abs(cg[k].real()));
-            c->reg_scale = m > 0 ? m : 1.0;
+            c->reg_scale = m > 0 ? -m : -1.0;
             // Chebyshev spectral width (td/prechebyshev.f90:56-110): spread of Re(sum of the
             // drawers' cgamma) over every ADO of the index table, the RDO (0) included
             double lo = 0.0, hi = 0.0;

@@ -1,0 +1,389 @@
+// Fused batched TFQMR for the inner solves of mixed-precision refinement (see inner.cuh
+// for the arrangement of the iteration).
+#include <cmath>
+
+#include "apply_entry.cuh"
+#include "inner.cuh"
+
+namespace heom {
+
+namespace {
+
+constexpr int NT = 256;
+
+// Per-thread accumulation of Re(a^H b) in the vectors' number type; warp_total() sums the
+// 32 lanes (every lane must call it) and returns the warp's total in FP64 on every lane.
+template <typename T> struct WarpAcc;
+template <> struct WarpAcc<double> {
+    double v = 0;
+    __device__ __forceinline__ void add(double2 a, double2 b) { v = fma(a.x, b.x, fma(a.y, b.y, v)); }
+    __device__ __forceinline__ double warp_total()
+    {
+        double s = v;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        return s;
+    }
+};
+template <> struct WarpAcc<float> {
+    float v = 0.f;
+    __device__ __forceinline__ void add(float2 a, float2 b) { v = fmaf(a.x, b.x, fmaf(a.y, b.y, v)); }
+    __device__ __forceinline__ double warp_total()
+    {
+        float s = v;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        return (double)s;
+    }
+};
+template <> struct WarpAcc<DF> {
+    f2r v{0.f, 0.f};
+    __device__ __forceinline__ void add(f2c a, f2c b) { v = f2r_add(v, f2r_add(f2r_mul(a.re, b.re), f2r_mul(a.im, b.im))); }
+    __device__ __forceinline__ double warp_total()
+    {
+        f2r s = f2r_norm(v);
+        for (int o = 16; o > 0; o >>= 1) {
+            const f2r q{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
+            s = f2r_add(s, q);
+        }
+        return (double)s.hi + (double)s.lo;
+    }
+};
+
+// K per-warp totals -> one partial per block (thread 0 sums the warps in a fixed order).
+template <int K>
+__device__ __forceinline__ void block_partials(const double (&wt)[K], double *out)
+{
+    __shared__ double sh[K][NT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) sh[k][wid] = wt[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double s = 0;
+            for (int w = 0; w < NT / 32; w++) s += sh[k][w];
+            out[k] = s;
+        }
+}
+
+// In the one-block-per-instance finalisers: the grand totals of the K partials of
+// instance b, summed in a fixed order, valid in thread 0.
+template <int K>
+__device__ __forceinline__ void grand_totals(const double *part, int nblk, int b, double (&tot)[K])
+{
+    __shared__ double sh[K][NT / 32];
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) s[k] = 0;
+    for (int i = threadIdx.x; i < nblk; i += NT)
+#pragma unroll
+        for (int k = 0; k < K; k++) s[k] += part[3 * ((size_t)b * nblk + i) + k];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+        if (lane == 0) sh[k][wid] = s[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double a = 0;
+            for (int w = 0; w < NT / 32; w++) a += sh[k][w];
+            tot[k] = a;
+        }
+}
+
+#define FUSED_SETUP                                            \
+    using N = Num<T>;                                          \
+    using A = typename N::A;                                   \
+    const int b = blockIdx.y;                                  \
+    if (W.st[b].done) return;                                  \
+    const int64_t o = (int64_t)b * W.vstride;                  \
+    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;  \
+    double *part = W.part + 3 * ((size_t)b * W.nblk + blockIdx.x);
+
+// w = b, other vectors 0; partials ||b||^2, <r~, b>
+template <typename T>
+__global__ void k_in_init(InnerWork<T> W)
+{
+    using N = Num<T>;
+    using A = typename N::A;
+    const int b = blockIdx.y;
+    const int64_t o = (int64_t)b * W.vstride;
+    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;
+    WarpAcc<T> bb, rb;
+    if (t < W.N) {
+        const A bv = N::load(W.b[o + t]);
+        const typename N::V z = N::store(N::zero());
+        W.w[o + t] = N::store(bv);
+        W.x[o + t] = z; W.xs[o + t] = z; W.y[o + t] = z; W.d[o + t] = z; W.v[o + t] = z; W.u2[o + t] = z;
+        bb.add(bv, bv);
+        rb.add(N::load(W.rt[t]), bv);
+    }
+    const double wt[2] = {bb.warp_total(), rb.warp_total()};
+    block_partials<2>(wt, W.part + 3 * ((size_t)b * W.nblk + blockIdx.x));
+}
+
+template <typename T>
+__global__ void k_in_init_fin(InnerWork<T> W, double crit, int nlim, int stag_window)
+{
+    const int b = blockIdx.x;
+    double tot[2];
+    grand_totals<2>(W.part, W.nblk, b, tot);
+    if (threadIdx.x != 0) return;
+    InnerState s = {};
+    s.r0 = sqrt(tot[0]);
+    s.tau = tot[0];
+    s.rho = tot[1];
+    s.crit = crit; s.nlim = nlim; s.stag_window = stag_window;
+    s.best = s.r0; s.ext_resid = s.r0;
+    if (s.r0 <= crit) { s.done = 1; s.conv = 1; }
+    else if (s.rho == 0.0) { s.done = 1; s.ierr = 8; }
+    W.st[b] = s;
+    InnerCoef<T> k;
+    k.beta = k.alpha = k.alpha_prev = k.dd1 = k.eta1 = k.dd2 = k.eta2 = Num<T>::sc(0.0);
+    W.cf[b] = k;
+}
+
+// B: u1 = A w + beta u2, the pending x / d updates, y = w + beta y2, v = u1 + beta (u2 + beta v)
+template <typename T, bool REG>
+__global__ void __launch_bounds__(NT, 4) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+{
+    FUSED_SETUP
+    WarpAcc<T> sg;
+    if (t < W.N) {
+        const A aw = apply_entry<T, false, REG>(P, C, W.w + o, t, b);
+        const InnerCoef<T> &k = W.cf[b];
+        const A u2 = N::load(W.u2[o + t]), vo = N::load(W.v[o + t]), yo = N::load(W.y[o + t]);
+        const A u1 = N::add(aw, N::scale(u2, k.beta));
+        W.u1[o + t] = N::store(u1);
+        const A d1 = N::add(yo, N::scale(N::load(W.d[o + t]), k.dd1));
+        const A y2 = N::sub(yo, N::scale(vo, k.alpha_prev));
+        const A d2 = N::add(y2, N::scale(d1, k.dd2));
+        W.d[o + t] = N::store(d2);
+        W.x[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+        W.y[o + t] = N::store(N::add(N::load(W.w[o + t]), N::scale(y2, k.beta)));
+        const A vn = N::add(u1, N::scale(N::add(u2, N::scale(vo, k.beta)), k.beta));
+        W.v[o + t] = N::store(vn);
+        sg.add(N::load(W.rt[t]), vn);
+    }
+    const double wt[1] = {sg.warp_total()};
+    block_partials<1>(wt, part);
+}
+
+template <typename T>
+__global__ void k_in_b_fin(InnerWork<T> W)
+{
+    const int b = blockIdx.x;
+    if (W.st[b].done) return;
+    double tot[1];
+    grand_totals<1>(W.part, W.nblk, b, tot);
+    if (threadIdx.x != 0) return;
+    InnerState s = W.st[b];
+    const double sigma = tot[0];
+    if (sigma == 0.0 || !isfinite(sigma)) { s.done = 1; s.ierr = 8; }
+    else {
+        s.alpha = s.rho / sigma;
+        W.cf[b].alpha = Num<T>::sc(s.alpha);
+    }
+    W.st[b] = s;
+}
+
+// A: u2 = u1 - alpha A v, w1 = w - alpha u1, w = w1 - alpha u2
+template <typename T, bool REG>
+__global__ void __launch_bounds__(NT, 4) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+{
+    FUSED_SETUP
+    WarpAcc<T> a1, a2, a3;
+    if (t < W.N) {
+        const A av = apply_entry<T, false, REG>(P, C, W.v + o, t, b);
+        const typename N::S al = W.cf[b].alpha;
+        const A u1 = N::load(W.u1[o + t]);
+        const A u2 = N::sub(u1, N::scale(av, al));
+        W.u2[o + t] = N::store(u2);
+        const A w1 = N::sub(N::load(W.w[o + t]), N::scale(u1, al));
+        const A w2 = N::sub(w1, N::scale(u2, al));
+        W.w[o + t] = N::store(w2);
+        a1.add(w1, w1);
+        a2.add(w2, w2);
+        a3.add(N::load(W.rt[t]), w2);
+    }
+    const double wt[3] = {a1.warp_total(), a2.warp_total(), a3.warp_total()};
+    block_partials<3>(wt, part);
+}
+
+template <typename T>
+__global__ void k_in_a_fin(InnerWork<T> W)
+{
+    const int b = blockIdx.x;
+    if (W.st[b].done) return;
+    double tot[3];
+    grand_totals<3>(W.part, W.nblk, b, tot);
+    if (threadIdx.x != 0) return;
+    InnerState s = W.st[b];
+    const double al = s.alpha;
+    const double dd1 = s.var * s.eta / al;
+    s.var = tot[0] / s.tau;
+    double cs = 1.0 / (1.0 + s.var);
+    s.tau = tot[0] * cs;
+    s.eta = al * cs;
+    const double eta1 = s.eta;
+    const double dd2 = s.var * s.eta / al;
+    s.var = tot[1] / s.tau;
+    cs = 1.0 / (1.0 + s.var);
+    s.tau = tot[1] * cs;
+    s.eta = al * cs;
+    s.n += 1;
+    s.unrm = sqrt((double)(2 * s.n + 1) * s.tau) / s.r0;
+    s.beta = tot[2] / s.rho;
+    s.rho = tot[2];
+    if (tot[2] == 0.0 || !isfinite(s.beta)) { s.done = 1; s.ierr = 8; }
+    W.st[b] = s;
+    using N = Num<T>;
+    InnerCoef<T> k = W.cf[b];
+    k.beta = N::sc(s.beta);
+    k.alpha_prev = N::sc(al);
+    k.dd1 = N::sc(dd1);
+    k.eta1 = N::sc(eta1);
+    k.dd2 = N::sc(dd2);
+    k.eta2 = N::sc(s.eta);
+    W.cf[b] = k;
+}
+
+// xs = x + the pending updates of the last iteration
+template <typename T>
+__global__ void k_in_x(InnerWork<T> W)
+{
+    using N = Num<T>;
+    using A = typename N::A;
+    const int b = blockIdx.y;
+    if (W.st[b].done) return;
+    const int64_t o = (int64_t)b * W.vstride;
+    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;
+    if (t >= W.N) return;
+    const InnerCoef<T> &k = W.cf[b];
+    const A yo = N::load(W.y[o + t]);
+    const A d1 = N::add(yo, N::scale(N::load(W.d[o + t]), k.dd1));
+    const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[o + t]), k.alpha_prev)), N::scale(d1, k.dd2));
+    W.xs[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+}
+
+// partial ||b - A xs||^2
+template <typename T, bool REG>
+__global__ void __launch_bounds__(NT, 4) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+{
+    FUSED_SETUP
+    WarpAcc<T> ee;
+    if (t < W.N) {
+        const A e = N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b));
+        ee.add(e, e);
+    }
+    const double wt[1] = {ee.warp_total()};
+    block_partials<1>(wt, part);
+}
+
+template <typename T>
+__global__ void k_in_chk_fin(InnerWork<T> W)
+{
+    const int b = blockIdx.x;
+    if (W.st[b].done) return;
+    double tot[1];
+    grand_totals<1>(W.part, W.nblk, b, tot);
+    if (threadIdx.x != 0) return;
+    InnerState s = W.st[b];
+    const double e = sqrt(tot[0]);
+    s.ext_resid = e;
+    s.checks += 1;
+    if (e <= s.crit) { s.done = 1; s.conv = 1; s.ierr = 0; }
+    else if (s.n >= s.nlim) { s.done = 1; s.ierr = 4; }
+    else if (s.stag_window) {
+        // the arithmetic's floor: the true residual 10x above TFQMR's bound, or
+        // stag_window checks without halving the best true residual
+        if (s.n > 2 && e > 10.0 * s.unrm * s.r0) { s.done = 1; s.ierr = 4; }
+        else if (e < 0.5 * s.best) { s.best = e; s.stag = 0; }
+        else if (++s.stag >= s.stag_window) { s.done = 1; s.ierr = 4; }
+    }
+    if (!isfinite(e)) { s.done = 1; s.ierr = 8; }
+    W.st[b] = s;
+}
+
+}  // namespace
+
+template <typename T>
+void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
+{
+    using V = typename Num<T>::V;
+    W.nbatch = nbatch;
+    W.N = N;
+    W.vstride = (N + 63) / 64 * 64;
+    W.nblk = (int)((N + NT - 1) / NT);
+    const size_t vbytes = sizeof(V) * (size_t)W.vstride * nbatch;
+    // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
+    auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(InnerState) * nbatch) +
+                         rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
+    char *p = nullptr;
+    if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the inner-solver workspace failed");
+    if (cudaMemsetAsync(p, 0, total, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaFree(p);
+        fail(HEOM_E_CUDA, "clearing the inner-solver workspace failed");
+    }
+    W.mem = p;
+    auto take = [&](size_t bytes) { char *q = p; p += rounded(bytes); return q; };
+    W.x = (V *)take(vbytes); W.xs = (V *)take(vbytes); W.b = (V *)take(vbytes); W.w = (V *)take(vbytes);
+    W.y = (V *)take(vbytes); W.d = (V *)take(vbytes); W.v = (V *)take(vbytes); W.u1 = (V *)take(vbytes);
+    W.u2 = (V *)take(vbytes);
+    W.rt = (V *)take(sizeof(V) * (size_t)W.vstride);
+    W.st = (InnerState *)take(sizeof(InnerState) * nbatch);
+    W.cf = (InnerCoef<T> *)take(sizeof(InnerCoef<T>) * nbatch);
+    W.part = (double *)take(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
+}
+
+template <typename T>
+void inner_free(InnerWork<T> &W)
+{
+    if (W.mem) cudaFree(W.mem);
+    W = InnerWork<T>();
+}
+
+template <typename T>
+void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaStream_t s)
+{
+    dim3 g((unsigned)W.nblk, (unsigned)W.nbatch);
+    k_in_init<T><<<g, NT, 0, s>>>(W);
+    k_in_init_fin<T><<<W.nbatch, NT, 0, s>>>(W, crit, nlim, stag_window);
+}
+
+template <typename T>
+void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int iters, cudaStream_t s)
+{
+    dim3 g((unsigned)W.nblk, (unsigned)W.nbatch);
+    const unsigned nb = (unsigned)W.nbatch;
+    DevPlan Q = P;
+    Q.order = nullptr;   // entry order: coalesced epilogue access
+    for (int i = 0; i < iters; i++) {
+        if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_b<T, false><<<g, NT, 0, s>>>(Q, C, W);
+        k_in_b_fin<T><<<nb, NT, 0, s>>>(W);
+        if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_a<T, false><<<g, NT, 0, s>>>(Q, C, W);
+        k_in_a_fin<T><<<nb, NT, 0, s>>>(W);
+    }
+    k_in_x<T><<<g, NT, 0, s>>>(W);
+    if (C.reg) k_in_chk<T, true><<<g, NT, 0, s>>>(Q, C, W);
+    else k_in_chk<T, false><<<g, NT, 0, s>>>(Q, C, W);
+    k_in_chk_fin<T><<<nb, NT, 0, s>>>(W);
+}
+
+#define INST(T)                                                                              \
+    template void inner_alloc<T>(InnerWork<T> &, int, int64_t, cudaStream_t);                \
+    template void inner_free<T>(InnerWork<T> &);                                              \
+    template void inner_start<T>(InnerWork<T> &, double, int, int, cudaStream_t);             \
+    template void inner_chunk<T>(InnerWork<T> &, const DevPlan &, const DevCoef<T> &, int, cudaStream_t);
+INST(double)
+INST(float)
+INST(DF)
+
+}  // namespace heom
