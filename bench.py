@@ -35,6 +35,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="profiler run: warm-up solves, then one timed mixed solve; prints one short line")
+    ap.add_argument("--profile-inner", action="store_true",
+                    help="profiler run of the two fused FP32x2 inner-iteration kernels: 3 warm-up + 2 timed launches each")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
     return ap.parse_args()
@@ -127,12 +129,12 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "apply_fp32x2_dqd_L4_batch8.md")
+def profile_traffic(name, key="dram_bytes_per_launch"):
+    """DRAM bytes per launch of a kernel from a committed ncu summary under profiles/, if any."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1].split()[0])
     except (OSError, ValueError):
         pass
@@ -218,6 +220,13 @@ def run_gb300(args, ws, rank, local, dist):
         batch.close()
         ctx.close()
         return 0
+    if args.profile_inner:
+        (sb, sa), (bb, ba) = ctx.bench_inner(heomq.PREC_MIXED, reps=2, nbatch=B)
+        print(json.dumps({"profile_inner": True, "batch": B, "k_in_b_us": sb * 1e6, "k_in_a_us": sa * 1e6,
+                          "alg_bytes": [bb, ba]}), flush=True)
+        batch.close()
+        ctx.close()
+        return 0
     for _ in range(args.warmup):
         step(heomq.PREC_MIXED)
     if args.profile:
@@ -270,12 +279,17 @@ def run_gb300(args, ws, rank, local, dist):
     h2d = B * L * 16 + B * 4 * 8 + B * model.nrho ** 2 * 16
     d2h = B * L * 16
 
-    # roofline of the dominant kernel: the FP32x2 apply over the batch
+    # roofline of the dominant kernel: the first fused kernel of an inner TFQMR iteration
+    # (apply of w + the first half of the vector updates) over the batch; the second one and
+    # the plain apply beside it
+    (sb, sa), (bb, ba) = ctx.bench_inner(heomq.PREC_MIXED, reps=20, nbatch=B)
     sec, alg_bytes = ctx.bench_apply(heomq.PREC_MIXED, reps=20, nbatch=B)
     sec64, alg64 = ctx.bench_apply(heomq.PREC_FP64, reps=10, nbatch=B)
     peak, peak_kind = measured_peak_hbm()
-    achieved = alg_bytes / sec / 1e9
-    traffic = profile_traffic()
+    achieved = bb / sb / 1e9
+    prof = "inner_fp32x2_dqd_L4_batch8.md"
+    traffic = profile_traffic(prof, "dram_bytes_per_launch_k_in_b")
+    traffic_a = profile_traffic(prof, "dram_bytes_per_launch_k_in_a")
     # accuracy: both paths against a reference steady state refined in FP64 to ||b - A x|| <= 1e-12
     # (mixed refinement; FP64 TFQMR alone stalls near 2e-10 on this model)
     info_ref = step(heomq.PREC_FP64_REFINED, crit=1e-12, refine=16, check=False)
@@ -308,10 +322,15 @@ def run_gb300(args, ws, rank, local, dist):
                        "current_reference": "steady state refined with FP64 inner solves to ||b - A x|| <= 1e-12",
                        "current_reference_resid": info_ref.resid},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_apply<FP32x2> over the batch",
-                         "note": "issue-bound on the FP32/ALU pipes (double-float arithmetic, ~75% issue "
-                                 "utilisation), not HBM-bound: profiles/apply_fp32x2_dqd_L4_batch8.md",
-                         "apply_us": sec * 1e6, "alg_bytes_per_launch": alg_bytes},
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_in_b<FP32x2, regularised>: apply of w plus the fused vector updates, over the batch",
+                         "kernel_us": sb * 1e6, "alg_bytes_per_launch": bb,
+                         "k_in_a": {"kernel_us": sa * 1e6, "alg_bytes_per_launch": ba, "achieved": ba / sa / 1e9,
+                                    "traffic": traffic_a},
+                         "plain_apply": {"kernel_us": sec * 1e6, "alg_bytes_per_launch": alg_bytes,
+                                         "achieved": alg_bytes / sec / 1e9},
+                         "note": "the apply inside is issue-bound on the FP32/ALU pipes (double-float arithmetic); "
+                                 "the fused vector updates use the HBM bandwidth it leaves idle: profiles/" + prof},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -909,79 +909,147 @@ int heom_solve_batch(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batc
     return rc;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device inputs of the measurement hooks: nbatch copies of the context's H values and lead
+// shifts, and the matching ADO diagonals of the FP32 / FP32x2 applies.
+struct BenchInputs {
+    std::vector<void *> blocks;
+    void *hv = nullptr, *gdiag = nullptr;
+    double *es = nullptr;
+    ~BenchInputs() { for (void *p : blocks) cudaFree(p); }
+    void *alloc(size_t n) { void *p = nullptr; CK(cudaMalloc(&p, n)); blocks.push_back(p); return p; }
+};
+
+void bench_inputs(heom_ctx *c, int precision, int nbatch, BenchInputs &I)
+{
+    const size_t nh = c->hst.rows.size();
+    I.hv = I.alloc(16 * std::max<size_t>(1, nh) * nbatch);
+    I.es = (double *)I.alloc(sizeof(double) * 4 * nbatch);
+    std::vector<double> e(4 * (size_t)nbatch);
+    for (int b = 0; b < nbatch; b++) for (int k = 0; k < 4; k++) e[4 * b + k] = c->eleadinfty[k];
+    CK(cudaMemcpyAsync(I.es, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice, c->stream));
+    std::vector<double2> h64; std::vector<float2> h32; std::vector<float4> hdf; int real;
+    hvalues(c, c->hs_host.data(), h64, h32, hdf, real);
+    for (int b = 0; b < nbatch; b++) {
+        if (precision == HEOM_PREC_FP64 || precision == HEOM_PREC_FP64_REFINED)
+            CK(cudaMemcpyAsync((double2 *)I.hv + b * nh, h64.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
+        else if (precision == HEOM_PREC_MIXED) CK(cudaMemcpyAsync((float4 *)I.hv + b * nh, hdf.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
+        else CK(cudaMemcpyAsync((float2 *)I.hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
+    }
+    I.gdiag = I.alloc(16 * std::max<size_t>(1, (size_t)c->dfwd.view.nado * nbatch));
+    if (precision == HEOM_PREC_MIXED) {
+        DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = I.es;
+        fill_gdiag<DF>(c->dfwd.view, K, (float4 *)I.gdiag, nbatch, c->stream);
+    } else if (precision == HEOM_PREC_MIXED_FP32) {
+        DevCoef<float> K = main_coef<float>(c, false); K.eshift = I.es;
+        fill_gdiag<float>(c->dfwd.view, K, (float2 *)I.gdiag, nbatch, c->stream);
+    } else if (precision == HEOM_PREC_FP64_REFINED) {
+        DevCoef<double> K = main_coef<double>(c, false); K.eshift = I.es;
+        fill_gdiag<double>(c->dfwd.view, K, (double2 *)I.gdiag, nbatch, c->stream);
+    }
+    CK(cudaStreamSynchronize(c->stream));
+}
+
+// the regularised coefficient set of an inner solve over the measurement inputs
+template <typename T> DevCoef<T> bench_coef(heom_ctx *c, const BenchInputs &I)
+{
+    DevCoef<T> K = regularised<T>(c, main_coef<T>(c, false));
+    K.hval = (const typename Num<T>::V *)I.hv;
+    K.eshift = I.es;
+    K.gdiag = (const typename Num<T>::V *)I.gdiag;
+    return K;
+}
+
+// the plan's bytes (heom_ctx_stats entry 8)
+double plan_bytes(heom_ctx *c)
+{
+    double st[9];
+    heom_ctx_stats(c, st);
+    return st[8];
+}
+
+template <typename T>
+void time_inner(heom_ctx *c, const BenchInputs &I, int nbatch, int reps, double *seconds, double *bytes)
+{
+    const int64_t N = c->lunk + 1;
+    InnerWork<T> W;
+    inner_alloc<T>(W, nbatch, N, c->stream);
+    try {
+        upload_rt_to<T>(c, W.rt, N);
+        float mb = 0, ma = 0;
+        inner_time<T>(W, c->dfwd.view, bench_coef<T>(c, I), reps, c->stream, mb, ma);
+        if (seconds) { seconds[0] = mb * 1e-3; seconds[1] = ma * 1e-3; }
+        // algorithmic bytes per launch: the apply's (source read once, result written once per
+        // instance, plus the plan), the epilogue's vectors once per instance, r~ once
+        const double v = (double)N * sizeof(typename Num<T>::V), pb = plan_bytes(c);
+        if (bytes) {
+            bytes[0] = nbatch * (2.0 + 10.0) * v + v + pb;   // B: reads u2 y v d x, writes y v d x
+            bytes[1] = nbatch * (2.0 + 3.0) * v + v + pb;    // A: reads u1 w, writes w
+        }
+    } catch (...) { inner_free(W); throw; }
+    inner_free(W);
+}
+
+}  // namespace
+
+extern "C" {
+
 int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes)
 {
     return guarded([&] {
         require_ctx(c);
         if (reps < 1) reps = 1;
         if (nbatch < 1) nbatch = 1;
-        int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64;
-        size_t nh = c->hst.rows.size();
-        std::vector<void *> blocks;
-        auto cleanup = [&] { for (void *p : blocks) cudaFree(p); };
-        try {
-            void *xin = nullptr, *yout = nullptr, *hv = nullptr;
-            double *es = nullptr;
-            CK(cudaMalloc(&xin, 16 * (size_t)vs * nbatch)); blocks.push_back(xin);
-            CK(cudaMalloc(&yout, 16 * (size_t)vs * nbatch)); blocks.push_back(yout);
-            CK(cudaMalloc(&hv, 16 * nh * nbatch)); blocks.push_back(hv);
-            CK(cudaMalloc((void **)&es, sizeof(double) * 4 * nbatch)); blocks.push_back(es);
-            CK(cudaMemsetAsync(xin, 0, 16 * (size_t)vs * nbatch, c->stream));
-            std::vector<double> e(4 * (size_t)nbatch);
-            for (int b = 0; b < nbatch; b++) for (int k = 0; k < 4; k++) e[4 * b + k] = c->eleadinfty[k];
-            CK(cudaMemcpyAsync(es, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice, c->stream));
-            std::vector<double2> h64; std::vector<float2> h32; std::vector<float4> hdf; int real;
-            hvalues(c, c->hs_host.data(), h64, h32, hdf, real);
-            for (int b = 0; b < nbatch; b++) {
-                if (precision == HEOM_PREC_FP64) CK(cudaMemcpyAsync((double2 *)hv + b * nh, h64.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
-                else if (precision == HEOM_PREC_MIXED) CK(cudaMemcpyAsync((float4 *)hv + b * nh, hdf.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
-                else CK(cudaMemcpyAsync((float2 *)hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
-            }
-            void *gdiag = nullptr;
-            CK(cudaMalloc(&gdiag, 16 * std::max<size_t>(1, (size_t)c->dfwd.view.nado * nbatch))); blocks.push_back(gdiag);
-            if (precision == HEOM_PREC_MIXED) {
-                DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = es;
-                fill_gdiag<DF>(c->dfwd.view, K, (float4 *)gdiag, nbatch, c->stream);
+        const int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64;
+        BenchInputs I;
+        bench_inputs(c, precision, nbatch, I);
+        void *xin = I.alloc(16 * (size_t)vs * nbatch), *yout = I.alloc(16 * (size_t)vs * nbatch);
+        CK(cudaMemsetAsync(xin, 0, 16 * (size_t)vs * nbatch, c->stream));
+        // the apply of each solver precision: FP64, and the regularised FP32 / FP32x2 applies
+        // of the mixed-precision inner solves
+        auto run = [&] {
+            if (precision == HEOM_PREC_FP64) {
+                DevCoef<double> K = main_coef<double>(c, false); K.hval = (double2 *)I.hv; K.eshift = I.es;
+                launch_apply<double, false>(c->dfwd.view, K, (double2 *)xin, (double2 *)yout, nbatch, vs, nullptr, c->stream);
+            } else if (precision == HEOM_PREC_MIXED) {
+                launch_apply<DF, false>(c->dfwd.view, bench_coef<DF>(c, I), (float4 *)xin, (float4 *)yout, nbatch, vs, nullptr, c->stream);
             } else if (precision == HEOM_PREC_MIXED_FP32) {
-                DevCoef<float> K = main_coef<float>(c, false); K.eshift = es;
-                fill_gdiag<float>(c->dfwd.view, K, (float2 *)gdiag, nbatch, c->stream);
-            }
-            CK(cudaStreamSynchronize(c->stream));
-            // the apply of each solver precision: FP64, and the regularised FP32 / FP32x2 applies
-            // of the mixed-precision inner solves
-            auto run = [&] {
-                if (precision == HEOM_PREC_FP64) {
-                    DevCoef<double> K = main_coef<double>(c, false); K.hval = (double2 *)hv; K.eshift = es;
-                    launch_apply<double, false>(c->dfwd.view, K, (double2 *)xin, (double2 *)yout, nbatch, vs, nullptr, c->stream);
-                } else if (precision == HEOM_PREC_MIXED) {
-                    DevCoef<DF> K = regularised<DF>(c, main_coef<DF>(c, false)); K.hval = (float4 *)hv; K.eshift = es;
-                    K.gdiag = (const float4 *)gdiag;
-                    launch_apply<DF, false>(c->dfwd.view, K, (float4 *)xin, (float4 *)yout, nbatch, vs, nullptr, c->stream);
-                } else if (precision == HEOM_PREC_MIXED_FP32) {
-                    DevCoef<float> K = regularised<float>(c, main_coef<float>(c, false)); K.hval = (float2 *)hv; K.eshift = es;
-                    K.gdiag = (const float2 *)gdiag;
-                    launch_apply<float, false>(c->dfwd.view, K, (float2 *)xin, (float2 *)yout, nbatch, vs, nullptr, c->stream);
-                } else fail(HEOM_E_ARG, "unknown precision");
-            };
-            cudaEvent_t e0, e1;
-            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
-            for (int w = 0; w < 3; w++) run();
-            CK(cudaEventRecord(e0, c->stream));
-            for (int r = 0; r < reps; r++) run();
-            CK(cudaEventRecord(e1, c->stream));
-            CK(cudaEventSynchronize(e1));
-            CK(cudaGetLastError());
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            cudaEventDestroy(e0); cudaEventDestroy(e1);
-            if (seconds) *seconds = ms * 1e-3 / reps;
-            double st[9];
-            heom_ctx_stats(c, st);
-            double s = precision == HEOM_PREC_MIXED_FP32 ? 8.0 : 16.0;
-            // algorithmic bytes of one launch: x read once, y written once per instance, plus the plan
-            if (bytes) *bytes = nbatch * 2.0 * (double)N * s + st[8];
-            cleanup();
-        } catch (...) { cleanup(); throw; }
+                launch_apply<float, false>(c->dfwd.view, bench_coef<float>(c, I), (float2 *)xin, (float2 *)yout, nbatch, vs, nullptr, c->stream);
+            } else fail(HEOM_E_ARG, "unknown precision");
+        };
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+        for (int w = 0; w < 3; w++) run();
+        CK(cudaEventRecord(e0, c->stream));
+        for (int r = 0; r < reps; r++) run();
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        if (seconds) *seconds = ms * 1e-3 / reps;
+        const double s = precision == HEOM_PREC_MIXED_FP32 ? 8.0 : 16.0;
+        // algorithmic bytes of one launch: x read once, y written once per instance, plus the plan
+        if (bytes) *bytes = nbatch * 2.0 * (double)N * s + plan_bytes(c);
+    });
+}
+
+int heom_bench_inner(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (reps < 1) reps = 1;
+        if (nbatch < 1) nbatch = 1;
+        BenchInputs I;
+        bench_inputs(c, precision, nbatch, I);
+        if (precision == HEOM_PREC_MIXED) time_inner<DF>(c, I, nbatch, reps, seconds, bytes);
+        else if (precision == HEOM_PREC_MIXED_FP32) time_inner<float>(c, I, nbatch, reps, seconds, bytes);
+        else if (precision == HEOM_PREC_FP64_REFINED) time_inner<double>(c, I, nbatch, reps, seconds, bytes);
+        else fail(HEOM_E_ARG, "heom_bench_inner: precision must be one of the refined (inner-solve) precisions");
     });
 }
 

@@ -1,6 +1,8 @@
 // Fused batched TFQMR for the inner solves of mixed-precision refinement (see inner.cuh
 // for the arrangement of the iteration).
 #include <cmath>
+#include <functional>
+#include <string>
 
 #include "apply_entry.cuh"
 #include "inner.cuh"
@@ -10,6 +12,9 @@ namespace heom {
 namespace {
 
 constexpr int NT = 256;
+// entries per thread: the per-thread fixed costs (flags, scalars, the warp reductions of the
+// inner products) are shared by kEPT entries, NT apart (coalesced)
+constexpr int kEPT = 1;
 
 // Per-thread accumulation of Re(a^H b) in the vectors' number type; warp_total() sums the
 // 32 lanes (every lane must call it) and returns the warp's total in FP64 on every lane.
@@ -48,37 +53,36 @@ template <> struct WarpAcc<DF> {
     }
 };
 
-// K per-warp totals -> one partial per block (thread 0 sums the warps in a fixed order).
+// K per-warp totals -> one partial per warp (lane 0 writes; no block barrier, so every warp
+// retires as soon as its own entries are done).  Layout: value k of instance b in the
+// contiguous run part[(3 b + k) np ...], np = warps per instance, so the finalisers read
+// each run with coalesced loads.
+constexpr int kWarps = NT / 32;
 template <int K>
-__device__ __forceinline__ void block_partials(const double (&wt)[K], double *out)
+__device__ __forceinline__ void warp_partials(const double (&wt)[K], double *part, int nblk, int b)
 {
-    __shared__ double sh[K][NT / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
+    if ((threadIdx.x & 31) == 0) {
+        const size_t np = (size_t)nblk * kWarps, slot = (size_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
 #pragma unroll
-        for (int k = 0; k < K; k++) sh[k][wid] = wt[k];
-    __syncthreads();
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            double s = 0;
-            for (int w = 0; w < NT / 32; w++) s += sh[k][w];
-            out[k] = s;
-        }
+        for (int k = 0; k < K; k++) part[(3 * (size_t)b + k) * np + slot] = wt[k];
+    }
 }
 
-// In the one-block-per-instance finalisers: the grand totals of the K partials of
-// instance b, summed in a fixed order, valid in thread 0.
+// In the one-block-per-instance finalisers (NTF threads): the grand totals of the K
+// partials of instance b, summed in a fixed order, valid in thread 0.
+constexpr int NTF = 1024;
 template <int K>
 __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b, double (&tot)[K])
 {
-    __shared__ double sh[K][NT / 32];
+    __shared__ double sh[K][NTF / 32];
     double s[K];
+    const size_t np = (size_t)nblk * kWarps;
 #pragma unroll
-    for (int k = 0; k < K; k++) s[k] = 0;
-    for (int i = threadIdx.x; i < nblk; i += NT)
-#pragma unroll
-        for (int k = 0; k < K; k++) s[k] += part[3 * ((size_t)b * nblk + i) + k];
+    for (int k = 0; k < K; k++) {
+        s[k] = 0;
+        const double *run = part + (3 * (size_t)b + k) * np;
+        for (size_t i = threadIdx.x; i < np; i += NTF) s[k] += run[i];
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -90,7 +94,7 @@ __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b
 #pragma unroll
         for (int k = 0; k < K; k++) {
             double a = 0;
-            for (int w = 0; w < NT / 32; w++) a += sh[k][w];
+            for (int w = 0; w < NTF / 32; w++) a += sh[k][w];
             tot[k] = a;
         }
 }
@@ -101,8 +105,7 @@ __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b
     const int b = blockIdx.y;                                  \
     if (W.st[b].done) return;                                  \
     const int64_t o = (int64_t)b * W.vstride;                  \
-    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;  \
-    double *part = W.part + 3 * ((size_t)b * W.nblk + blockIdx.x);
+    const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
 
 // w = b, other vectors 0; partials ||b||^2, <r~, b>
 template <typename T>
@@ -112,9 +115,12 @@ __global__ void k_in_init(InnerWork<T> W)
     using A = typename N::A;
     const int b = blockIdx.y;
     const int64_t o = (int64_t)b * W.vstride;
-    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;
+    const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
     WarpAcc<T> bb, rb;
-    if (t < W.N) {
+#pragma unroll 1
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
         const A bv = N::load(W.b[o + t]);
         const typename N::V z = N::store(N::zero());
         W.w[o + t] = N::store(bv);
@@ -123,7 +129,7 @@ __global__ void k_in_init(InnerWork<T> W)
         rb.add(N::load(W.rt[t]), bv);
     }
     const double wt[2] = {bb.warp_total(), rb.warp_total()};
-    block_partials<2>(wt, W.part + 3 * ((size_t)b * W.nblk + blockIdx.x));
+    warp_partials<2>(wt, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -149,11 +155,14 @@ __global__ void k_in_init_fin(InnerWork<T> W, double crit, int nlim, int stag_wi
 
 // B: u1 = A w + beta u2, the pending x / d updates, y = w + beta y2, v = u1 + beta (u2 + beta v)
 template <typename T, bool REG>
-__global__ void __launch_bounds__(NT, 4) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+__global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     FUSED_SETUP
     WarpAcc<T> sg;
-    if (t < W.N) {
+#pragma unroll 1
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
         const A aw = apply_entry<T, false, REG>(P, C, W.w + o, t, b);
         const InnerCoef<T> &k = W.cf[b];
         const A u2 = N::load(W.u2[o + t]), vo = N::load(W.v[o + t]), yo = N::load(W.y[o + t]);
@@ -170,7 +179,7 @@ __global__ void __launch_bounds__(NT, 4) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
         sg.add(N::load(W.rt[t]), vn);
     }
     const double wt[1] = {sg.warp_total()};
-    block_partials<1>(wt, part);
+    warp_partials<1>(wt, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -193,11 +202,14 @@ __global__ void k_in_b_fin(InnerWork<T> W)
 
 // A: u2 = u1 - alpha A v, w1 = w - alpha u1, w = w1 - alpha u2
 template <typename T, bool REG>
-__global__ void __launch_bounds__(NT, 4) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+__global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     FUSED_SETUP
     WarpAcc<T> a1, a2, a3;
-    if (t < W.N) {
+#pragma unroll 1
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
         const A av = apply_entry<T, false, REG>(P, C, W.v + o, t, b);
         const typename N::S al = W.cf[b].alpha;
         const A u1 = N::load(W.u1[o + t]);
@@ -211,7 +223,7 @@ __global__ void __launch_bounds__(NT, 4) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
         a3.add(N::load(W.rt[t]), w2);
     }
     const double wt[3] = {a1.warp_total(), a2.warp_total(), a3.warp_total()};
-    block_partials<3>(wt, part);
+    warp_partials<3>(wt, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -261,27 +273,33 @@ __global__ void k_in_x(InnerWork<T> W)
     const int b = blockIdx.y;
     if (W.st[b].done) return;
     const int64_t o = (int64_t)b * W.vstride;
-    const int64_t t = (int64_t)blockIdx.x * NT + threadIdx.x;
-    if (t >= W.N) return;
+    const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
     const InnerCoef<T> &k = W.cf[b];
-    const A yo = N::load(W.y[o + t]);
-    const A d1 = N::add(yo, N::scale(N::load(W.d[o + t]), k.dd1));
-    const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[o + t]), k.alpha_prev)), N::scale(d1, k.dd2));
-    W.xs[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
+        const A yo = N::load(W.y[o + t]);
+        const A d1 = N::add(yo, N::scale(N::load(W.d[o + t]), k.dd1));
+        const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[o + t]), k.alpha_prev)), N::scale(d1, k.dd2));
+        W.xs[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+    }
 }
 
 // partial ||b - A xs||^2
 template <typename T, bool REG>
-__global__ void __launch_bounds__(NT, 4) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+__global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     FUSED_SETUP
     WarpAcc<T> ee;
-    if (t < W.N) {
-        const A e = N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b));
-        ee.add(e, e);
+#pragma unroll 1
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
+        const A r = N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b));
+        ee.add(r, r);
     }
     const double wt[1] = {ee.warp_total()};
-    block_partials<1>(wt, part);
+    warp_partials<1>(wt, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -309,7 +327,69 @@ __global__ void k_in_chk_fin(InnerWork<T> W)
     W.st[b] = s;
 }
 
+// measurement pattern: every vector = (1 + k/8) r~, finite scalars, no instance done
+template <typename T>
+__global__ void k_in_fill(InnerWork<T> W)
+{
+    using N = Num<T>;
+    const int b = blockIdx.y;
+    const int64_t o = (int64_t)b * W.vstride;
+    const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
+#pragma unroll 1
+    for (int e = 0; e < kEPT; e++) {
+        const int64_t t = t0 + (int64_t)e * NT;
+        if (t >= W.N) break;
+        const typename N::V r = W.rt[t];
+        typename N::V *vec[9] = {W.x, W.xs, W.b, W.w, W.y, W.d, W.v, W.u1, W.u2};
+        for (int k = 0; k < 9; k++)
+            vec[k][o + t] = N::store(N::scale(N::load(r), N::sc(1.0 + 0.125 * k)));
+    }
+    if (t0 == 0) {
+        InnerState st = {};
+        st.r0 = 1; st.tau = 1; st.rho = 1; st.nlim = 1 << 30;
+        W.st[b] = st;
+        InnerCoef<T> k;
+        k.beta = k.alpha = k.alpha_prev = k.dd1 = k.eta1 = k.dd2 = k.eta2 = N::sc(0.5);
+        W.cf[b] = k;
+    }
+}
+
 }  // namespace
+
+template <typename T>
+void inner_time(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a)
+{
+    dim3 g((unsigned)W.nblk, (unsigned)W.nbatch);
+    DevPlan Q = P;
+    Q.order = nullptr;
+    k_in_fill<T><<<g, NT, 0, s>>>(W);
+    auto run_b = [&] {
+        if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_b<T, false><<<g, NT, 0, s>>>(Q, C, W);
+    };
+    auto run_a = [&] {
+        if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_a<T, false><<<g, NT, 0, s>>>(Q, C, W);
+    };
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) fail(HEOM_E_CUDA, "cudaEventCreate failed");
+    auto timed = [&](const std::function<void()> &f) {
+        for (int w = 0; w < 3; w++) f();
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < reps; r++) f();
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / reps;
+    };
+    ms_b = timed(run_b);
+    ms_a = timed(run_a);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) fail(HEOM_E_CUDA, std::string("fused inner kernels: ") + cudaGetErrorString(e));
+}
 
 template <typename T>
 void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
@@ -318,12 +398,12 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     W.nbatch = nbatch;
     W.N = N;
     W.vstride = (N + 63) / 64 * 64;
-    W.nblk = (int)((N + NT - 1) / NT);
+    W.nblk = (int)((N + (int64_t)NT * kEPT - 1) / ((int64_t)NT * kEPT));
     const size_t vbytes = sizeof(V) * (size_t)W.vstride * nbatch;
     // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
     auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(InnerState) * nbatch) +
-                         rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
+                         rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * kWarps * (size_t)nbatch * W.nblk);
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the inner-solver workspace failed");
     if (cudaMemsetAsync(p, 0, total, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
@@ -338,7 +418,7 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     W.rt = (V *)take(sizeof(V) * (size_t)W.vstride);
     W.st = (InnerState *)take(sizeof(InnerState) * nbatch);
     W.cf = (InnerCoef<T> *)take(sizeof(InnerCoef<T>) * nbatch);
-    W.part = (double *)take(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
+    W.part = (double *)take(sizeof(double) * 3 * kWarps * (size_t)nbatch * W.nblk);
 }
 
 template <typename T>
@@ -353,7 +433,7 @@ void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaSt
 {
     dim3 g((unsigned)W.nblk, (unsigned)W.nbatch);
     k_in_init<T><<<g, NT, 0, s>>>(W);
-    k_in_init_fin<T><<<W.nbatch, NT, 0, s>>>(W, crit, nlim, stag_window);
+    k_in_init_fin<T><<<W.nbatch, NTF, 0, s>>>(W, crit, nlim, stag_window);
 }
 
 template <typename T>
@@ -366,22 +446,23 @@ void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int ite
     for (int i = 0; i < iters; i++) {
         if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_b<T, false><<<g, NT, 0, s>>>(Q, C, W);
-        k_in_b_fin<T><<<nb, NT, 0, s>>>(W);
+        k_in_b_fin<T><<<nb, NTF, 0, s>>>(W);
         if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_a<T, false><<<g, NT, 0, s>>>(Q, C, W);
-        k_in_a_fin<T><<<nb, NT, 0, s>>>(W);
+        k_in_a_fin<T><<<nb, NTF, 0, s>>>(W);
     }
     k_in_x<T><<<g, NT, 0, s>>>(W);
     if (C.reg) k_in_chk<T, true><<<g, NT, 0, s>>>(Q, C, W);
     else k_in_chk<T, false><<<g, NT, 0, s>>>(Q, C, W);
-    k_in_chk_fin<T><<<nb, NT, 0, s>>>(W);
+    k_in_chk_fin<T><<<nb, NTF, 0, s>>>(W);
 }
 
 #define INST(T)                                                                              \
     template void inner_alloc<T>(InnerWork<T> &, int, int64_t, cudaStream_t);                \
     template void inner_free<T>(InnerWork<T> &);                                              \
     template void inner_start<T>(InnerWork<T> &, double, int, int, cudaStream_t);             \
-    template void inner_chunk<T>(InnerWork<T> &, const DevPlan &, const DevCoef<T> &, int, cudaStream_t);
+    template void inner_chunk<T>(InnerWork<T> &, const DevPlan &, const DevCoef<T> &, int, cudaStream_t);    \
+    template void inner_time<T>(InnerWork<T> &, const DevPlan &, const DevCoef<T> &, int, cudaStream_t, float &, float &);
 INST(double)
 INST(float)
 INST(DF)

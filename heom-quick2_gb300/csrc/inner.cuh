@@ -46,7 +46,7 @@ struct InnerWork {
       *u1 = nullptr, *u2 = nullptr, *rt = nullptr;
     InnerState *st = nullptr;
     InnerCoef<T> *cf = nullptr;
-    double *part = nullptr;     // nbatch * nblk * 3
+    double *part = nullptr;     // per-warp partials: 3 runs of nblk * 8 per instance
     void *mem = nullptr;        // single allocation backing everything above
 };
 
@@ -62,6 +62,11 @@ void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaSt
 // Enqueue `iters` iterations and one check (capturable in a CUDA graph).
 template <typename T>
 void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int iters, cudaStream_t s);
+
+// Measurement: fill the workspace with a fixed pattern (no instance done), then time `reps`
+// launches of the B kernel and of the A kernel; milliseconds per launch.
+template <typename T>
+void inner_time(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a);
 
 constexpr int kInnerStartLaunches = 2;
 constexpr int kInnerIterationLaunches = 4;

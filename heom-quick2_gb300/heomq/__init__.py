@@ -110,6 +110,7 @@ SIGNATURES = {
     "heom_td_gradient": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "heom_solve_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "heom_bench_inner": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_ctx_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "heom_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(C.c_void_p)]),
     "heom_batch_stride": (C.c_int64, [C.c_void_p]),
@@ -369,6 +370,14 @@ class Context:
         b = C.c_double()
         _check(lib().heom_bench_apply(self.h, precision, nbatch, reps, C.byref(s), C.byref(b)))
         return s.value, b.value
+
+    def bench_inner(self, precision=PREC_MIXED, reps=20, nbatch=1):
+        """Average device times of the two fused kernels of an inner TFQMR iteration over nbatch
+        instances, and their algorithmic bytes per launch: ((s_b, s_a), (bytes_b, bytes_a))."""
+        s = (C.c_double * 2)()
+        b = (C.c_double * 2)()
+        _check(lib().heom_bench_inner(self.h, precision, nbatch, reps, s, b))
+        return (s[0], s[1]), (b[0], b[1])
 
     def stats(self):
         """Plan statistics (see heom_ctx_stats in include/heom_gb300.h)."""

@@ -241,6 +241,15 @@ int heom_batch_current_static(heom_ctx *ctx, const void *x_dev, int32_t nbatch, 
  * return the average kernel time in seconds and the algorithmic bytes of one launch. */
 int heom_bench_apply(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
 
+/* Measurement hook: time `reps` launches of each of the two fused kernels of one inner
+ * TFQMR iteration (the apply of w with the first half of the vector updates, and the apply
+ * of v with the second half) on `nbatch` instances, in the number type of `precision`
+ * (HEOM_PREC_MIXED: FP32x2, HEOM_PREC_MIXED_FP32: FP32, HEOM_PREC_FP64_REFINED: FP64).
+ * seconds[0..1] and bytes[0..1] receive the average kernel time and the algorithmic bytes
+ * of one launch of each kernel.  No reference counterpart (the reference has no mixed
+ * precision). */
+int heom_bench_inner(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
+
 /* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs
  * with entries, [2] pattern classes, [3] coupling records, [4] gather maps, [5] useful
  * gathers (nonzero map halves), [6] same-tier terms, [7] lower-tier (complex-coefficient)
