@@ -82,38 +82,41 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
     const A dlt = N::mul_i(N::norm(sd));
     acc = N::add(acc, ADJ ? N::neg(dlt) : dlt);
 
-    // couplings to the neighbouring tiers
-    const int e0 = __ldg(P.coup_ptr + n), e1 = __ldg(P.coup_ptr + n + 1);
-    A ua = N::zero();   // sum of unit-coefficient contributions (times -i at the end)
-    for (int e = e0; e < e1; e++) {
+    // couplings to the neighbouring tiers: coefficient pairs (lower tier) first, then the
+    // unit pairs (higher tier / RDO); a map word holds the left and right source entries
+    // (q + 1, 0 = none) with their signs in bit 15
+    const int e0 = __ldg(P.coup_ptr + n), em = __ldg(P.coup_mid + n), e1 = __ldg(P.coup_ptr + n + 1);
+    for (int e = e0; e < em; e++) {
         const int4 rec = __ldg(P.coup + e);
         const uint32_t mw = __ldg(P.maps + rec.y + p);
-        if (!mw) continue;
-        const bool cj = rec.z < 0;
-        const uint32_t lo = mw & 0xFFFFu, hi = mw >> 16;
-        A vl = N::zero(), vr = N::zero();
+        const uint32_t cj = (uint32_t)rec.z >> 31, lo = mw & 0xFFFFu, hi = mw >> 16;
         const bool src_rdo = REG && rec.x == 0;
+        const int cid = rec.z & 0x3FFFFFFF;
         if (lo) {
-            vl = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
-            if (cj) vl = N::conj(vl);
-            if (lo & 0x8000u) vl = N::neg(vl);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            acc = N::add(acc, N::mul(N::load(C.cl[cid]), N::flip(v, lo >> 15, cj)));
         }
         if (hi) {
-            vr = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
-            if (cj) vr = N::conj(vr);
-            if (hi & 0x8000u) vr = N::neg(vr);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            acc = N::add(acc, N::mul(N::load(C.cr[cid]), N::flip(v, hi >> 15, cj)));
         }
-        if (rec.z & kCoefUnit) {
-            // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
-            if (C.unit_on) {
-                ua = N::add(ua, (rec.z & 1) ? N::neg(vl) : vl);
-                ua = N::add(ua, (rec.z & 2) ? N::neg(vr) : vr);
-            }
-        } else {
-            const int cid = rec.z & 0x3FFFFFFF;
-            if (lo) acc = N::add(acc, N::mul(N::load(C.cl[cid]), vl));
-            if (hi) acc = N::add(acc, N::mul(N::load(C.cr[cid]), vr));
-            if ((e - e0) & 1) acc = N::norm(acc);
+        if ((e - e0) & 1) acc = N::norm(acc);
+    }
+    // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
+    A ua = N::zero();
+    const int eu = C.unit_on ? e1 : em;
+    for (int e = em; e < eu; e++) {
+        const int4 rec = __ldg(P.coup + e);
+        const uint32_t mw = __ldg(P.maps + rec.y + p);
+        const uint32_t cj = (uint32_t)rec.z >> 31, lo = mw & 0xFFFFu, hi = mw >> 16;
+        const bool src_rdo = REG && rec.x == 0;
+        if (lo) {
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            ua = N::add(ua, N::flip(v, ((lo >> 15) ^ (uint32_t)rec.z) & 1u, cj));
+        }
+        if (hi) {
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            ua = N::add(ua, N::flip(v, ((hi >> 15) ^ ((uint32_t)rec.z >> 1)) & 1u, cj));
         }
         if (((e - e0) & 3) == 3) ua = N::norm(ua);
     }

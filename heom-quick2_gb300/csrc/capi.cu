@@ -47,6 +47,7 @@ void PlanDev::upload(const HostPlan &P)
     view.ado_cls = upload_vec(blocks, P.ado_cls);
     view.ado_cnt = upload_vec(blocks, P.ado_cnt);
     view.coup_ptr = upload_vec(blocks, P.coup_ptr);
+    view.coup_mid = upload_vec(blocks, P.coup_mid);
     view.cls_tptr = upload_vec(blocks, P.cls_tptr);
     view.term_ptr = upload_vec(blocks, P.term_ptr);
     view.trace_idx = upload_vec(blocks, P.trace_idx);

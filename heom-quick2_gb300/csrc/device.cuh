@@ -16,7 +16,7 @@ struct DevPlan {
     int64_t lunk = 0;
     int32_t nado = 0, nslots = 0, nh = 0, ntrace = 0;
     const int32_t *ent_ado = nullptr, *ado_off = nullptr, *ado_cls = nullptr, *ado_cnt = nullptr;
-    const int32_t *coup_ptr = nullptr, *cls_tptr = nullptr, *term_ptr = nullptr, *trace_idx = nullptr;
+    const int32_t *coup_ptr = nullptr, *coup_mid = nullptr, *cls_tptr = nullptr, *term_ptr = nullptr, *trace_idx = nullptr;
     const int4 *coup = nullptr;
     const uint32_t *maps = nullptr, *terms = nullptr;
     // thread -> entry order: entries grouped by their work profile (couplings, useful

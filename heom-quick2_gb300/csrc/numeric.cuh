@@ -42,6 +42,13 @@ template <> struct Num<double> {
     static __device__ __forceinline__ A mul_i(A a) { return make_double2(-a.y, a.x); }
     static __device__ __forceinline__ A neg(A a) { return make_double2(-a.x, -a.y); }
     static __device__ __forceinline__ A conj(A a) { return make_double2(a.x, -a.y); }
+    // (-1)^ng a, conjugated when cj = 1 (ng, cj in {0, 1}): sign-bit flips, no branches
+    static __device__ __forceinline__ A flip(A a, uint32_t ng, uint32_t cj)
+    {
+        const unsigned long long mr = (unsigned long long)ng << 63, mi = (unsigned long long)(ng ^ cj) << 63;
+        return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ (long long)mr),
+                            __longlong_as_double(__double_as_longlong(a.y) ^ (long long)mi));
+    }
     static __device__ __forceinline__ double re(A a) { return a.x; }
     static __device__ __forceinline__ double im(A a) { return a.y; }
 };
@@ -66,6 +73,11 @@ template <> struct Num<float> {
     static __device__ __forceinline__ A mul_i(A a) { return make_float2(-a.y, a.x); }
     static __device__ __forceinline__ A neg(A a) { return make_float2(-a.x, -a.y); }
     static __device__ __forceinline__ A conj(A a) { return make_float2(a.x, -a.y); }
+    static __device__ __forceinline__ A flip(A a, uint32_t ng, uint32_t cj)
+    {
+        const uint32_t mr = ng << 31, mi = (ng ^ cj) << 31;
+        return make_float2(__uint_as_float(__float_as_uint(a.x) ^ mr), __uint_as_float(__float_as_uint(a.y) ^ mi));
+    }
     static __device__ __forceinline__ double re(A a) { return a.x; }
     static __device__ __forceinline__ double im(A a) { return a.y; }
 };
@@ -142,6 +154,12 @@ template <> struct Num<DF> {
     static __device__ __forceinline__ A mul_i(A a) { return {f2r_neg(a.im), a.re}; }
     static __device__ __forceinline__ A neg(A a) { return {f2r_neg(a.re), f2r_neg(a.im)}; }
     static __device__ __forceinline__ A conj(A a) { return {a.re, f2r_neg(a.im)}; }
+    static __device__ __forceinline__ A flip(A a, uint32_t ng, uint32_t cj)
+    {
+        const uint32_t mr = ng << 31, mi = (ng ^ cj) << 31;
+        return {{__uint_as_float(__float_as_uint(a.re.hi) ^ mr), __uint_as_float(__float_as_uint(a.re.lo) ^ mr)},
+                {__uint_as_float(__float_as_uint(a.im.hi) ^ mi), __uint_as_float(__float_as_uint(a.im.lo) ^ mi)}};
+    }
     static __device__ __forceinline__ double re(A a) { return (double)a.re.hi + (double)a.re.lo; }
     static __device__ __forceinline__ double im(A a) { return (double)a.im.hi + (double)a.im.lo; }
 };

@@ -324,6 +324,7 @@ void build_forward_plan(const heom_tables &t, const HStructure &hst, HostPlan &P
         for (int q = 0; q < t.nnz_spa[0]; q++)
             if (t.irow_spa[q] == t.icol_spa[q]) P.trace_idx.push_back(q);
     P.n_couplings = (int64_t)P.coup.size();
+    split_couplings(P);
     if (P.maps.size() >= (size_t)1 << 31 || P.cl.size() >= (size_t)1 << 30) fail(HEOM_E_UNSUPPORTED, "plan too large");
 }
 
@@ -423,7 +424,18 @@ void build_adjoint_plan(const heom_tables &t, const HostPlan &F, HostPlan &A) {
         A.coup_ptr.push_back((int32_t)A.coup.size());
     }
     A.n_couplings = (int64_t)A.coup.size();
+    split_couplings(A);
     (void)t;
+}
+
+void split_couplings(HostPlan &P)
+{
+    P.coup_mid.assign(P.nado, 0);
+    for (int32_t a = 0; a < P.nado; a++) {
+        auto b = P.coup.begin() + P.coup_ptr[a], e = P.coup.begin() + P.coup_ptr[a + 1];
+        auto mid = std::stable_partition(b, e, [](const CoupRec &r) { return (r.cid & kCoefUnit) == 0; });
+        P.coup_mid[a] = (int32_t)(mid - P.coup.begin());
+    }
 }
 
 void gamma_derivative_coefs(const heom_tables &, const HostPlan &F, double gamma, std::vector<cd> &cl, std::vector<cd> &cr) {

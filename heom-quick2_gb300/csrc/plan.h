@@ -35,6 +35,8 @@ struct HostPlan {
     std::vector<int32_t> ado_cnt;           // nado: 4 signed int8 counts of sum(dipm) per slot
     std::vector<cd> g0;                     // nado: sum of cgamma over the drawers
     std::vector<int32_t> coup_ptr;          // nado + 1
+    std::vector<int32_t> coup_mid;          // nado: first unit-coefficient coupling of the ADO
+                                            // (its couplings are ordered coefficient pairs first)
     std::vector<CoupRec> coup;
     std::vector<uint32_t> maps;             // word: lo16 = left src (q+1, bit15 = minus), hi16 = right
     std::vector<cd> cl, cr;                 // coefficient pairs
@@ -60,6 +62,9 @@ struct HStructure {
 HStructure make_hstructure(const heom_tables &t, const std::vector<const double _Complex *> &extra);
 void build_forward_plan(const heom_tables &t, const HStructure &hst, HostPlan &out);
 void build_adjoint_plan(const heom_tables &t, const HostPlan &fwd, HostPlan &out);
+// Order every ADO's couplings as coefficient pairs first, then unit pairs (stable, so each
+// kind keeps its order), and record the boundary in coup_mid.
+void split_couplings(HostPlan &P);
 // derivative coefficient table of the forward plan w.r.t. a common linewidth scale:
 // lower-tier pairs divided by gamma, everything else zero
 void gamma_derivative_coefs(const heom_tables &t, const HostPlan &fwd, double gamma, std::vector<cd> &cl, std::vector<cd> &cr);
