@@ -76,7 +76,7 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         if (ADJ) h = N::conj(h);
         const A xs = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF)) : N::load(x[off + (int)(w & 0xFFFF)]);
         const A hx = C.h_real ? N::scale(xs, N::re_s(h)) : N::mul(h, xs);
-        sd = N::add(sd, (w >> 31) ? hx : N::neg(hx));
+        sd = N::add(sd, N::flip(hx, (w >> 31) ^ 1u, 0u));
     }
     // forward: acc += i (sum_right - sum_left); adjoint: acc += -i (...)
     const A dlt = N::mul_i(N::norm(sd));

@@ -484,6 +484,7 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     double2 *r64 = nullptr;
     CK(cudaMalloc((void **)&r64, sizeof(double2) * (size_t)vstride * nbatch));
     tmp.push_back(r64);
+    DevCoef<double> k64 = K.k64;   // gets the per-instance ADO diagonals below
     int total_iters = 0, last_ierr = 0;
     bool converged = false;
     std::vector<double> norms(nbatch, 0.0);
@@ -493,10 +494,18 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         aux += nbatch;
     };
     std::function<void(const double2 *, double2 *)> residual = [&](const double2 *xx, double2 *r) {
-        residual64(c, K.k64, xx, r, nbatch, vstride, adj, rhs);
+        residual64(c, k64, xx, r, nbatch, vstride, adj, rhs);
         aux += rhs ? 2 : 2 + nbatch;
     };
     try {
+        // per-instance ADO diagonals of the FP64 applies, so they do no per-entry lead-shift sums
+        const DevPlan &PV = adj ? c->dadj.view : c->dfwd.view;
+        double2 *gd64 = nullptr;
+        CK(cudaMalloc((void **)&gd64, sizeof(double2) * std::max<int64_t>(1, (int64_t)PV.nado * nbatch)));
+        tmp.push_back(gd64);
+        fill_gdiag<double>(PV, K.k64, gd64, nbatch, c->stream);
+        aux++;
+        k64.gdiag = gd64;
         if (o.precision == HEOM_PREC_FP64) {
             TfqWork<double> W;
             tfq_alloc<double>(W, nbatch, N, c->stream);
@@ -509,7 +518,7 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                 tfq_start<double>(W, o.crit * 1e-3, nlim, o.crit, 0.0, 0, c->stream);
                 aux += kTfqStartLaunches;
                 int it = 0;
-                tfq_run<double>(c, W, make_apply<double>(c, K.k64, nbatch, W.vstride, adj), nlim, it, info.launches);
+                tfq_run<double>(c, W, make_apply<double>(c, k64, nbatch, W.vstride, adj), nlim, it, info.launches);
                 for (int b = 0; b < nbatch; b++)
                     vec_axpby<double>(N, x + (int64_t)b * vstride, 1.0, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
                 std::vector<TfqState> st(nbatch);
@@ -522,13 +531,13 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         } else {
             if (adj) fail(HEOM_E_UNSUPPORTED, "mixed precision is implemented for the forward operator");
             if (o.precision == HEOM_PREC_MIXED)
-                mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, K.k64, K.kdf, r64, norms, nlim, total_iters, last_ierr,
+                mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, k64, K.kdf, r64, norms, nlim, total_iters, last_ierr,
                                  converged, info.refinements, info.launches, aux, residual, batch_norms);
             else if (o.precision == HEOM_PREC_FP64_REFINED)
-                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, K.k64, K.k64, r64, norms, nlim, total_iters, last_ierr,
+                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim, total_iters, last_ierr,
                                      converged, info.refinements, info.launches, aux, residual, batch_norms);
             else if (o.precision == HEOM_PREC_MIXED_FP32)
-                mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, K.k64, K.k32, r64, norms, nlim, total_iters, last_ierr,
+                mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, k64, K.k32, r64, norms, nlim, total_iters, last_ierr,
                                     converged, info.refinements, info.launches, aux, residual, batch_norms);
             else fail(HEOM_E_ARG, "unknown precision");
         }
@@ -947,7 +956,7 @@ void bench_inputs(heom_ctx *c, int precision, int nbatch, BenchInputs &I)
     } else if (precision == HEOM_PREC_MIXED_FP32) {
         DevCoef<float> K = main_coef<float>(c, false); K.eshift = I.es;
         fill_gdiag<float>(c->dfwd.view, K, (float2 *)I.gdiag, nbatch, c->stream);
-    } else if (precision == HEOM_PREC_FP64_REFINED) {
+    } else if (precision == HEOM_PREC_FP64_REFINED || precision == HEOM_PREC_FP64) {
         DevCoef<double> K = main_coef<double>(c, false); K.eshift = I.es;
         fill_gdiag<double>(c->dfwd.view, K, (double2 *)I.gdiag, nbatch, c->stream);
     }
@@ -1014,6 +1023,7 @@ int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
         auto run = [&] {
             if (precision == HEOM_PREC_FP64) {
                 DevCoef<double> K = main_coef<double>(c, false); K.hval = (double2 *)I.hv; K.eshift = I.es;
+                K.gdiag = (const double2 *)I.gdiag;
                 launch_apply<double, false>(c->dfwd.view, K, (double2 *)xin, (double2 *)yout, nbatch, vs, nullptr, c->stream);
             } else if (precision == HEOM_PREC_MIXED) {
                 launch_apply<DF, false>(c->dfwd.view, bench_coef<DF>(c, I), (float4 *)xin, (float4 *)yout, nbatch, vs, nullptr, c->stream);
