@@ -16,56 +16,80 @@ constexpr int NT = 256;
 // inner products) are shared by kEPT entries, NT apart (coalesced)
 constexpr int kEPT = 1;
 
-// Per-thread accumulation of Re(a^H b) in the vectors' number type; warp_total() sums the
-// 32 lanes (every lane must call it) and returns the warp's total in FP64 on every lane.
+// Per-thread accumulation of Re(a^H b) in the vectors' number type.  warp_sum() adds the 32
+// lanes (every lane must call it; the result is valid on every lane) in the same type;
+// add() and to_double() combine and convert warp sums.  FP64 appears only in to_double,
+// called once per block: the FP64 pipe of GB300 runs at 1/64 of the FP32 rate.
 template <typename T> struct WarpAcc;
 template <> struct WarpAcc<double> {
+    using R = double;
     double v = 0;
     __device__ __forceinline__ void add(double2 a, double2 b) { v = fma(a.x, b.x, fma(a.y, b.y, v)); }
-    __device__ __forceinline__ double warp_total()
+    __device__ __forceinline__ R warp_sum() const
     {
         double s = v;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         return s;
     }
+    static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+    static __device__ __forceinline__ double to_double(R a) { return a; }
 };
 template <> struct WarpAcc<float> {
+    using R = float;
     float v = 0.f;
     __device__ __forceinline__ void add(float2 a, float2 b) { v = fmaf(a.x, b.x, fmaf(a.y, b.y, v)); }
-    __device__ __forceinline__ double warp_total()
+    __device__ __forceinline__ R warp_sum() const
     {
         float s = v;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        return (double)s;
+        return s;
     }
+    static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+    static __device__ __forceinline__ double to_double(R a) { return (double)a; }
 };
 template <> struct WarpAcc<DF> {
+    using R = f2r;
     f2r v{0.f, 0.f};
     __device__ __forceinline__ void add(f2c a, f2c b) { v = f2r_add(v, f2r_add(f2r_mul(a.re, b.re), f2r_mul(a.im, b.im))); }
-    __device__ __forceinline__ double warp_total()
+    __device__ __forceinline__ R warp_sum() const
     {
         f2r s = f2r_norm(v);
         for (int o = 16; o > 0; o >>= 1) {
             const f2r q{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
             s = f2r_add(s, q);
         }
-        return (double)s.hi + (double)s.lo;
+        return s;
     }
+    static __device__ __forceinline__ R add(R a, R b) { return f2r_add(a, b); }
+    static __device__ __forceinline__ double to_double(R a) { return (double)a.hi + (double)a.lo; }
 };
 
-// K per-warp totals -> one partial per warp (lane 0 writes; no block barrier, so every warp
-// retires as soon as its own entries are done).  Layout: value k of instance b in the
-// contiguous run part[(3 b + k) np ...], np = warps per instance, so the finalisers read
-// each run with coalesced loads.
+// K warp sums -> one FP64 partial per block, written to part[(3 b + k) nblk + block].
+// Warps 1..7 leave their sums in shared memory, arrive at named barrier 1 and retire at
+// once; warp 0 waits there (bar.sync), then its lane 0 adds the eight sums in warp order
+// (deterministic).  Every thread of the block must reach this call.
 constexpr int kWarps = NT / 32;
-template <int K>
-__device__ __forceinline__ void warp_partials(const double (&wt)[K], double *part, int nblk, int b)
+template <typename T, int K>
+__device__ __forceinline__ void block_partials(const typename WarpAcc<T>::R (&ws)[K], double *part, int nblk, int b)
 {
-    if ((threadIdx.x & 31) == 0) {
-        const size_t np = (size_t)nblk * kWarps, slot = (size_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
+    using R = typename WarpAcc<T>::R;
+    __shared__ R sh[K][kWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (wid != 0) {
+        if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < K; k++) part[(3 * (size_t)b + k) * np + slot] = wt[k];
+            for (int k = 0; k < K; k++) sh[k][wid] = ws[k];
+        asm volatile("bar.arrive 1, %0;" ::"r"(NT) : "memory");
+        return;
     }
+    asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            R s = ws[k];
+            for (int w = 1; w < kWarps; w++) s = WarpAcc<T>::add(s, sh[k][w]);
+            part[(3 * (size_t)b + k) * nblk + blockIdx.x] = WarpAcc<T>::to_double(s);
+        }
 }
 
 // In the one-block-per-instance finalisers (NTF threads): the grand totals of the K
@@ -76,12 +100,11 @@ __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b
 {
     __shared__ double sh[K][NTF / 32];
     double s[K];
-    const size_t np = (size_t)nblk * kWarps;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         s[k] = 0;
-        const double *run = part + (3 * (size_t)b + k) * np;
-        for (size_t i = threadIdx.x; i < np; i += NTF) s[k] += run[i];
+        const double *run = part + (3 * (size_t)b + k) * nblk;
+        for (int i = threadIdx.x; i < nblk; i += NTF) s[k] += run[i];
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -128,8 +151,8 @@ __global__ void k_in_init(InnerWork<T> W)
         bb.add(bv, bv);
         rb.add(N::load(W.rt[t]), bv);
     }
-    const double wt[2] = {bb.warp_total(), rb.warp_total()};
-    warp_partials<2>(wt, W.part, W.nblk, b);
+    const typename WarpAcc<T>::R ws[2] = {bb.warp_sum(), rb.warp_sum()};
+    block_partials<T, 2>(ws, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -178,8 +201,8 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
         W.v[o + t] = N::store(vn);
         sg.add(N::load(W.rt[t]), vn);
     }
-    const double wt[1] = {sg.warp_total()};
-    warp_partials<1>(wt, W.part, W.nblk, b);
+    const typename WarpAcc<T>::R ws[1] = {sg.warp_sum()};
+    block_partials<T, 1>(ws, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -222,8 +245,8 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
         a2.add(w2, w2);
         a3.add(N::load(W.rt[t]), w2);
     }
-    const double wt[3] = {a1.warp_total(), a2.warp_total(), a3.warp_total()};
-    warp_partials<3>(wt, W.part, W.nblk, b);
+    const typename WarpAcc<T>::R ws[3] = {a1.warp_sum(), a2.warp_sum(), a3.warp_sum()};
+    block_partials<T, 3>(ws, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -298,8 +321,8 @@ __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, Inner
         const A r = N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b));
         ee.add(r, r);
     }
-    const double wt[1] = {ee.warp_total()};
-    warp_partials<1>(wt, W.part, W.nblk, b);
+    const typename WarpAcc<T>::R ws[1] = {ee.warp_sum()};
+    block_partials<T, 1>(ws, W.part, W.nblk, b);
 }
 
 template <typename T>
@@ -403,7 +426,7 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
     auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(InnerState) * nbatch) +
-                         rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * kWarps * (size_t)nbatch * W.nblk);
+                         rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the inner-solver workspace failed");
     if (cudaMemsetAsync(p, 0, total, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
@@ -418,7 +441,7 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     W.rt = (V *)take(sizeof(V) * (size_t)W.vstride);
     W.st = (InnerState *)take(sizeof(InnerState) * nbatch);
     W.cf = (InnerCoef<T> *)take(sizeof(InnerCoef<T>) * nbatch);
-    W.part = (double *)take(sizeof(double) * 3 * kWarps * (size_t)nbatch * W.nblk);
+    W.part = (double *)take(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
 }
 
 template <typename T>

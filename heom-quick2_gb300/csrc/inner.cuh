@@ -46,7 +46,7 @@ struct InnerWork {
       *u1 = nullptr, *u2 = nullptr, *rt = nullptr;
     InnerState *st = nullptr;
     InnerCoef<T> *cf = nullptr;
-    double *part = nullptr;     // per-warp partials: 3 runs of nblk * 8 per instance
+    double *part = nullptr;     // per-block partials: 3 runs of nblk per instance
     void *mem = nullptr;        // single allocation backing everything above
 };
 
