@@ -16,7 +16,8 @@ constexpr int NT = 256;
 // inner products) are shared by kEPT entries, NT apart (coalesced)
 constexpr int kEPT = 1;
 
-// Per-thread accumulation of Re(a^H b) in the vectors' number type.  warp_sum() adds the 32
+// Per-thread accumulation of Re(a^H b) in the vectors' number type (for FP32x2 at least one
+// operand of each product must be normalised; see f2r_mul).  warp_sum() adds the 32
 // lanes (every lane must call it; the result is valid on every lane) in the same type;
 // add() and to_double() combine and convert warp sums.  FP64 appears only in to_double,
 // called once per block: the FP64 pipe of GB300 runs at 1/64 of the FP32 rate.
@@ -238,9 +239,10 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
         const A u1 = N::load(W.u1[o + t]);
         const A u2 = N::sub(u1, N::scale(av, al));
         W.u2[o + t] = N::store(u2);
-        const A w1 = N::sub(N::load(W.w[o + t]), N::scale(u1, al));
-        const A w2 = N::sub(w1, N::scale(u2, al));
-        W.w[o + t] = N::store(w2);
+        // normalised before the squared norms (the lazy differences cancel near convergence)
+        const A w1 = N::norm(N::sub(N::load(W.w[o + t]), N::scale(u1, al)));
+        const A w2 = N::norm(N::sub(w1, N::scale(u2, al)));
+        W.w[o + t] = N::pack(w2);
         a1.add(w1, w1);
         a2.add(w2, w2);
         a3.add(N::load(W.rt[t]), w2);
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, Inner
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
-        const A r = N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b));
+        const A r = N::norm(N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b)));
         ee.add(r, r);
     }
     const typename WarpAcc<T>::R ws[1] = {ee.warp_sum()};

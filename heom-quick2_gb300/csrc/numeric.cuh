@@ -27,6 +27,7 @@ template <> struct Num<double> {
     static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
     static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
     static __host__ __device__ __forceinline__ V store_host(const A &a) { return a; }
+    static __device__ __forceinline__ V pack(const A &a) { return a; }
     static __device__ __forceinline__ A norm(A a) { return a; }
     static __host__ __device__ __forceinline__ A zero() { return make_double2(0, 0); }
     static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_double2(re, im); }
@@ -60,6 +61,7 @@ template <> struct Num<float> {
     static __host__ __device__ __forceinline__ A load(const V &v) { return v; }
     static __host__ __device__ __forceinline__ V store(const A &a) { return a; }
     static __host__ __device__ __forceinline__ V store_host(const A &a) { return a; }
+    static __device__ __forceinline__ V pack(const A &a) { return a; }
     static __device__ __forceinline__ A norm(A a) { return a; }
     static __host__ __device__ __forceinline__ A zero() { return make_float2(0, 0); }
     static __host__ __device__ __forceinline__ A from_d(double re, double im) { return make_float2((float)re, (float)im); }
@@ -110,7 +112,10 @@ __device__ __forceinline__ f2r f2r_add(f2r a, f2r b)
     return {s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
 }
 __device__ __forceinline__ f2r f2r_neg(f2r a) { return {-a.hi, -a.lo}; }
-// unnormalised product: exact product of the high parts plus the cross terms
+// unnormalised product: exact product of the high parts plus the cross terms.  The lo x lo
+// term is dropped, so at least one operand must be normalised (|lo| <= ulp(hi) / 2): a lazy
+// sum after cancellation can carry |lo| >= |hi|, and its square would then lose its leading
+// term (even turn negative).  Loaded values are normalised; lazy sums go through norm first.
 __device__ __forceinline__ f2r f2r_mul(f2r a, f2r b)
 {
     float p = __fmul_rn(a.hi, b.hi);
@@ -133,6 +138,8 @@ template <> struct Num<DF> {
         return make_float4(r.hi, i.hi, r.lo, i.lo);
     }
     static __host__ __device__ __forceinline__ V store_host(const A &a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
+    // store of a value that is already normalised (the result of norm)
+    static __device__ __forceinline__ V pack(const A &a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
     // renormalise an accumulator (keeps long sums near 2^-48 relative)
     static __device__ __forceinline__ A norm(A a) { return {two_sum(a.re.hi, a.re.lo), two_sum(a.im.hi, a.im.lo)}; }
     static __host__ __device__ __forceinline__ A zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }

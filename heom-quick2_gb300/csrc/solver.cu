@@ -109,7 +109,13 @@ template <> struct DotAcc<float> {   // a few elements per thread: FP32 partial 
 };
 template <> struct DotAcc<DF> {
     f2r v{0.f, 0.f};
-    __device__ __forceinline__ void add(f2c a, f2c b) { v = f2r_add(v, f2r_add(f2r_mul(a.re, b.re), f2r_mul(a.im, b.im))); }
+    // operands normalised first: lazy sums may carry |lo| >= |hi| after cancellation
+    __device__ __forceinline__ void add(f2c a, f2c b)
+    {
+        a = Num<DF>::norm(a);
+        b = Num<DF>::norm(b);
+        v = f2r_add(v, f2r_add(f2r_mul(a.re, b.re), f2r_mul(a.im, b.im)));
+    }
     __device__ __forceinline__ double val() const { return (double)v.hi + (double)v.lo; }
 };
 
