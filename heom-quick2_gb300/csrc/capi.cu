@@ -394,13 +394,14 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
 template <typename T>
 void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, const double2 *rhs,
                   const DevCoef<double> &K64, const DevCoef<T> &KT, double2 *r64, std::vector<double> &norms,
-                  int nlim, int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
+                  int nlim, int max_rounds, bool stall_exit, bool &stalled,
+                  int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
                   const std::function<void(const double2 *, double2 *)> &residual,
                   const std::function<void(const double2 *)> &batch_norms)
 {
     constexpr int kInnerChunk = 25;   // 50 applies between residual checks, as in the reference driver
     const int64_t N = c->lunk + 1;
-    const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 3e-7);
+    const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-10);
     InnerWork<T> W;
     inner_alloc<T>(W, nbatch, N, c->stream);
     typename Num<T>::V *gd = nullptr;
@@ -427,13 +428,22 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         CK(cudaGraphInstantiate(&gexec, graph, 0));
         std::vector<InnerState> st(nbatch);
         int round = 0;
-        for (; round < std::max(1, o.max_refine); round++) {
+        std::vector<double> prev;
+        for (; round < std::max(1, max_rounds); round++) {
             if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
             residual(x, r64);
             batch_norms(r64);
             bool all_ok = true;
             for (double v : norms) all_ok = all_ok && v <= o.crit;
             if (all_ok) { converged = true; break; }
+            // a round that did not halve some instance's residual: the inner arithmetic cannot
+            // resolve what is left, so the caller continues with FP64 inner solves
+            if (stall_exit && !prev.empty()) {
+                bool stuck = false;
+                for (int b = 0; b < nbatch; b++) stuck = stuck || (norms[b] > o.crit && norms[b] > 0.5 * prev[b]);
+                if (stuck) { stalled = true; break; }
+            }
+            prev = norms;
             for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
                 vec_from_d<T>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride,
                               norms[b] <= o.crit ? 0.0 : 1.0 / norms[b], c->stream);
@@ -443,7 +453,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             double tgt = 1.0;
             for (double v : norms) if (v > o.crit) tgt = std::min(tgt, o.crit / v);
             tgt = std::max(tgt, itol);
-            inner_start<T>(W, tgt, nlim, o.stag_window > 0 ? o.stag_window : 16, c->stream);
+            inner_start<T>(W, tgt, nlim, o.stag_window > 0 ? o.stag_window : 40, c->stream);
             aux += kInnerStartLaunches;
             for (int iters = 0;;) {
                 CK(cudaGraphLaunch(gexec, c->stream));
@@ -459,7 +469,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             for (const auto &sv : st) { applies = std::max(applies, 2 * sv.n + sv.checks); last_ierr = sv.ierr; }
             total_iters += applies;
             for (int b = 0; b < nbatch; b++)
-                if (norms[b] > o.crit) vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.xs + (int64_t)b * W.vstride, c->stream), aux++;
+                if (norms[b] > o.crit)
+                    vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.slot(st[b].best_slot) + (int64_t)b * W.vstride, c->stream), aux++;
         }
         if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
         rounds = round;
@@ -530,16 +541,25 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             tfq_free(W);
         } else {
             if (adj) fail(HEOM_E_UNSUPPORTED, "mixed precision is implemented for the forward operator");
+            bool stalled = false, unused = false;
             if (o.precision == HEOM_PREC_MIXED)
-                mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, k64, K.kdf, r64, norms, nlim, total_iters, last_ierr,
-                                 converged, info.refinements, info.launches, aux, residual, batch_norms);
+                mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, k64, K.kdf, r64, norms, nlim, o.max_refine, true, stalled,
+                                 total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
             else if (o.precision == HEOM_PREC_FP64_REFINED)
-                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim, total_iters, last_ierr,
-                                     converged, info.refinements, info.launches, aux, residual, batch_norms);
+                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim, o.max_refine, false, unused,
+                                     total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
             else if (o.precision == HEOM_PREC_MIXED_FP32)
-                mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, k64, K.k32, r64, norms, nlim, total_iters, last_ierr,
-                                    converged, info.refinements, info.launches, aux, residual, batch_norms);
+                mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, k64, K.k32, r64, norms, nlim, o.max_refine, true, stalled,
+                                    total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
             else fail(HEOM_E_ARG, "unknown precision");
+            if (stalled && !converged) {
+                // the remaining rounds with FP64 inner solves on the same regularised operator
+                int more = 0;
+                mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim,
+                                     std::max(1, o.max_refine - info.refinements), false, unused, total_iters, last_ierr,
+                                     converged, more, info.launches, aux, residual, batch_norms);
+                info.refinements += more;
+            }
         }
     } catch (...) { for (void *p : tmp) cudaFree(p); cudaEventDestroy(e0); cudaEventDestroy(e1); throw; }
     // final FP64 residual

@@ -148,7 +148,7 @@ __global__ void k_in_init(InnerWork<T> W)
         const A bv = N::load(W.b[o + t]);
         const typename N::V z = N::store(N::zero());
         W.w[o + t] = N::store(bv);
-        W.x[o + t] = z; W.xs[o + t] = z; W.y[o + t] = z; W.d[o + t] = z; W.v[o + t] = z; W.u2[o + t] = z;
+        W.x[o + t] = z; W.xs[o + t] = z; W.xs2[o + t] = z; W.y[o + t] = z; W.d[o + t] = z; W.v[o + t] = z; W.u2[o + t] = z;
         bb.add(bv, bv);
         rb.add(N::load(W.rt[t]), bv);
     }
@@ -157,7 +157,7 @@ __global__ void k_in_init(InnerWork<T> W)
 }
 
 template <typename T>
-__global__ void k_in_init_fin(InnerWork<T> W, double crit, int nlim, int stag_window)
+__global__ void __launch_bounds__(NTF) k_in_init_fin(InnerWork<T> W, double crit, int nlim, int stag_window)
 {
     const int b = blockIdx.x;
     double tot[2];
@@ -169,6 +169,7 @@ __global__ void k_in_init_fin(InnerWork<T> W, double crit, int nlim, int stag_wi
     s.rho = tot[1];
     s.crit = crit; s.nlim = nlim; s.stag_window = stag_window;
     s.best = s.r0; s.ext_resid = s.r0;
+    s.best_e = s.r0; s.best_slot = 0;   // slot 0 holds x = 0
     if (s.r0 <= crit) { s.done = 1; s.conv = 1; }
     else if (s.rho == 0.0) { s.done = 1; s.ierr = 8; }
     W.st[b] = s;
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
 }
 
 template <typename T>
-__global__ void k_in_b_fin(InnerWork<T> W)
+__global__ void __launch_bounds__(NTF) k_in_b_fin(InnerWork<T> W)
 {
     const int b = blockIdx.x;
     if (W.st[b].done) return;
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
 }
 
 template <typename T>
-__global__ void k_in_a_fin(InnerWork<T> W)
+__global__ void __launch_bounds__(NTF) k_in_a_fin(InnerWork<T> W)
 {
     const int b = blockIdx.x;
     if (W.st[b].done) return;
@@ -277,6 +278,8 @@ __global__ void k_in_a_fin(InnerWork<T> W)
     s.beta = tot[2] / s.rho;
     s.rho = tot[2];
     if (tot[2] == 0.0 || !isfinite(s.beta)) { s.done = 1; s.ierr = 8; }
+    // predicted true residual below a third of the target: stop here, measured at the next check
+    else if (s.ratio > 0.0 && s.unrm * s.r0 * s.ratio <= s.crit / 3.0) { s.done = 1; s.finishing = 1; }
     W.st[b] = s;
     using N = Num<T>;
     InnerCoef<T> k = W.cf[b];
@@ -296,17 +299,18 @@ __global__ void k_in_x(InnerWork<T> W)
     using N = Num<T>;
     using A = typename N::A;
     const int b = blockIdx.y;
-    if (W.st[b].done) return;
+    if (W.st[b].done && !W.st[b].finishing) return;
     const int64_t o = (int64_t)b * W.vstride;
     const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
     const InnerCoef<T> &k = W.cf[b];
+    typename N::V *xo = W.slot(1 - W.st[b].best_slot);   // keep the best checked iterate
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
         const A yo = N::load(W.y[o + t]);
         const A d1 = N::add(yo, N::scale(N::load(W.d[o + t]), k.dd1));
         const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[o + t]), k.alpha_prev)), N::scale(d1, k.dd2));
-        W.xs[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+        xo[o + t] = N::store(N::add(N::load(W.x[o + t]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
     }
 }
 
@@ -314,13 +318,19 @@ __global__ void k_in_x(InnerWork<T> W)
 template <typename T, bool REG>
 __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
-    FUSED_SETUP
+    using N = Num<T>;
+    using A = typename N::A;
+    const int b = blockIdx.y;
+    if (W.st[b].done && !W.st[b].finishing) return;
+    const int64_t o = (int64_t)b * W.vstride;
+    const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
+    const typename N::V *xc = W.slot(1 - W.st[b].best_slot);
     WarpAcc<T> ee;
 #pragma unroll 1
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
-        const A r = N::norm(N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, W.xs + o, t, b)));
+        const A r = N::norm(N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, xc + o, t, b)));
         ee.add(r, r);
     }
     const typename WarpAcc<T>::R ws[1] = {ee.warp_sum()};
@@ -328,10 +338,10 @@ __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, Inner
 }
 
 template <typename T>
-__global__ void k_in_chk_fin(InnerWork<T> W)
+__global__ void __launch_bounds__(NTF) k_in_chk_fin(InnerWork<T> W)
 {
     const int b = blockIdx.x;
-    if (W.st[b].done) return;
+    if (W.st[b].done && !W.st[b].finishing) return;
     double tot[1];
     grand_totals<1>(W.part, W.nblk, b, tot);
     if (threadIdx.x != 0) return;
@@ -339,6 +349,15 @@ __global__ void k_in_chk_fin(InnerWork<T> W)
     const double e = sqrt(tot[0]);
     s.ext_resid = e;
     s.checks += 1;
+    if (s.unrm > 0.0) s.ratio = e / (s.unrm * s.r0);
+    if (e < s.best_e) { s.best_e = e; s.best_slot = 1 - s.best_slot; }
+    if (s.finishing) {   // stopped on the prediction: record what the check found
+        s.finishing = 0;
+        s.conv = e <= s.crit;
+        s.ierr = isfinite(e) ? (s.conv ? 0 : 4) : 8;
+        W.st[b] = s;
+        return;
+    }
     if (e <= s.crit) { s.done = 1; s.conv = 1; s.ierr = 0; }
     else if (s.n >= s.nlim) { s.done = 1; s.ierr = 4; }
     else if (s.stag_window) {
@@ -365,8 +384,8 @@ __global__ void k_in_fill(InnerWork<T> W)
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
         const typename N::V r = W.rt[t];
-        typename N::V *vec[9] = {W.x, W.xs, W.b, W.w, W.y, W.d, W.v, W.u1, W.u2};
-        for (int k = 0; k < 9; k++)
+        typename N::V *vec[10] = {W.x, W.xs, W.b, W.w, W.y, W.d, W.v, W.u1, W.u2, W.xs2};
+        for (int k = 0; k < 10; k++)
             vec[k][o + t] = N::store(N::scale(N::load(r), N::sc(1.0 + 0.125 * k)));
     }
     if (t0 == 0) {
@@ -427,7 +446,7 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     const size_t vbytes = sizeof(V) * (size_t)W.vstride * nbatch;
     // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
     auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t total = rounded(vbytes) * 9 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(InnerState) * nbatch) +
+    const size_t total = rounded(vbytes) * 10 + rounded(sizeof(V) * (size_t)W.vstride) + rounded(sizeof(InnerState) * nbatch) +
                          rounded(sizeof(InnerCoef<T>) * nbatch) + rounded(sizeof(double) * 3 * (size_t)nbatch * W.nblk);
     char *p = nullptr;
     if (cudaMalloc((void **)&p, total) != cudaSuccess) fail(HEOM_E_NOMEM, "device allocation of the inner-solver workspace failed");
@@ -439,7 +458,7 @@ void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s)
     auto take = [&](size_t bytes) { char *q = p; p += rounded(bytes); return q; };
     W.x = (V *)take(vbytes); W.xs = (V *)take(vbytes); W.b = (V *)take(vbytes); W.w = (V *)take(vbytes);
     W.y = (V *)take(vbytes); W.d = (V *)take(vbytes); W.v = (V *)take(vbytes); W.u1 = (V *)take(vbytes);
-    W.u2 = (V *)take(vbytes);
+    W.u2 = (V *)take(vbytes); W.xs2 = (V *)take(vbytes);
     W.rt = (V *)take(sizeof(V) * (size_t)W.vstride);
     W.st = (InnerState *)take(sizeof(InnerState) * nbatch);
     W.cf = (InnerCoef<T> *)take(sizeof(InnerCoef<T>) * nbatch);

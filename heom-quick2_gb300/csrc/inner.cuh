@@ -14,8 +14,12 @@
 //      partials ||w1||^2, ||w2||^2, <r~, w2>
 //   A_fin: the two half steps' var, cos, tau, eta; the pending coefficients; beta, rho
 // Every `chunk` iterations a check forms xs = x + pending updates and ||b - A xs||; the
-// solve of an instance ends at a check (converged, floor reached or iteration limit) and
-// its result is xs.  Inner products are summed per thread and per warp in the vectors'
+// solve of an instance ends at a check (converged, floor reached or iteration limit), or
+// at the iteration where TFQMR's bound times the bound-to-true ratio of the last check
+// predicts a residual of a third of the target; such an instance skips the rest of the
+// chunk and the next check forms and measures its xs.  Checked iterates alternate between
+// two slots so that the best one is kept: it is the result, also when an instance stops
+// at its arithmetic's floor after the residual has begun to drift up.  Inner products are summed per thread and per warp in the vectors'
 // number type and across warps and blocks in FP64, in a fixed order (deterministic).
 // Launches per iteration: 4 (no guarded no-ops).  The FP64 reference solver keeps the
 // unfused form of solver.cuh, whose iterates follow the reference driver step by step.
@@ -26,7 +30,11 @@ namespace heom {
 
 struct InnerState {
     double r0, tau, var, eta, rho, beta, alpha, crit, best, ext_resid, unrm;
+    double ratio;      // true residual / TFQMR's bound sqrt(2n+1) tau at the last check (0 before it)
+    double best_e;     // smallest checked residual, held by iterate slot best_slot
     int n, nlim, done, ierr, stag, stag_window, checks, conv;
+    int finishing;     // stopped on the predicted residual: the next check forms and measures xs
+    int best_slot;     // 0 or 1: which xs slot holds the best checked iterate (the result)
 };
 
 // Per-instance scalars in the number type of the vectors, written by the finalisers so
@@ -44,6 +52,8 @@ struct InnerWork {
     int64_t vstride = 0;        // complex elements between instances
     V *x = nullptr, *xs = nullptr, *b = nullptr, *w = nullptr, *y = nullptr, *d = nullptr, *v = nullptr,
       *u1 = nullptr, *u2 = nullptr, *rt = nullptr;
+    V *xs2 = nullptr;           // second iterate slot (xs is slot 0)
+    __host__ __device__ V *slot(int s) const { return s ? xs2 : xs; }
     InnerState *st = nullptr;
     InnerCoef<T> *cf = nullptr;
     double *part = nullptr;     // per-block partials: 3 runs of nblk per instance

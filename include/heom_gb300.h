@@ -151,10 +151,14 @@ typedef struct {
     int32_t precision;        /* HEOM_PREC_FP64, HEOM_PREC_MIXED or HEOM_PREC_MIXED_FP32 */
     double inner_tol;         /* MIXED*: an inner solve stops at ||r|| <= max(crit, inner_tol ||r0||),
                                  r0 its FP64 right-hand side; <= 0 selects the default
-                                 (3e-7 for MIXED and FP64_REFINED, 1e-2 for MIXED_FP32) */
-    int32_t max_refine;       /* MIXED: outer refinement rounds */
+                                 (1e-10 for MIXED and FP64_REFINED: one round to the target
+                                 unless the inner arithmetic's floor stops it; 1e-2 for
+                                 MIXED_FP32) */
+    int32_t max_refine;       /* MIXED: outer refinement rounds; a round that fails to halve an
+                                 instance's FP64 residual hands the remaining rounds to FP64
+                                 inner solves on the same regularised operator */
     int32_t stag_window;      /* MIXED: an inner solve also stops after this many every-50-applies
-                                 tests without halving its residual; <= 0 selects 16 */
+                                 tests without halving its residual; <= 0 selects 40 */
 } heom_solve_opts;
 
 typedef struct {
