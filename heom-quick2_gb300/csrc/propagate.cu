@@ -119,9 +119,17 @@ int cheby_terms(double delta, double dt, double dpre)
     return n;
 }
 
-void stage_shift(const PropClock *clk, double frac, double *es, cudaStream_t s)
+void stage_prepare(heom_ctx *c, PropBuffers &B, double frac, bool adj, cudaStream_t s)
 {
-    k_stage_shift<<<1, 32, 0, s>>>(clk, frac, es);
+    k_stage_shift<<<1, 32, 0, s>>>(B.clk, frac, B.es);
+    DevCoef<double> K = c->dfwd.template coef<double>();
+    K.eshift = B.es;
+    fill_gdiag<double>(c->dfwd.view, K, B.gd, 1, s);
+    if (adj) {
+        DevCoef<double> KA = c->dadj.template coef<double>();
+        KA.eshift = B.es;
+        fill_gdiag<double>(c->dadj.view, KA, B.gda, 1, s);
+    }
 }
 
 void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale)
@@ -139,8 +147,10 @@ PropBuffers::PropBuffers(heom_ctx *c, int nvec, int64_t njt)
     N = c->lunk + 1;
     // every piece starts on a 256-byte boundary; the size is the sum of the rounded pieces
     auto rounded = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t nd = (size_t)std::max<int32_t>(1, std::max(c->dfwd.view.nado, c->has_adj ? c->dadj.view.nado : 0));
     const size_t bytes = rounded(sizeof(double2) * (size_t)N) * nvec + rounded(sizeof(double) * 8) +
-                         rounded(sizeof(PropClock)) + rounded(sizeof(double) * std::max<int64_t>(njt, 1));
+                         rounded(sizeof(PropClock)) + rounded(sizeof(double) * std::max<int64_t>(njt, 1)) +
+                         2 * rounded(sizeof(double2) * nd);
     CK(cudaMalloc(&mem, bytes));
     char *p = (char *)mem;
     auto take = [&](size_t b) { char *q = p; p += rounded(b); return (void *)q; };
@@ -148,6 +158,8 @@ PropBuffers::PropBuffers(heom_ctx *c, int nvec, int64_t njt)
     es = (double *)take(sizeof(double) * 8);
     clk = (PropClock *)take(sizeof(PropClock));
     jt = (double *)take(sizeof(double) * std::max<int64_t>(njt, 1));
+    gd = (double2 *)take(sizeof(double2) * nd);
+    gda = (double2 *)take(sizeof(double2) * nd);
     CK(cudaMemsetAsync(mem, 0, bytes, c->stream));
 }
 PropBuffers::~PropBuffers() { if (mem) cudaFree(mem); }
@@ -160,6 +172,7 @@ void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &Kin, PropBuffe
     DevCoef<double> K = Kin;
     K.trace_on = 0;
     K.eshift = B.es;
+    K.gdiag = B.gd;   // refreshed by stage_prepare before each stage's applies
     const int64_t N = B.N, L = c->lunk;
     const int ns = c->nalf * c->nspin;
     cudaStream_t s = c->stream;
@@ -170,7 +183,7 @@ void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &Kin, PropBuffe
         const double fr[4] = {0.0, 0.5, 0.5, 1.0};
         const double a[4] = {dt / 2, dt / 2, dt, 0.0}, b[4] = {dt / 6, dt / 3, dt / 3, dt / 6};
         for (int st = 0; st < 4; st++) {
-            k_stage_shift<<<1, 32, 0, s>>>(B.clk, fr[st], B.es);
+            stage_prepare(c, B, fr[st], false, s);
             launch_apply<double, false>(P, K, st == 0 ? rho : rt, k, 1, N, nullptr, s);
             k_rk4<<<grid_for(L), NT, 0, s>>>(L, rho, k, rt, acc, a[st], b[st], st == 0, st < 3);
         }
@@ -178,7 +191,7 @@ void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &Kin, PropBuffe
     } else {
         // rho(t+dt) = J0 P0 + 2 sum_n J_n(delta dt) P_n, P1 = L P0 / delta, P_n = P_{n-2} + (2/delta) L P_{n-1}
         double2 *pm2 = B.vec[0], *pm1 = B.vec[1], *pn = B.vec[2], *lp = B.vec[3];
-        k_stage_shift<<<1, 32, 0, s>>>(B.clk, 0.0, B.es);
+        stage_prepare(c, B, 0.0, false, s);
         CK(cudaMemcpyAsync(pm2, rho, sizeof(double2) * L, cudaMemcpyDeviceToDevice, s));
         launch_apply<double, false>(P, K, pm2, lp, 1, N, nullptr, s);
         k_cheb<<<grid_for(L), NT, 0, s>>>(L, pm2, lp, pm1, rho, 1.0 / delta, 2.0 * bes[1], 1, bes[0]);

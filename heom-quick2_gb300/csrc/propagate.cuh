@@ -21,6 +21,8 @@ struct PropBuffers {
     void *mem = nullptr;
     std::vector<double2 *> vec;   // nvec FP64 vectors of lunk + 1 elements
     double *es = nullptr;         // 4 lead shifts of the current stage (+4 spare)
+    double2 *gd = nullptr;        // ADO diagonals of the forward plan at the current stage
+    double2 *gda = nullptr;       // ADO diagonals of the adjoint plan at the current stage
     PropClock *clk = nullptr;
     double *jt = nullptr;         // recorded currents
     PropBuffers(heom_ctx *c, int nvec, int64_t njt);
@@ -29,12 +31,15 @@ struct PropBuffers {
     PropBuffers &operator=(const PropBuffers &) = delete;
 };
 
+// es = the lead shifts at the stage (frac of a step) and the matching ADO diagonals in B.gd
+// (and B.gda for the adjoint plan when adj is set), so the stage's FP64 applies read g
+// instead of summing the lead shifts per entry
+void stage_prepare(heom_ctx *c, PropBuffers &B, double frac, bool adj, cudaStream_t s);
+
 double bessel_j(int n, double x);
 double cheby_width(heom_ctx *c);
 int cheby_terms(double delta, double dt, double dpre);
 void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale);
-// es = eshift at t0 + (n + frac) dt, n read from the device clock
-void stage_shift(const PropClock *clk, double frac, double *es, cudaStream_t s);
 void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &K, PropBuffers &B, double2 *rho, double delta,
                   const std::vector<double> &bes, bool record_current);
 

@@ -156,6 +156,7 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
             DevCoef<double> KF = Kf.k64, KA = Ka.k64;
             KF.trace_on = 0; KA.trace_on = 0;
             KF.eshift = B.es; KA.eshift = B.es;
+            KF.gdiag = B.gd; KA.gdiag = B.gda;   // refreshed by stage_prepare
             cudaStream_t s = c->stream;
             const int gL = grid_for(L);
             for (int sg = ncp - 1; sg >= 0; sg--) {
@@ -170,7 +171,7 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
                 }
                 for (int n = n1 - 1; n >= n0; n--) {
                     k_set_step<<<1, 1, 0, s>>>(B.clk, n);
-                    stage_shift(B.clk, 0.0, B.es, s);
+                    stage_prepare(c, B, 0.0, true, s);
                     // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1}
                     CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
                     for (int k = 1; k < K; k++) {
