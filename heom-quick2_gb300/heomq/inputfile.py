@@ -13,7 +13,8 @@ Supported subset: the Lorentzian PSD sparse path (psdjob = T, lsparse = T, metho
 fieldtype = 0) with $para1 (one orbital), $para4 (two orbitals, $ddots), or
 $hamil_sys lreadhs = T (H from hamil_sys.data, internal units).  Anything else raises.
 
-State files (Intel form='binary', i.e. raw streams without record markers):
+State files (Intel form='binary', i.e. raw streams without record markers; TAPE_n.resume
+of a time propagation in write_tape / read_tape):
   rho_spa.st / .gr / .sav / .chk : int32 norbs, nspin, ncor, ntier0, nalf; int64 nunk;
                                    then the nnz_spa(n) complex128 entries of every ADO n with
                                    entries, in ADO order (main/main.f90:1087-1105,
@@ -202,6 +203,41 @@ def read_rho_spa(path, model):
     rho = np.zeros(model.lunk, dtype=np.complex128)
     rho[:count] = data[:count]
     return rho
+
+
+def write_tape(path, model, t, rho):
+    """Resume tape of a time propagation (td/resumejob.f90:83-105, sparse mode, no heat bath):
+    float64 t; int32 ntier, norbs, nspin, ncor, nalf, numfff (0 without psdfff); int64 nunk;
+    int32 lhb (0); int64 lunk; then the lunk complex128 entries."""
+    rho = np.ascontiguousarray(rho, dtype=np.complex128)
+    if rho.size != model.lunk:
+        raise ValueError("rho must hold lunk entries")
+    with open(path, "wb") as f:
+        f.write(struct.pack("<d", float(t)))
+        f.write(struct.pack("<6i", model.ntier, model.norbs, model.nspin, model.ncor, model.nalf, 0))
+        f.write(struct.pack("<q", model.nunk))
+        f.write(struct.pack("<i", 0))
+        f.write(struct.pack("<q", model.lunk))
+        f.write(rho.tobytes())
+
+
+def read_tape(path, model):
+    """(t, rho) from a resume tape written for `model` (td/resumejob.f90:17-70): every header
+    field must match, as in the reference, and tapes with heat-bath data are refused."""
+    with open(path, "rb") as f:
+        (t,) = struct.unpack("<d", f.read(8))
+        head = struct.unpack("<6i", f.read(24))
+        (nunk,) = struct.unpack("<q", f.read(8))
+        (lhb,) = struct.unpack("<i", f.read(4))
+        if lhb:
+            raise ValueError("resume tape carries heat-bath data (lhb = T), which is not supported")
+        (lunk,) = struct.unpack("<q", f.read(8))
+        data = np.frombuffer(f.read(16 * lunk), dtype=np.complex128)
+    if head != (model.ntier, model.norbs, model.nspin, model.ncor, model.nalf, 0):
+        raise ValueError(f"resume tape does not match the model: {head}")
+    if nunk != model.nunk or lunk != model.lunk or data.size != lunk:
+        raise ValueError("resume tape does not match the model's ADO count or stored entries")
+    return t, data.copy()
 
 
 def write_hamil_sys(path, hs):

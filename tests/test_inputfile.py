@@ -109,3 +109,23 @@ def test_unsupported_options_are_refused():
         inp.to_config(SIAM_INPUT.replace("methodss=2", "methodss=0"))
     with pytest.raises(ValueError):
         inp.to_config(SIAM_INPUT.replace("$field fieldtype=0", "$field fieldtype=1"))
+
+
+def test_resume_tape_round_trip_and_layout(tmp_path):
+    m = heomq.Model(cf.siam(ntier=3, nmats=2))
+    rng = np.random.default_rng(5)
+    rho = rng.standard_normal(m.lunk) + 1j * rng.standard_normal(m.lunk)
+    path = tmp_path / "TAPE_3.resume"
+    inp.write_tape(path, m, 12.5, rho)
+    raw = path.read_bytes()
+    assert len(raw) == 8 + 24 + 8 + 4 + 8 + 16 * m.lunk
+    assert np.frombuffer(raw[:8], dtype="<f8")[0] == 12.5
+    assert np.frombuffer(raw[8:32], dtype="<i4").tolist() == [m.ntier, m.norbs, m.nspin, m.ncor, m.nalf, 0]
+    assert np.frombuffer(raw[32:40], dtype="<i8")[0] == m.nunk
+    assert np.frombuffer(raw[44:52], dtype="<i8")[0] == m.lunk
+    t, back = inp.read_tape(path, m)
+    assert t == 12.5
+    np.testing.assert_array_equal(back, rho)
+    other = heomq.Model(cf.siam(ntier=4, nmats=2))
+    with pytest.raises(ValueError):
+        inp.read_tape(path, other)
