@@ -5,8 +5,12 @@ sparsity) differ only in their H values and lead shifts; each such group is one
 heom_batch, solved in one launch sequence.  Groups are solved one after the other: each
 batch already fills the GPU, and running two contexts' solves from two host threads
 overlaps little (about 6 % measured) while their graph captures would have to be kept
-apart from each other's synchronisations.
+apart from each other's synchronisations.  The host work of a group (its tables and the
+per-instance H) runs in worker threads, so that the larger tables are built while the
+smaller groups solve.
 """
+
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -47,14 +51,19 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8):
     currents = np.zeros(len(cfgs))
     infos = [None] * len(groups)
 
-    def run(gi):
-        idx = groups[gi]
+    def prepare(idx):
+        # host only (the table builder and the tier-1 models release the GIL in their C calls):
+        # runs in worker threads while earlier groups solve on the device
         rep = Model(cfgs[idx[0]])
-        ctx = Context(rep, device=device, adjoint=False)
         nd2 = rep.nrho ** 2
         # H depends on the level parameters only: a tier-1 model of each instance gives it cheaply
         hs = np.stack([Model(dict(cfgs[i], ntier=2)).get("hs", nd2, np.complex128) for i in idx])
         es = np.stack([_lead_shift(cfgs[i], rep.nalf, rep.nspin) for i in idx])
+        return rep, hs, es
+
+    def run(gi, rep, hs, es):
+        idx = groups[gi]
+        ctx = Context(rep, device=device, adjoint=False)
         batch = Batch(ctx, hs_batch=hs, eshift_batch=es, nbatch=len(idx))
         with torch.cuda.device(device):
             x = torch.zeros((len(idx), batch.stride), dtype=torch.complex128, device=f"cuda:{device}")
@@ -67,6 +76,10 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8):
         batch.close()
         ctx.close()
 
-    for gi in range(len(groups)):
-        run(gi)
+    # groups with the smaller tables first, so that the larger tables are built meanwhile
+    order = sorted(range(len(groups)), key=lambda g: (cfgs[groups[g][0]]["ntier"], len(groups[g])))
+    with ThreadPoolExecutor(max_workers=max(1, min(4, len(groups)))) as ex:
+        futures = {g: ex.submit(prepare, groups[g]) for g in order}
+        for g in order:
+            run(g, *futures[g].result())
     return currents, infos
