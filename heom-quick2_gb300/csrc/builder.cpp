@@ -499,25 +499,30 @@ void build_pattern(heom_model &m) {
     std::vector<std::vector<int>> rofc(m.norbs * m.nspin), cofr(m.norbs * m.nspin);
     for (int s = 1; s <= m.nspin; s++)
         for (int o = 1; o <= m.norbs; o++) opmaps(o, s, rofc[(o - 1) + (s - 1) * m.norbs], cofr[(o - 1) + (s - 1) * m.norbs]);
-    std::vector<Bits> pat((size_t)m.nunk, Bits(0));
-    pat[0] = e;
+    // pattern bits of every ADO in one flat array; scratch sets reused across ADOs
+    const size_t nw = ((size_t)n * n + 63) / 64;
+    std::vector<uint64_t> pat((size_t)m.nunk * nw, 0);
+    std::copy(e.w.begin(), e.w.end(), pat.begin());
+    auto bit = [n](const uint64_t *w, int i, int j) { size_t k = (size_t)i + (size_t)j * n; return (w[k >> 6] >> (k & 63)) & 1; };
+    Bits acc(n), sl(n), sr(n);
     for (int it = 2; it <= m.ntier; it++) {
         int nb = it - 1;
         for (int64_t lni = m.nfirst[it - 1]; lni <= m.nlast[it - 1]; lni++) {
-            Bits acc(n);
+            std::fill(acc.w.begin(), acc.w.end(), 0);
             bool empty = false;
             int64_t lnl = m.index_coef_ref[lni - 1];
             for (int b = 0; b < nb; b++, lnl++) {
                 int d = m.indextable[m.ifirst[it - 1] - 1 + (lni - m.nfirst[it - 1]) * nb + b];
                 int o = m.morbs[d - 1], s = m.mspin[d - 1], a = m.ilead[d - 1];
                 if (std::fabs(m.hybrid[(a - 1) * m.norbs + (o - 1)]) <= heom::kDsmall) { empty = true; continue; }
-                const Bits &low = pat[m.indexcoef[lnl - 1] - 1];
+                const uint64_t *low = &pat[(size_t)(m.indexcoef[lnl - 1] - 1) * nw];
                 bool tr = m.itypecoef[lnl - 1] != 0, dag = m.mpm[d - 1] == 1;
                 const std::vector<int> &rc = rofc[(o - 1) + (s - 1) * m.norbs], &cr = cofr[(o - 1) + (s - 1) * m.norbs];
-                Bits sl(n), sr(n);
+                std::fill(sl.w.begin(), sl.w.end(), 0);
+                std::fill(sr.w.begin(), sr.w.end(), 0);
                 for (int c = 0; c < n; c++)
                     for (int r = 0; r < n; r++) {
-                        if (!(tr ? low.get(c, r) : low.get(r, c))) continue;
+                        if (!(tr ? bit(low, c, r) : bit(low, r, c))) continue;
                         int i = dag ? cr[r + 1] : rc[r + 1];    // left:  op(a)(i, r)
                         if (i) sl.set(i - 1, c);
                         int jj = dag ? rc[c + 1] : cr[c + 1];   // right: op(a)(c, jj)
@@ -529,7 +534,7 @@ void build_pattern(heom_model &m) {
                             if (src->get(k, j))
                                 for (int i : ecol[k]) acc.set(i, j);
             }
-            pat[lni - 1] = empty ? Bits(n) : acc;
+            if (!empty) std::copy(acc.w.begin(), acc.w.end(), pat.begin() + (size_t)(lni - 1) * nw);
         }
     }
     m.nnz_spa.assign(m.nunk, 0);
@@ -538,10 +543,10 @@ void build_pattern(heom_model &m) {
     for (int64_t u = 0; u < m.nunk; u++) {
         m.ind_spa[u] = off;
         int cnt = 0;
-        if (!pat[u].w.empty())
-            for (int j = 0; j < n; j++)
-                for (int i = 0; i < n; i++)
-                    if (pat[u].get(i, j)) { m.irow_spa.push_back(i + 1); m.icol_spa.push_back(j + 1); cnt++; }
+        const uint64_t *pu = &pat[(size_t)u * nw];
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++)
+                if (bit(pu, i, j)) { m.irow_spa.push_back(i + 1); m.icol_spa.push_back(j + 1); cnt++; }
         m.nnz_spa[u] = cnt;
         off += cnt;
     }
