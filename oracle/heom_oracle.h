@@ -138,4 +138,23 @@ double orc_besselj_ext(int n, double x);
 void orc_drandn(int64_t n, double *dx, int seed);
 double orc_dnrm2(int64_t n, const double *x);
 
+/* Correlation-function system of B rho, B = a_{iorbs,ispin} (corrfunc/prelude_cf_spa.f90,
+ * calc_ax_cf_spa_omp.f90, solve_cf_tfqmr_spa.f90).  The unknown has two components h and a
+ * (rcga, rcgb), each lunkcf entries on the pattern nnzcf/indcf/irowcf/icolcf. */
+typedef struct {
+    int iorbs, ispin;
+    int64_t lunkcf;
+    int *nnzcf; int64_t *indcf;
+    int *irowcf, *icolcf;
+} orc_cf;
+int  orc_cf_build(const orc_model *m, int iorbs, int ispin, unsigned long long seed, orc_cf **out);
+void orc_cf_free(orc_cf *cf);
+/* (yh, ya) = L_cf(omega, isgnw) (xh, xa) */
+void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw, const ozc *xh, const ozc *xa,
+                  ozc *yh, ozc *ya);
+/* brhoh, brhoa from the steady rho (lunk entries); isgnb 1: a^dag rho + rho a, 2: a rho + rho a^dag */
+void orc_cf_rhs(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, ozc *bh, ozc *ba);
+int64_t orc_cf_info(const orc_cf *cf, const char *key);
+int orc_cf_copy(const orc_cf *cf, int64_t nunk, const char *name, void *dst);
+
 #endif

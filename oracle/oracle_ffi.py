@@ -67,6 +67,13 @@ def lib():
         L.orc_drandn.argtypes = [C.c_int64, C.c_void_p, C.c_int]
         L.orc_besselj_ext.restype = C.c_double
         L.orc_besselj_ext.argtypes = [C.c_int, C.c_double]
+        L.orc_cf_build.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]
+        L.orc_cf_free.argtypes = [C.c_void_p]
+        L.orc_cf_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int] + [C.c_void_p] * 4
+        L.orc_cf_rhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_cf_info.restype = C.c_int64
+        L.orc_cf_info.argtypes = [C.c_void_p, C.c_char_p]
+        L.orc_cf_copy.argtypes = [C.c_void_p, C.c_int64, C.c_char_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -138,6 +145,15 @@ class Model:
         a = np.zeros(cnt, dtype=self._dtypes.get(name, np.int32))
         if lib().orc_copy(self.h, name.encode(), a.ctypes.data) != 0:
             raise KeyError(name)
+        return a
+
+    def dense_op(self, iorbs, ispin):
+        """a_{iorbs,ispin} as a dense nrho x nrho matrix."""
+        nr, na = self.nrho, self.nams
+        k = na * ((iorbs - 1) + (ispin - 1) * self.norbs)
+        r, c, sg = (self.get(x)[k:k + na] for x in ("rowams", "colams", "sgnams"))
+        a = np.zeros((nr, nr))
+        a[r - 1, c - 1] = np.where(sg != 0, -1.0, 1.0)
         return a
 
     # ---- applies ----
@@ -213,3 +229,97 @@ def besselj(n, x):
 
 def cheby_nterms(delta, dt, dpre=1e-21):
     return lib().orc_cheby_nterms(delta, dt, dpre)
+
+
+HBAR = 0.658211928
+
+
+class CF:
+    """Correlation-function system of B = a_{iorbs,ispin} on an oracle model
+    (corrfunc/prelude_cf_spa.f90, calc_ax_cf_spa_omp.f90, solve_cf_tfqmr_spa.f90).
+
+    The unknown has two components (h, a), each lunkcf complex entries.  The operator is
+    real-linear only (its RDO row adds conjugate transposes), so solves work on the real
+    vector [Re h, Im h, Re a, Im a]."""
+
+    def __init__(self, model, iorbs=1, ispin=1, seed=20261203):
+        self.model = model
+        h = C.c_void_p()
+        if lib().orc_cf_build(model.h, iorbs, ispin, seed, C.byref(h)) != 0:
+            raise RuntimeError("oracle cf build failed: " + lib().orc_last_error().decode())
+        self.h = h
+        self.iorbs, self.ispin = iorbs, ispin
+        self.lunkcf = int(lib().orc_cf_info(h, b"lunkcf"))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_cf_free(self.h)
+            self.h = None
+
+    def get(self, name):
+        n = {"nnzcf_spa": self.model.nunk, "indcf_spa": self.model.nunk,
+             "irowcf_spa": self.lunkcf, "icolcf_spa": self.lunkcf}[name]
+        a = np.zeros(n, dtype=np.int64 if name == "indcf_spa" else np.int32)
+        if lib().orc_cf_copy(self.h, self.model.nunk, name.encode(), a.ctypes.data) != 0:
+            raise KeyError(name)
+        return a
+
+    def apply(self, omega, isgnw, xh, xa):
+        """(yh, ya) = L_cf (xh, xa); omega in internal units (energy / hbar)."""
+        xh = np.ascontiguousarray(xh, dtype=np.complex128)
+        xa = np.ascontiguousarray(xa, dtype=np.complex128)
+        yh = np.zeros(self.lunkcf, dtype=np.complex128)
+        ya = np.zeros(self.lunkcf, dtype=np.complex128)
+        lib().orc_cf_apply(self.model.h, self.h, omega, isgnw, xh.ctypes.data, xa.ctypes.data,
+                           yh.ctypes.data, ya.ctypes.data)
+        return yh, ya
+
+    def rhs(self, rho, isgnb):
+        rho = np.ascontiguousarray(rho, dtype=np.complex128)
+        bh = np.zeros(self.lunkcf, dtype=np.complex128)
+        ba = np.zeros(self.lunkcf, dtype=np.complex128)
+        lib().orc_cf_rhs(self.model.h, self.h, rho.ctypes.data, isgnb, bh.ctypes.data, ba.ctypes.data)
+        return bh, ba
+
+    def _split(self, z):
+        n = self.lunkcf
+        return z[:n] + 1j * z[n:2 * n], z[2 * n:3 * n] + 1j * z[3 * n:]
+
+    def solve(self, rho, omega, isgnb, isgnw, tol=1e-12):
+        """Solve L_cf x = -(brhoh, brhoa) (solve_cf_tfqmr_spa.f90:185-197) with restarted GMRES."""
+        from scipy.sparse.linalg import LinearOperator, gmres
+        n = self.lunkcf
+
+        def mv(z):
+            yh, ya = self.apply(omega, isgnw, *self._split(np.asarray(z).ravel()))
+            return np.concatenate([yh.real, yh.imag, ya.real, ya.imag])
+
+        bh, ba = self.rhs(rho, isgnb)
+        b = -np.concatenate([bh.real, bh.imag, ba.real, ba.imag])
+        op = LinearOperator((4 * n, 4 * n), matvec=mv, dtype=np.float64)
+        z, info = gmres(op, b, rtol=tol, atol=0.0, restart=200, maxiter=200)
+        resid = np.linalg.norm(mv(z) - b) / max(np.linalg.norm(b), 1e-300)
+        xh, xa = self._split(z)
+        return xh, xa, resid
+
+    def rdo(self, x):
+        """Dense nrho x nrho matrix of the first (RDO) block of a cf component."""
+        nr = self.model.nrho
+        nz = int(self.get("nnzcf_spa")[0])
+        ir, ic = self.get("irowcf_spa")[:nz], self.get("icolcf_spa")[:nz]
+        out = np.zeros((nr, nr), dtype=np.complex128)
+        out[ir - 1, ic - 1] = x[:nz]
+        return out
+
+    def dos(self, rho, omega_ev, tol=1e-12):
+        """Spectral function A(omega) of a_{iorbs,ispin} in 1/eV (corrfunc/corrfunc.f90:146-192):
+        (total, part from C_{B^dag B}, part from C_{B B^dag})."""
+        a = self.model.dense_op(self.iorbs, self.ispin)
+        w = omega_ev / HBAR
+        xh, xa, _ = self.solve(rho, w, 2, 2, tol)
+        c5 = 0.5 * self.rdo(xh) + 0.5j * self.rdo(xa)
+        d1 = np.trace(a.conj().T @ c5).real / np.pi / HBAR
+        xh, xa, _ = self.solve(rho, w, 1, 1, tol)
+        c5 = 0.5 * self.rdo(xh) + 0.5j * self.rdo(xa)
+        d2 = np.trace(a @ c5).real / np.pi / HBAR
+        return d1 + d2, d1, d2

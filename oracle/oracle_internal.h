@@ -12,6 +12,12 @@ int orc_build_tables(orc_model *m);
 int orc_build_pattern(orc_model *m, unsigned long long seed);
 void orc_symeig(int n, double *a, double *w, double *v);
 size_t orc_cbidx(const orc_model *m, int iorbs, int ispin, int icor, int ialf, int isgn);
+/* shared by the steady and correlation-function pattern builders */
+void orc_rng_seed(unsigned long long seed);
+double orc_normal(void);
+void orc_exp_taylor(int n, const ozc *h, double alpha, int kmax, ozc *out);
+int orc_ams_coo(const orc_model *m, int left, int dag_a, int dag_b, int iorbs, int ispin,
+                int nnz, const int *ir, const int *ic, const ozc *v, int *orow, int *ocol, ozc *oval);
 
 /* operator entry k (0-based) of a_{iorbs,ispin} */
 static inline size_t orc_opbase(const orc_model *m, int iorbs, int ispin)

@@ -214,19 +214,20 @@ int orc_build_tables(orc_model *m)
 /* ---------------- sparsity (fermion/prelude_spa.f90:146-747) ---------------- */
 
 static unsigned long long g_rng;
+void orc_rng_seed(unsigned long long seed) { g_rng = seed * 2654435761ULL + 88172645463325252ULL; }
 static double orc_uniform(void)
 {
     g_rng ^= g_rng << 13; g_rng ^= g_rng >> 7; g_rng ^= g_rng << 17;
     return ((g_rng >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
-static double orc_normal(void)
+double orc_normal(void)
 {
     double u1 = orc_uniform(), u2 = orc_uniform();
     return sqrt(-2.0 * log(u1)) * cos(2.0 * ORC_PI * u2);
 }
 
 /* utility/calc_exp_hmat.f90: 1 + sum_{k<=kmax} (alpha H)^k / k! */
-static void orc_exp_taylor(int n, const ozc *h, double alpha, int kmax, ozc *out)
+void orc_exp_taylor(int n, const ozc *h, double alpha, int kmax, ozc *out)
 {
     size_t nn = (size_t)n * n;
     ozc *c1 = calloc(nn, sizeof(ozc)), *c2 = calloc(nn, sizeof(ozc));
@@ -247,8 +248,8 @@ static void orc_exp_taylor(int n, const ozc *h, double alpha, int kmax, ozc *out
 /* zamsmm_coo semantics (utility/zamsmm_coo.f90): op(a) op(B) (left) or op(B) op(a) (right)
  * for B in COO; the result of a partial permutation times a COO matrix is returned
  * as a COO list (no duplicates can arise). */
-static int orc_ams_coo(const orc_model *m, int left, int dag_a, int dag_b, int iorbs, int ispin,
-                       int nnz, const int *ir, const int *ic, const ozc *v, int *orow, int *ocol, ozc *oval)
+int orc_ams_coo(const orc_model *m, int left, int dag_a, int dag_b, int iorbs, int ispin,
+                int nnz, const int *ir, const int *ic, const ozc *v, int *orow, int *ocol, ozc *oval)
 {
     int cnt = 0;
     for (int q = 0; q < nnz; q++) {
@@ -264,7 +265,7 @@ static int orc_ams_coo(const orc_model *m, int left, int dag_a, int dag_b, int i
 int orc_build_pattern(orc_model *m, unsigned long long seed)
 {
     int n = m->nrho; size_t nn = (size_t)n * n;
-    g_rng = seed * 2654435761ULL + 88172645463325252ULL;
+    orc_rng_seed(seed);
     ozc *e10 = calloc(nn, sizeof(ozc)), *e11 = calloc(nn, sizeof(ozc));
     orc_exp_taylor(n, m->hs, 0.31415926, 10, e10);
     orc_exp_taylor(n, m->hs, 0.31415926, 11, e11);
