@@ -12,6 +12,9 @@
 //
 // REG selects the regularised operator of the mixed-precision inner solves (see DevCoef):
 // reads of RDO entries (source offset 0) see the Hermitian part (x_q + conj x_q')/2.
+// CF selects the correlation-function operator (corrfunc/calc_ax_cf_spa_omp.f90) on a plan
+// of build_cf_plan: its unit pairs are real (no factor i), and every entry adds the
+// frequency term -w x[t + half] (h rows) or +w x[t - half] (a rows).
 #pragma once
 #include "device.cuh"
 
@@ -25,7 +28,7 @@ __device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V
 }
 
 // y[t] of instance b (x: that instance's vector); t in [0, lunk], lunk = the trace slot
-template <typename T, bool ADJ, bool REG>
+template <typename T, bool ADJ, bool REG, bool CF = false>
 __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, const DevCoef<T> &C,
                                                           const typename Num<T>::V *__restrict__ x, int64_t t, int b)
 {
@@ -63,6 +66,11 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         const A xq = N::load(x[q]);
         acc = N::add(acc, N::scale(N::sub(xq, N::conj(N::load(x[qp]))), N::sc(0.5 * C.reg_scale)));
         if (qp == q) acc = N::add(acc, N::from_d(C.reg_scale * N::re(N::load(x[P.lunk])) / C.ndiag, 0.0));
+    }
+    if (CF) {   // dfacta = -s, dfactb = +s (calc_ax_cf_spa_omp.f90:96-105); cf_omega[b] = s w
+        const bool hrow = t < C.cf_half;
+        const double w = hrow ? -C.cf_omega[b] : C.cf_omega[b];
+        acc = N::add(acc, N::scale(N::load(x[hrow ? t + C.cf_half : t - C.cf_half]), N::sc(w)));
     }
 
     // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
@@ -120,7 +128,7 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         }
         if (((e - e0) & 3) == 3) ua = N::norm(ua);
     }
-    acc = N::add(acc, N::mul_i(ua));
+    acc = N::add(acc, CF ? ua : N::mul_i(ua));
     return acc;
 }
 

@@ -36,6 +36,11 @@ struct heom_model {
     std::vector<int64_t> ind_spa;
     int64_t nunk = 0, lall = 0, lunk = 0;
     heom_tables view{};
+    // correlation-function pattern of the last heom_model_cf_pattern call
+    std::vector<int32_t> cf_nnz, cf_irow, cf_icol;
+    std::vector<int64_t> cf_ind;
+    int64_t cf_lunk = 0;
+    int cf_iorbs = 0, cf_ispin = 0;
 };
 
 namespace {
@@ -469,9 +474,19 @@ struct Bits {
     void set(int i, int j) { size_t k = (size_t)i + (size_t)j * n; w[k >> 6] |= 1ull << (k & 63); }
 };
 
-void build_pattern(heom_model &m) {
+// Pattern of every ADO from the RDO seed by the tier rule: an ADO of tier >= 2 holds the
+// structure of E0 (op(a) X_low + X_low op(a)) summed over its lower-tier couplings, and
+// nothing when one of its drawers has no hybridisation.  Structural propagation stands in
+// for the reference's random-coefficient products (nonzero with probability one).
+struct PatternOut {
+    std::vector<int32_t> nnz, irow, icol;
+    std::vector<int64_t> ind;
+    int64_t lunk = 0;
+};
+
+// E0 = exp(0.314 H) to Taylor order 10: pairs joined by a walk of <= 10 steps in the graph of H
+Bits exp_structure(const heom_model &m) {
     const int n = m.nrho;
-    // exp(0.314 H) to Taylor order 10: pairs joined by a walk of <= 10 steps in the graph of H
     Bits h(n), e(n);
     for (int j = 0; j < n; j++)
         for (int i = 0; i < n; i++)
@@ -486,6 +501,11 @@ void build_pattern(heom_model &m) {
                         if (e.get(i, k)) nx.set(i, j);
         e = nx;
     }
+    return e;
+}
+
+void propagate_pattern(const heom_model &m, const Bits &e, const Bits &seed, PatternOut &out) {
+    const int n = m.nrho;
     std::vector<std::vector<int>> ecol(n);   // rows of each column of E0
     for (int j = 0; j < n; j++)
         for (int i = 0; i < n; i++)
@@ -502,7 +522,7 @@ void build_pattern(heom_model &m) {
     // pattern bits of every ADO in one flat array; scratch sets reused across ADOs
     const size_t nw = ((size_t)n * n + 63) / 64;
     std::vector<uint64_t> pat((size_t)m.nunk * nw, 0);
-    std::copy(e.w.begin(), e.w.end(), pat.begin());
+    std::copy(seed.w.begin(), seed.w.end(), pat.begin());
     auto bit = [n](const uint64_t *w, int i, int j) { size_t k = (size_t)i + (size_t)j * n; return (w[k >> 6] >> (k & 63)) & 1; };
     Bits acc(n), sl(n), sr(n);
     for (int it = 2; it <= m.ntier; it++) {
@@ -537,20 +557,53 @@ void build_pattern(heom_model &m) {
             if (!empty) std::copy(acc.w.begin(), acc.w.end(), pat.begin() + (size_t)(lni - 1) * nw);
         }
     }
-    m.nnz_spa.assign(m.nunk, 0);
-    m.ind_spa.assign(m.nunk, 0);
+    out = PatternOut();
+    out.nnz.assign(m.nunk, 0);
+    out.ind.assign(m.nunk, 0);
     int64_t off = 1;
     for (int64_t u = 0; u < m.nunk; u++) {
-        m.ind_spa[u] = off;
+        out.ind[u] = off;
         int cnt = 0;
         const uint64_t *pu = &pat[(size_t)u * nw];
         for (int j = 0; j < n; j++)
             for (int i = 0; i < n; i++)
-                if (bit(pu, i, j)) { m.irow_spa.push_back(i + 1); m.icol_spa.push_back(j + 1); cnt++; }
-        m.nnz_spa[u] = cnt;
+                if (bit(pu, i, j)) { out.irow.push_back(i + 1); out.icol.push_back(j + 1); cnt++; }
+        out.nnz[u] = cnt;
         off += cnt;
     }
-    m.lunk = off - 1;
+    out.lunk = off - 1;
+}
+
+// fermion/prelude_spa.f90:146-747: the RDO seed is E0 itself
+void build_pattern(heom_model &m) {
+    Bits e = exp_structure(m);
+    PatternOut p;
+    propagate_pattern(m, e, e, p);
+    m.nnz_spa = std::move(p.nnz); m.ind_spa = std::move(p.ind);
+    m.irow_spa = std::move(p.irow); m.icol_spa = std::move(p.icol);
+    m.lunk = p.lunk;
+}
+
+// corrfunc/prelude_cf_spa.f90:146-760: the RDO seed is E0 a E0 + E0 a^dag E0 (the reference
+// mixes the two with random weights), a = a_{iorbs,ispin}
+void build_cf_pattern(heom_model &m, int iorbs, int ispin) {
+    const int n = m.nrho;
+    Bits e = exp_structure(m), seed(n);
+    size_t base = (size_t)m.nams * ((iorbs - 1) + (size_t)(ispin - 1) * m.norbs);
+    for (int q = 0; q < m.nams; q++) {
+        int k = m.rowams[base + q] - 1, l = m.colams[base + q] - 1;   // a(k, l) != 0
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++) {
+                if (e.get(i, k) && e.get(l, j)) seed.set(i, j);          // E0 a E0
+                if (e.get(i, l) && e.get(k, j)) seed.set(i, j);          // E0 a^dag E0
+            }
+    }
+    PatternOut p;
+    propagate_pattern(m, e, seed, p);
+    m.cf_nnz = std::move(p.nnz); m.cf_ind = std::move(p.ind);
+    m.cf_irow = std::move(p.irow); m.cf_icol = std::move(p.icol);
+    m.cf_lunk = p.lunk;
+    m.cf_iorbs = iorbs; m.cf_ispin = ispin;
 }
 
 void fill_view(heom_model &m) {
@@ -640,6 +693,19 @@ int heom_model_build(const heom_params *p, heom_model **out) {
 }
 
 void heom_model_destroy(heom_model *m) { delete m; }
+
+int heom_model_cf_pattern(heom_model *m, int32_t iorbs, int32_t ispin, heom_cf_tables *out) {
+    return heom::guarded([&] {
+        if (!m || !out) heom::fail(HEOM_E_ARG, "null argument");
+        if (iorbs < 1 || iorbs > m->norbs || ispin < 1 || ispin > m->nspin) heom::fail(HEOM_E_ARG, "invalid spin-orbital");
+        if (m->cf_iorbs != iorbs || m->cf_ispin != ispin) build_cf_pattern(*m, iorbs, ispin);
+        *out = heom_cf_tables{};
+        out->iorbs = iorbs; out->ispin = ispin;
+        out->lunkcf_spa = m->cf_lunk;
+        out->nnzcf_spa = m->cf_nnz.data(); out->indcf_spa = m->cf_ind.data();
+        out->irowcf_spa = m->cf_irow.data(); out->icolcf_spa = m->cf_icol.data();
+    });
+}
 
 const heom_tables *heom_model_tables(const heom_model *m) { return m ? &m->view : nullptr; }
 

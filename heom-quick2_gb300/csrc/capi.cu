@@ -340,6 +340,13 @@ double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b)
     return device_dot(n, a, b, c->dscratch, c->stream);
 }
 
+void run_tfqmr64(heom_ctx *c, TfqWork<double> &W, const ApplyFn<double> &apply, int nlim, int &iters, int64_t &launches)
+{
+    tfq_run<double>(c, W, apply, nlim, iters, launches);
+}
+
+void drandn_host(int64_t n, std::vector<double> &out) { drandn_stream(n, out); }
+
 void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, double2 *x, double crit_abs, int maxit0,
                     heom_solve_info &info)
 {

@@ -55,6 +55,11 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
 // Values of a full nrho x nrho matrix on the context's H structure (FP64).
 void hvalues64(heom_ctx *c, const cd *hs, std::vector<double2> &h64);
 double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b);
+// Batched FP64 TFQMR iterations until every instance of W has finished (graph-captured
+// chunks on the context's stream); iters: iterations launched.
+void run_tfqmr64(heom_ctx *c, TfqWork<double> &W, const ApplyFn<double> &apply, int nlim, int &iters, int64_t &launches);
+// The reference's shadow-vector stream (tfqmr_double/drandn.f90, SEED = 1): n reals.
+void drandn_host(int64_t n, std::vector<double> &out);
 }  // namespace heom
 
 struct heom_ctx {

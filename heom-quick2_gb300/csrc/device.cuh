@@ -46,6 +46,9 @@ struct DevCoef {
     int32_t nz0 = 0, ndiag = 0;
     const int32_t *rdo_pair = nullptr;   // index of the transposed RDO entry
     double reg_scale = 0;
+    // correlation-function operator: entries [h; a] of cf_half each, signed frequency per instance
+    const double *cf_omega = nullptr;
+    int64_t cf_half = 0;
 };
 
 // y = A x (ADJ = false) or y = A^H x (ADJ = true) for nbatch instances (gridDim.y);

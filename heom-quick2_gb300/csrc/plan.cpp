@@ -445,4 +445,71 @@ void gamma_derivative_coefs(const heom_tables &, const HostPlan &F, double gamma
         if (F.coef_kind[k] == 1) { cl[k] = F.cl[k] / gamma; cr[k] = F.cr[k] / gamma; }
 }
 
+// Plan of the correlation-function operator (corrfunc/calc_ax_cf_spa_omp.f90) on the
+// entries [h (lunkcf); a (lunkcf)].  Each component has the steady operator's same-tier
+// terms on the cf pattern; every coupling crosses the components: the h rows gather from
+// a with the coefficients (cL zfront, cR zrear), zfront = -i, zrear = +i, and the a rows
+// gather from h with the negated pair (calc_ax_cf_spa_omp.f90:344-416, 467-510).  The RDO
+// rows' Hermitian-conjugate pushes (c2 + c2^dag for h, c1 + c1^dag for a, lines 161-235)
+// transform the same way, because the conjugate of zrear is zfront.  A unit pair
+// (i sL, i sR) becomes the real pair (sL, -sR) in h rows and (-sL, sR) in a rows: the
+// kernel adds the unit gathers without the factor i when it runs the cf operator.  The
+// +-omega terms between h and a are added by the kernel from the per-instance frequency.
+void build_cf_plan(const heom_tables &t, const heom_cf_tables &cf, const HStructure &hst, HostPlan &out) {
+    if (cf.lunkcf_spa < 1 || !cf.nnzcf_spa || !cf.indcf_spa || !cf.irowcf_spa || !cf.icolcf_spa)
+        fail(HEOM_E_ARG, "empty correlation-function pattern");
+    if (cf.nnzcf_spa[0] < 1) fail(HEOM_E_ARG, "correlation-function pattern without RDO entries");
+    if (2 * cf.lunkcf_spa >= (int64_t)1 << 31) fail(HEOM_E_UNSUPPORTED, "more than 2^30 correlation-function entries");
+    heom_tables tc = t;
+    tc.lunk_spa = cf.lunkcf_spa;
+    tc.nnz_spa = cf.nnzcf_spa; tc.ind_spa = cf.indcf_spa;
+    tc.irow_spa = cf.irowcf_spa; tc.icol_spa = cf.icolcf_spa;
+    HostPlan P;
+    build_forward_plan(tc, hst, P);
+    const int64_t L = P.lunk;
+    const int32_t na = P.nado, ncoef = (int32_t)P.cl.size(), ncp = (int32_t)P.coup.size();
+    out = HostPlan();
+    out.lunk = 2 * L; out.nado = 2 * na; out.nslots = P.nslots; out.nh = P.nh;
+    out.ent_ado.resize(2 * L);
+    for (int64_t e = 0; e < L; e++) { out.ent_ado[e] = P.ent_ado[e]; out.ent_ado[L + e] = P.ent_ado[e] + na; }
+    out.ado_off.resize(2 * (size_t)na + 1);
+    for (int32_t a = 0; a < na; a++) { out.ado_off[a] = P.ado_off[a]; out.ado_off[na + a] = (int32_t)(L + P.ado_off[a]); }
+    out.ado_off[2 * na] = (int32_t)(2 * L);
+    for (int h = 0; h < 2; h++) {
+        out.ado_cls.insert(out.ado_cls.end(), P.ado_cls.begin(), P.ado_cls.end());
+        out.ado_cnt.insert(out.ado_cnt.end(), P.ado_cnt.begin(), P.ado_cnt.end());
+        out.g0.insert(out.g0.end(), P.g0.begin(), P.g0.end());
+    }
+    out.cls_tptr = P.cls_tptr; out.term_ptr = P.term_ptr; out.terms = P.terms; out.maps = P.maps;
+    const cd zf(0, -1), zr(0, 1);
+    out.cl.resize(2 * (size_t)ncoef); out.cr.resize(2 * (size_t)ncoef); out.coef_kind.resize(2 * (size_t)ncoef);
+    for (int32_t k = 0; k < ncoef; k++) {
+        out.cl[k] = P.cl[k] * zf; out.cr[k] = P.cr[k] * zr;
+        out.cl[ncoef + k] = -out.cl[k]; out.cr[ncoef + k] = -out.cr[k];
+        out.coef_kind[k] = out.coef_kind[ncoef + k] = P.coef_kind[k];
+    }
+    out.coup.resize(2 * (size_t)ncp);
+    out.coup_ptr.resize(2 * (size_t)na + 1);
+    out.coup_mid.resize(2 * (size_t)na);
+    for (int h = 0; h < 2; h++) {
+        for (int32_t k = 0; k < ncp; k++) {
+            CoupRec r = P.coup[k];
+            const int32_t conj = r.cid & kCoefConj, id = r.cid & ~kCoefConj;
+            if (h == 0) r.src_off = (int32_t)(r.src_off + L);     // h rows read a
+            int32_t nid;
+            if (id & kCoefUnit) nid = id ^ (h == 0 ? 2 : 1);       // (sL, -sR) / (-sL, sR)
+            else nid = id + (h == 0 ? 0 : ncoef);
+            r.cid = nid | conj;
+            out.coup[(size_t)h * ncp + k] = r;
+        }
+        for (int32_t a = 0; a < na; a++) {
+            out.coup_ptr[(size_t)h * na + a] = P.coup_ptr[a] + h * ncp;
+            out.coup_mid[(size_t)h * na + a] = P.coup_mid[a] + h * ncp;
+        }
+    }
+    out.coup_ptr[2 * (size_t)na] = 2 * ncp;
+    out.n_terms_same = 2 * P.n_terms_same; out.n_couplings = 2 * P.n_couplings; out.n_maps = P.n_maps;
+    out.n_classes = P.n_classes; out.gather_hits = 2 * P.gather_hits;
+}
+
 }  // namespace heom

@@ -65,6 +65,9 @@ void build_adjoint_plan(const heom_tables &t, const HostPlan &fwd, HostPlan &out
 // Order every ADO's couplings as coefficient pairs first, then unit pairs (stable, so each
 // kind keeps its order), and record the boundary in coup_mid.
 void split_couplings(HostPlan &P);
+// Plan of the correlation-function operator on the pattern cf: entries [h; a], no trace slot
+// (corrfunc/calc_ax_cf_spa_omp.f90)
+void build_cf_plan(const heom_tables &t, const heom_cf_tables &cf, const HStructure &hst, HostPlan &out);
 // derivative coefficient table of the forward plan w.r.t. a common linewidth scale:
 // lower-tier pairs divided by gamma, everything else zero
 void gamma_derivative_coefs(const heom_tables &t, const HostPlan &fwd, double gamma, std::vector<cd> &cl, std::vector<cd> &cr);

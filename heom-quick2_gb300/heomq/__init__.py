@@ -79,6 +79,11 @@ class SolveInfo(C.Structure):
                 ("resid", C.c_double), ("seconds", C.c_double), ("launches", C.c_int64)]
 
 
+class CfTables(C.Structure):
+    _fields_ = [("iorbs", C.c_int32), ("ispin", C.c_int32), ("lunkcf_spa", C.c_int64), ("nnzcf_spa", C.c_void_p),
+                ("indcf_spa", C.c_void_p), ("irowcf_spa", C.c_void_p), ("icolcf_spa", C.c_void_p)]
+
+
 class GradOpts(C.Structure):
     _fields_ = [("deshift", C.c_void_p), ("gamma", C.c_double), ("dhs_du", C.c_void_p), ("dhs_deps", C.c_void_p),
                 ("crit", C.c_double), ("maxit0", C.c_int32)]
@@ -117,6 +122,15 @@ SIGNATURES = {
     "heom_batch_solve_dev": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_batch_destroy": (None, [C.c_void_p]),
     "heom_batch_current_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
+    "heom_model_cf_pattern": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _p(CfTables)]),
+    "heom_cf_create": (C.c_int, [C.c_void_p, _p(Tables), _p(CfTables), _p(C.c_void_p)]),
+    "heom_cf_destroy": (None, [C.c_void_p]),
+    "heom_cf_lunk": (C.c_int64, [C.c_void_p]),
+    "heom_cf_calc_ax": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_int64] + [C.c_void_p] * 4),
+    "heom_cf_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, _p(SolveOpts),
+                                C.c_void_p, C.c_void_p, _p(SolveInfo)]),
+    "heom_cf_dos": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, _p(SolveOpts), C.c_void_p,
+                              _p(SolveInfo)]),
 }
 
 _lib = None
@@ -230,6 +244,20 @@ class Model:
         r = np.zeros(self.lunk, dtype=np.complex128)
         _check(lib().heom_model_initial_guess(self.h, r.ctypes.data))
         return r
+
+    def cf_pattern(self, iorbs=1, ispin=1):
+        """Correlation-function pattern of a_{iorbs,ispin} (prelude_cf_spa) as numpy arrays."""
+        t = CfTables()
+        _check(lib().heom_model_cf_pattern(self.h, iorbs, ispin, C.byref(t)))
+
+        def arr(ptr, cnt, dt):
+            buf = (C.c_char * (cnt * np.dtype(dt).itemsize)).from_address(ptr)
+            return np.frombuffer(bytes(buf), dtype=dt).copy()
+
+        L = t.lunkcf_spa
+        return {"iorbs": iorbs, "ispin": ispin, "lunkcf_spa": L,
+                "nnzcf_spa": arr(t.nnzcf_spa, self.nunk, np.int32), "indcf_spa": arr(t.indcf_spa, self.nunk, np.int64),
+                "irowcf_spa": arr(t.irowcf_spa, L, np.int32), "icolcf_spa": arr(t.icolcf_spa, L, np.int32)}
 
     def field(self):
         a = np.zeros(self.nalf * self.nspin)
@@ -385,6 +413,73 @@ class Context:
         _check(lib().heom_ctx_stats(self.h, out.ctypes.data))
         keys = ("entries", "ados", "classes", "couplings", "maps", "gathers", "same_tier_terms", "lower_gathers", "plan_bytes")
         return dict(zip(keys, out.tolist()))
+
+
+class CorrFunc:
+    """Frequency-domain correlation functions of B = a_{iorbs,ispin} (corrfunc/): the operator
+    calc_ax_cf_spa_omp, the solve solve_cf_tfqmr_spa batched over frequencies, and the
+    spectral function of corrfunc.f90.  pattern: dict of nnzcf_spa, indcf_spa, irowcf_spa,
+    icolcf_spa (1-based, as prelude_cf_spa makes them); default: the model's own."""
+
+    def __init__(self, ctx, iorbs=1, ispin=1, pattern=None):
+        self.ctx = ctx
+        pat = pattern if pattern is not None else ctx.model.cf_pattern(iorbs, ispin)
+        self.pattern = {
+            "nnzcf_spa": np.ascontiguousarray(pat["nnzcf_spa"], dtype=np.int32),
+            "indcf_spa": np.ascontiguousarray(pat["indcf_spa"], dtype=np.int64),
+            "irowcf_spa": np.ascontiguousarray(pat["irowcf_spa"], dtype=np.int32),
+            "icolcf_spa": np.ascontiguousarray(pat["icolcf_spa"], dtype=np.int32),
+        }
+        t = CfTables(iorbs=iorbs, ispin=ispin, lunkcf_spa=int(self.pattern["irowcf_spa"].size))
+        for k, v in self.pattern.items():
+            setattr(t, k, v.ctypes.data)
+        h = C.c_void_p()
+        _check(lib().heom_cf_create(ctx.h, C.byref(ctx.model.tables), C.byref(t), C.byref(h)))
+        self.h = h
+        self.iorbs, self.ispin = iorbs, ispin
+        self.lunkcf = int(lib().heom_cf_lunk(h))
+        self.nrho = ctx.model.nrho
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.heom_cf_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def calc_ax_cf_spa(self, dfreq, isgnw, rcga, rcgb):
+        """(rhsa, rhsb) = L_cf (rcga, rcgb); dfreq in energy / hbar."""
+        xa, xb = _c128(rcga, self.lunkcf), _c128(rcgb, self.lunkcf)
+        ya = np.zeros(self.lunkcf, dtype=np.complex128)
+        yb = np.zeros(self.lunkcf, dtype=np.complex128)
+        _check(lib().heom_cf_calc_ax(self.h, float(dfreq), int(isgnw), self.lunkcf, xa.ctypes.data, xb.ctypes.data,
+                                     ya.ctypes.data, yb.ctypes.data))
+        return ya, yb
+
+    def solve_cf_tfqmr_spa(self, rho, isgnb, isgnw, dfreq, crit=1e-10, maxit0=20000):
+        """RDO blocks (zouth, zouta), each (nfreq, nrho, nrho), of the solves at every dfreq."""
+        w = np.ascontiguousarray(np.atleast_1d(dfreq), dtype=np.float64)
+        rho = _c128(rho, self.ctx.lunk)
+        n = self.nrho
+        zh = np.zeros(w.size * n * n, dtype=np.complex128)
+        za = np.zeros(w.size * n * n, dtype=np.complex128)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=PREC_FP64)
+        info = SolveInfo()
+        _check(lib().heom_cf_solve(self.h, rho.ctypes.data, int(isgnb), int(isgnw), w.size, w.ctypes.data, C.byref(o),
+                                   zh.ctypes.data, za.ctypes.data, C.byref(info)))
+        # column-major nrho x nrho blocks
+        return zh.reshape(w.size, n, n).transpose(0, 2, 1), za.reshape(w.size, n, n).transpose(0, 2, 1), info
+
+    def dos(self, rho, freq_ev, crit=1e-10, maxit0=20000):
+        """Columns A(w), occupied part, empty part, Re G^r, Im G^r at every frequency (eV)."""
+        f = np.ascontiguousarray(np.atleast_1d(freq_ev), dtype=np.float64)
+        rho = _c128(rho, self.ctx.lunk)
+        out = np.zeros(5 * f.size)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=PREC_FP64)
+        info = SolveInfo()
+        _check(lib().heom_cf_dos(self.h, rho.ctypes.data, f.size, f.ctypes.data, C.byref(o), out.ctypes.data,
+                                 C.byref(info)))
+        return out.reshape(f.size, 5), info
 
 
 class Batch:

@@ -254,6 +254,61 @@ int heom_bench_apply(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t r
  * precision). */
 int heom_bench_inner(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
 
+/* ------------------------------------------------------------------------- */
+/* Correlation functions and spectral functions in the frequency domain (corrfunc/).
+ * For B = a_{iorbs,ispin} the unknown holds two components h and a (the reference's
+ * rcga, rcgb), each on the correlation-function pattern below; vectors of the device
+ * solves are laid out [h (lunkcf); a (lunkcf)], the order of the reference's qmrvecs_cf. */
+typedef struct {
+    int32_t iorbs, ispin;                 /* B = a_{iorbs,ispin} (iorbs_dos, ispin_dos) */
+    int64_t lunkcf_spa;
+    const int32_t *nnzcf_spa;             /* nunk */
+    const int64_t *indcf_spa;             /* nunk, 1-based */
+    const int32_t *irowcf_spa, *icolcf_spa;   /* lunkcf_spa, 1-based */
+} heom_cf_tables;
+
+/* The pattern of prelude_cf_spa (corrfunc/prelude_cf_spa.f90:146-760): the tier rule of
+ * prelude_spa seeded with the RDO structure of exp(0.314 H) (a + a^dag) exp(0.314 H).
+ * The arrays belong to the model (valid while it lives; a later call for another
+ * spin-orbital replaces them). */
+int heom_model_cf_pattern(heom_model *m, int32_t iorbs, int32_t ispin, heom_cf_tables *out);
+
+typedef struct heom_cf heom_cf;
+/* Device plan of the correlation-function operator on the pattern `cf` (the caller's
+ * nnzcf_spa etc., e.g. from the Fortran prelude_cf_spa, or heom_model_cf_pattern).
+ * t: the same tables the context was created from.  The arrays are read here only. */
+int  heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf, heom_cf **out);
+void heom_cf_destroy(heom_cf *cf);
+int64_t heom_cf_lunk(const heom_cf *cf);
+
+/* (rhsa, rhsb) = L_cf (rcga, rcgb)  (calc_ax_cf_spa_omp, corrfunc/calc_ax_cf_spa_omp.f90:1)
+ * at frequency dfreq (internal units, energy / hbar) with the sign of the reference's
+ * lplus_cf: isgnw = 1 (+i omega), 2 (-i omega).  All vectors ldim = lunkcf complex (host). */
+int heom_cf_calc_ax(heom_cf *cf, double dfreq, int32_t isgnw, int64_t ldim, const double _Complex *rcga,
+                    const double _Complex *rcgb, double _Complex *rhsa, double _Complex *rhsb);
+
+/* solve_cf_tfqmr_spa (corrfunc/solve_cf_tfqmr_spa.f90:1) for nfreq frequencies at once:
+ * L_cf(dfreq_k, isgnw) x_k = -(B rho) with brhoh = op(a) rho + rho op'(a),
+ * brhoa = -i op(a) rho + i rho op'(a) (isgnb = 1: op = a^dag, op' = a; isgnb = 2: the
+ * reverse).  rho: steady state (lunk_spa complex, host).  Each solve starts from x = 0,
+ * runs TFQMR with tolerance 1e-3 crit and stops at ||b - L x|| <= crit (o->crit,
+ * o->maxit0; FP64 only).  zouth, zouta: nfreq dense nrho x nrho RDO blocks (column-major)
+ * of the two components, as the reference returns them; either may be NULL. */
+int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_t isgnw, int32_t nfreq,
+                  const double *dfreq, const heom_solve_opts *o, double _Complex *zouth, double _Complex *zouta,
+                  heom_solve_info *info);
+
+/* The frequency-domain spectral function of corrfunc (corrfunc/corrfunc.f90:146-217,
+ * lfreq_dos with ljw_dos): for every frequency freq_ev[k] (eV) the two solves
+ * (isgnb, isgnw) = (2, 2) and (1, 1), batched together, and
+ *   out[5k+0] = A(w) = out[5k+1] + out[5k+2]                     (1/eV)
+ *   out[5k+1] = Re Tr[a^dag X_22] / pi / hbar  (occupied part, C_{B^dag B})
+ *   out[5k+2] = Re Tr[a X_11] / pi / hbar      (empty part, C_{B B^dag})
+ *   out[5k+3], out[5k+4] = Re, Im G^r(w) = -i (conj Tr[a^dag X_22] + Tr[a X_11]) / hbar
+ * with X = (zouth + i zouta) / 2. */
+int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const double *freq_ev,
+                const heom_solve_opts *o, double *out, heom_solve_info *info);
+
 /* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs
  * with entries, [2] pattern classes, [3] coupling records, [4] gather maps, [5] useful
  * gathers (nonzero map halves), [6] same-tier terms, [7] lower-tier (complex-coefficient)

@@ -151,3 +151,22 @@ def test_stored_sizes_match_an_independent_count(cfg, nunk, lall):
     assert m.nunk == nunk
     if lall is not None:
         assert m.lall == lall
+
+
+@pytest.mark.parametrize("spin", [1, 2])
+def test_correlation_function_pattern_bit_exact(pair, spin):
+    """corrfunc/prelude_cf_spa.f90:146-760: the library's structural propagation from the
+    seed E0 (a + a^dag) E0 against the oracle's random-coefficient products."""
+    p, o = pair
+    for iorbs in range(1, p.norbs + 1):
+        a = p.cf_pattern(iorbs, spin)
+        c = of.CF(o, iorbs, spin)
+        assert a["lunkcf_spa"] == c.lunkcf
+        for k in ("nnzcf_spa", "indcf_spa", "irowcf_spa", "icolcf_spa"):
+            np.testing.assert_array_equal(a[k].astype(np.int64), c.get(k).astype(np.int64))
+
+
+def test_correlation_function_pattern_rejects_a_bad_spin_orbital(pair):
+    p, _ = pair
+    with pytest.raises(heomq.HeomError):
+        p.cf_pattern(p.norbs + 1, 1)
