@@ -39,6 +39,11 @@ def parse():
                     help="profiler run of the two fused FP32x2 inner-iteration kernels: 3 warm-up + 2 timed launches each")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
+    ap.add_argument("--workload", default="steady", choices=["steady", "dos"],
+                    help="steady: batched steady states (the headline); dos: spectral function over frequencies")
+    ap.add_argument("--freqs", type=int, default=8, help="dos: frequencies per step")
+    ap.add_argument("--profile-cf", action="store_true",
+                    help="dos: profiler run of the correlation-function apply alone: 3 warm-up + 2 timed launches")
     return ap.parse_args()
 
 
@@ -344,10 +349,161 @@ def run_gb300(args, ws, rank, local, dist):
     return 0
 
 
+DOS_METRIC = "HEOM spectral-function frequencies/s (corrfunc frequency domain, FP64)"
+DOS_WORKLOAD = ("spectral function A(w) of a_(1,up) of the serial double quantum dot nd=16, tier L=4 "
+                "(correlation-function pattern: 670672 entries per component), steady state at V=0.8, "
+                "two FP64 TFQMR solves per frequency to ||b - L x|| <= crit")
+DOS_CRIT = 1e-8
+
+
+def dos_freqs(n):
+    import numpy as np
+
+    return np.linspace(-3.0, 3.0, n)
+
+
+def cpu_dos_sample(nthreads, applies_per_freq, napply=40):
+    """The oracle's C restatement of calc_ax_cf_spa_omp on the host cores: `napply` applies
+    timed, scaled to one frequency by the applies the same TFQMR takes per frequency."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_ffi
+    import heomq.models as models
+
+    m = oracle_ffi.Model(models.dqd(ntier=5, nmats=3, V=0.8))
+    c = oracle_ffi.CF(m, 1, 1)
+    rng = np.random.default_rng(1)
+    xh = rng.standard_normal(c.lunkcf) + 1j * rng.standard_normal(c.lunkcf)
+    xa = rng.standard_normal(c.lunkcf) + 1j * rng.standard_normal(c.lunkcf)
+    c.apply(0.3, 1, xh, xa, nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(napply):
+        xh, xa = c.apply(0.3, 1, xh * 1e-3, xa * 1e-3, nthreads=nthreads)
+    t_apply = (time.perf_counter() - t0) / napply
+    return t_apply, 1.0 / (t_apply * applies_per_freq)
+
+
+def run_dos_reference(args, ws, rank, dist):
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    # applies per frequency of the FP64 TFQMR at this criterion (two solves of at most 750
+    # applies each), the count the GPU path measured for the same algorithm on this workload
+    applies = 2 * 750
+    for _ in range(args.warmup):
+        cpu_dos_sample(nthreads, applies, napply=2)
+    vals, per = [], []
+    for _ in range(args.steps):
+        t_apply, v = cpu_dos_sample(nthreads, applies, napply=10)
+        vals.append(v)
+        per.append(t_apply)
+    value = statistics.median(vals)
+    line = {
+        "metric": DOS_METRIC, "value": value, "unit": "freqs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": DOS_WORKLOAD, "crit": DOS_CRIT, "apply_s": statistics.median(per),
+                   "applies_per_frequency": applies},
+        "cpu_baseline": {"value": value, "unit": "freqs/s", "cores": nthreads, "kind": "port",
+                         "sample": "10 applies of the C restatement of calc_ax_cf_spa_omp (OpenMP over ADOs) per step, "
+                                   f"scaled by {applies} applies per frequency"},
+        "e2e": {"value": value, "unit": "freqs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_dos(args, ws, rank, local, dist):
+    import numpy as np
+    import torch
+
+    import heomq
+
+    dev = local
+    torch.cuda.set_device(dev)
+    model = heomq.Model(heomq.models.dqd(ntier=5, nmats=3, V=0.8))
+    ctx = heomq.Context(model, device=dev, adjoint=False)
+    cf = heomq.CorrFunc(ctx, 1, 1)
+    nf = args.freqs
+    freqs = dos_freqs(nf * ws)[rank * nf:(rank + 1) * nf]
+    if args.profile_cf:
+        sec, alg = cf.bench_apply(nbatch=2 * nf, reps=2)
+        print(json.dumps({"profile_cf": True, "instances": 2 * nf, "apply_us": sec * 1e6, "alg_bytes": alg}), flush=True)
+        return 0
+    rho, sinfo = ctx.solve_tfqmr(crit=1e-10, precision=heomq.PREC_MIXED)
+    for _ in range(args.warmup):
+        cf.dos(rho, freqs, crit=DOS_CRIT)
+    clk = clocks_start() if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    dev_s, wall_s, launches, infos = 0.0, [], 0, []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out, info = cf.dos(rho, freqs, crit=DOS_CRIT)
+        wall_s.append(time.perf_counter() - t0)
+        dev_s += info.seconds
+        launches += info.launches
+        infos.append(info)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = clocks_stop(clk, dev) if rank == 0 else None
+    t_step = max_over_ranks(dev_s / args.steps, dist, device="cuda")
+    value = ws * nf / t_step
+    e2e_value = ws * nf / max_over_ranks(statistics.median(wall_s), dist, device="cuda")
+    sec, alg = cf.bench_apply(nbatch=2 * nf, reps=10)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg / sec / 1e9
+    prof = "apply_cf_fp64_dqd_L4_16inst.md"
+    traffic = profile_traffic(prof)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        applies = 2 * infos[-1].iters
+        t_apply, v = cpu_dos_sample(nthreads, applies, napply=20)
+        cpu = {"value": v, "unit": "freqs/s", "cores": nthreads, "kind": "port",
+               "sample": f"20 applies of the C restatement of calc_ax_cf_spa_omp (OpenMP over ADOs, {t_apply * 1e3:.1f} ms "
+                         f"each), scaled by the {applies} applies per frequency the same FP64 TFQMR took on the GPU "
+                         "(batch maximum per solve)"}
+    if rank == 0:
+        n = model.nrho
+        line = {
+            "metric": DOS_METRIC, "value": value, "unit": "freqs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": DOS_WORKLOAD, "freqs_per_step": nf, "freq_range_eV": [-3.0, 3.0], "crit": DOS_CRIT,
+                       "solves_per_step": 2 * nf, "applies_per_solve_max": infos[-1].iters,
+                       "resid_max": infos[-1].resid, "converged": bool(infos[-1].converged),
+                       "l2": f"inputs larger than L2: {2 * nf} instances x 12 vectors x {2 * cf.lunkcf * 16 / 1e6:.1f} MB",
+                       "parallelism": f"frequencies split over {ws} replicas",
+                       "spectrum_min": float(out[:, 1:3].min()), "steady_resid": sinfo.resid},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": f"k_apply_cf<FP64> over {2 * nf} instances", "kernel_us": sec * 1e6,
+                         "alg_bytes_per_launch": alg,
+                         "note": "FP64-pipe bound like the steady FP64 apply (GB300 FP64 = 1/64 of FP32): profiles/" + prof},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "freqs/s", "h2d_bytes_per_step": model.lunk * 16 + nf * 8,
+                    "d2h_bytes_per_step": nf * 5 * 8},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    cf.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     ws, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
+        if args.workload == "dos":
+            return run_dos_reference(args, ws, rank, dist)
         return run_reference(args, ws, rank, dist)
     sys.path.insert(0, ROOT)
     import __graft_entry__
@@ -356,6 +512,8 @@ def main():
         __graft_entry__.build()
     if dist:
         dist.barrier()
+    if args.workload == "dos":
+        return run_dos(args, ws, rank, local, dist)
     return run_gb300(args, ws, rank, local, dist)
 
 

@@ -1115,12 +1115,7 @@ int heom_ctx_stats(const heom_ctx *c, double *out)
         out[5] = P.gather_hits;
         out[6] = (double)P.n_terms_same;
         out[7] = lower;
-        // plan bytes read per apply: coupling records (16 B) + one map word per record and
-        // output entry (4 B) + per-entry ADO index (4 B) + per-ADO arrays (g0 16 B + 4 ints)
-        double mapwords = 0;
-        for (int32_t a = 0; a < P.nado; a++)
-            mapwords += (double)(P.coup_ptr[a + 1] - P.coup_ptr[a]) * (P.ado_off[a + 1] - P.ado_off[a]);
-        out[8] = (double)P.n_couplings * 16.0 + mapwords * 4.0 + (double)P.lunk * 4.0 + (double)P.nado * 32.0;
+        out[8] = plan_read_bytes(P);
     });
 }
 

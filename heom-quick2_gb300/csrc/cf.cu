@@ -493,4 +493,61 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
     });
 }
 
+int heom_cf_bench_apply(heom_cf *cf, int32_t nbatch, int32_t reps, double *seconds, double *bytes)
+{
+    return guarded([&] {
+        require_cf(cf);
+        if (nbatch < 1 || reps < 1) fail(HEOM_E_ARG, "nbatch and reps must be positive");
+        heom_ctx *c = cf->ctx;
+        const int64_t N = 2 * cf->lunkcf + 1, vs = (N + 63) / 64 * 64;
+        std::vector<void *> tmp;
+        auto cleanup = [&] { for (void *p : tmp) cudaFree(p); tmp.clear(); };
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        try {
+            ensure_omega(cf, nbatch);
+            std::vector<double> w(nbatch);
+            for (int b = 0; b < nbatch; b++) w[b] = (b % 2 ? 1.0 : -1.0) * (0.1 + 0.01 * b) / kHbar;
+            CK(cudaMemcpyAsync(cf->d_omega, w.data(), sizeof(double) * nbatch, cudaMemcpyHostToDevice, c->stream));
+            double2 *x = nullptr, *y = nullptr, *hv = nullptr, *gd = nullptr;
+            double *es = nullptr;
+            CK(cudaMalloc((void **)&x, sizeof(double2) * (size_t)vs * nbatch)); tmp.push_back(x);
+            CK(cudaMalloc((void **)&y, sizeof(double2) * (size_t)vs * nbatch)); tmp.push_back(y);
+            const DevPlan P = cf->dplan.view;
+            CK(cudaMalloc((void **)&hv, sizeof(double2) * (size_t)std::max(1, P.nh) * nbatch)); tmp.push_back(hv);
+            CK(cudaMalloc((void **)&es, sizeof(double) * 4 * (size_t)nbatch)); tmp.push_back(es);
+            CK(cudaMalloc((void **)&gd, sizeof(double2) * (size_t)P.nado * nbatch)); tmp.push_back(gd);
+            // x = 1e-3 (1 + i) everywhere: the timing does not depend on the values
+            std::vector<double2> ones((size_t)vs, make_double2(1e-3, 1e-3));
+            for (int b = 0; b < nbatch; b++) {
+                CK(cudaMemcpyAsync(x + (size_t)b * vs, ones.data(), sizeof(double2) * vs, cudaMemcpyHostToDevice, c->stream));
+                CK(cudaMemcpyAsync(hv + (size_t)b * P.nh, c->hval64, sizeof(double2) * P.nh, cudaMemcpyDeviceToDevice, c->stream));
+                CK(cudaMemcpyAsync(es + 4 * (size_t)b, c->es64, sizeof(double) * 4, cudaMemcpyDeviceToDevice, c->stream));
+            }
+            DevCoef<double> K = cf_coef(cf);
+            K.hval = hv;
+            K.eshift = es;
+            fill_gdiag<double>(P, K, gd, nbatch, c->stream);
+            K.gdiag = gd;
+            for (int r = 0; r < 3; r++) launch_apply_cf(P, K, x, y, nbatch, vs, nullptr, c->stream);
+            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+            CK(cudaEventRecord(e0, c->stream));
+            for (int r = 0; r < reps; r++) launch_apply_cf(P, K, r % 2 ? y : x, r % 2 ? x : y, nbatch, vs, nullptr, c->stream);
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaGetLastError());
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (seconds) *seconds = ms * 1e-3 / reps;
+            if (bytes) *bytes = nbatch * 2.0 * (double)N * sizeof(double2) + plan_read_bytes(cf->plan);
+        } catch (...) {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            cleanup();
+            throw;
+        }
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        cleanup();
+    });
+}
+
 }  // extern "C"

@@ -438,6 +438,13 @@ void split_couplings(HostPlan &P)
     }
 }
 
+double plan_read_bytes(const HostPlan &P) {
+    double mapwords = 0;
+    for (int32_t a = 0; a < P.nado; a++)
+        mapwords += (double)(P.coup_ptr[a + 1] - P.coup_ptr[a]) * (P.ado_off[a + 1] - P.ado_off[a]);
+    return (double)P.coup.size() * 16.0 + mapwords * 4.0 + (double)P.lunk * 4.0 + (double)P.nado * 32.0;
+}
+
 void gamma_derivative_coefs(const heom_tables &, const HostPlan &F, double gamma, std::vector<cd> &cl, std::vector<cd> &cr) {
     cl.assign(F.cl.size(), 0.0);
     cr.assign(F.cr.size(), 0.0);

@@ -68,6 +68,9 @@ void split_couplings(HostPlan &P);
 // Plan of the correlation-function operator on the pattern cf: entries [h; a], no trace slot
 // (corrfunc/calc_ax_cf_spa_omp.f90)
 void build_cf_plan(const heom_tables &t, const heom_cf_tables &cf, const HStructure &hst, HostPlan &out);
+// plan bytes one apply reads: coupling records (16 B), one map word per record and output
+// entry (4 B), the per-entry ADO index (4 B) and the per-ADO arrays (g0 16 B + 4 ints)
+double plan_read_bytes(const HostPlan &P);
 // derivative coefficient table of the forward plan w.r.t. a common linewidth scale:
 // lower-tier pairs divided by gamma, everything else zero
 void gamma_derivative_coefs(const heom_tables &t, const HostPlan &fwd, double gamma, std::vector<cd> &cl, std::vector<cd> &cr);

@@ -129,6 +129,7 @@ SIGNATURES = {
     "heom_cf_calc_ax": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_int64] + [C.c_void_p] * 4),
     "heom_cf_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, _p(SolveOpts),
                                 C.c_void_p, C.c_void_p, _p(SolveInfo)]),
+    "heom_cf_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_cf_dos": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, _p(SolveOpts), C.c_void_p,
                               _p(SolveInfo)]),
 }
@@ -480,6 +481,13 @@ class CorrFunc:
         _check(lib().heom_cf_dos(self.h, rho.ctypes.data, f.size, f.ctypes.data, C.byref(o), out.ctypes.data,
                                  C.byref(info)))
         return out.reshape(f.size, 5), info
+
+    def bench_apply(self, nbatch=1, reps=20):
+        """(seconds per launch, algorithmic bytes per launch) of the FP64 cf apply."""
+        s = C.c_double()
+        b = C.c_double()
+        _check(lib().heom_cf_bench_apply(self.h, nbatch, reps, C.byref(s), C.byref(b)))
+        return s.value, b.value
 
 
 class Batch:

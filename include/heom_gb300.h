@@ -309,6 +309,11 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
 int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const double *freq_ev,
                 const heom_solve_opts *o, double *out, heom_solve_info *info);
 
+/* Measurement hook: average time of `reps` back-to-back FP64 correlation-function applies on
+ * `nbatch` instances (frequencies) and the algorithmic bytes of one launch (each instance's
+ * vector read once and written once, plus the plan).  No reference counterpart. */
+int heom_cf_bench_apply(heom_cf *cf, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
+
 /* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs
  * with entries, [2] pattern classes, [3] coupling records, [4] gather maps, [5] useful
  * gathers (nonzero map halves), [6] same-tier terms, [7] lower-tier (complex-coefficient)

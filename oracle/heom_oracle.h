@@ -151,7 +151,10 @@ int  orc_cf_build(const orc_model *m, int iorbs, int ispin, unsigned long long s
 void orc_cf_free(orc_cf *cf);
 /* (yh, ya) = L_cf(omega, isgnw) (xh, xa) */
 void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw, const ozc *xh, const ozc *xa,
-                  ozc *yh, ozc *ya);
+                  ozc *yh, ozc *ya, int nthreads);
+/* the reference's TFQMR solve of L_cf x = -(B rho) from x = 0 (solve_cf_tfqmr_spa.f90) */
+int orc_cf_solve(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, int isgnw, double omega, double crit,
+                 int maxit0, ozc *xh, ozc *xa, orc_solve_info *info, int nthreads);
 /* brhoh, brhoa from the steady rho (lunk entries); isgnb 1: a^dag rho + rho a, 2: a rho + rho a^dag */
 void orc_cf_rhs(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, ozc *bh, ozc *ba);
 int64_t orc_cf_info(const orc_cf *cf, const char *key);

@@ -15,6 +15,9 @@
  * of this file.
  */
 #include "oracle_internal.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* dense a_{iorbs,ispin}: a(ra, ca) = sign */
 static void cf_dense_op(const orc_model *m, int iorbs, int ispin, ozc *a)
@@ -159,15 +162,29 @@ static void cf_add_coupling(const orc_model *m, const orc_cf *cf, const int *pos
 }
 
 void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw, const ozc *xh, const ozc *xa,
-                  ozc *yh, ozc *ya)
+                  ozc *yh, ozc *ya, int nthreads)
 {
     int n = m->nrho;
     size_t nn = (size_t)n * n;
     const double sw = isgnw == 1 ? 1.0 : -1.0, fa = -sw, fb = sw;   /* dfacta, dfactb (lplus_cf) */
     const ozc zfront = -I, zrear = I;
     for (int64_t k = 0; k < cf->lunkcf; k++) yh[k] = ya[k] = 0;
-    int *pos = malloc(sizeof(int) * nn);
-    for (size_t k = 0; k < nn; k++) pos[k] = -1;
+    /* nonzeros of H by column and by row */
+    int *hc_ptr = calloc(n + 1, sizeof(int)), *hr_ptr = calloc(n + 1, sizeof(int));
+    int *hc_row = malloc(sizeof(int) * nn), *hr_col = malloc(sizeof(int) * nn);
+    ozc *hc_val = malloc(sizeof(ozc) * nn), *hr_val = malloc(sizeof(ozc) * nn);
+    for (int c = 0; c < n; c++) {
+        hc_ptr[c + 1] = hc_ptr[c];
+        for (int r = 0; r < n; r++) if (cabs(m->hs[r + (size_t)c * n]) >= ORC_DSMALL) {
+            hc_row[hc_ptr[c + 1]] = r; hc_val[hc_ptr[c + 1]] = m->hs[r + (size_t)c * n]; hc_ptr[c + 1]++;
+        }
+    }
+    for (int r = 0; r < n; r++) {
+        hr_ptr[r + 1] = hr_ptr[r];
+        for (int c = 0; c < n; c++) if (cabs(m->hs[r + (size_t)c * n]) >= ORC_DSMALL) {
+            hr_col[hr_ptr[r + 1]] = c; hr_val[hr_ptr[r + 1]] = m->hs[r + (size_t)c * n]; hr_ptr[r + 1]++;
+        }
+    }
     /* ---- RDO (calc_ax_cf_spa_omp.f90 first tier) ---- */
     {
         int nz = cf->nnzcf[0];
@@ -225,8 +242,16 @@ void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw,
         free(x0h); free(x0a); free(c1); free(c2); free(s4); free(s5);
     }
     /* ---- tiers 2..ntier ---- */
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
     for (int itier = 2; itier <= m->ntier; itier++) {
         int nb = itier - 1;
+#pragma omp parallel
+        {
+        int *pos = malloc(sizeof(int) * nn);
+        for (size_t k = 0; k < nn; k++) pos[k] = -1;
+#pragma omp for schedule(dynamic, 16)
         for (int64_t lni = m->nfirst[itier - 1]; lni <= m->nlast[itier - 1]; lni++) {
             int nz = cf->nnzcf[lni - 1];
             if (nz == 0) continue;
@@ -245,17 +270,13 @@ void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw,
                 ozc vh = xh[st + q], va = xa[st + q];
                 yhn[q] += g * vh + fa * omega * va;
                 yan[q] += g * va + fb * omega * vh;
-                for (int k = 0; k < n; k++) {
-                    ozc hv = m->hs[k + (size_t)r * n];   /* H(k, r): (H X)(k, c) */
-                    if (cabs(hv) >= ORC_DSMALL) {
-                        int p = pos[k + (size_t)c * n];
-                        if (p >= 0) { yhn[p] += -I * (hv * vh); yan[p] += -I * (hv * va); }
-                    }
-                    ozc vhk = m->hs[c + (size_t)k * n];  /* H(c, k): (X H)(r, k) */
-                    if (cabs(vhk) >= ORC_DSMALL) {
-                        int p = pos[r + (size_t)k * n];
-                        if (p >= 0) { yhn[p] += I * (vh * vhk); yan[p] += I * (va * vhk); }
-                    }
+                for (int k = hc_ptr[r]; k < hc_ptr[r + 1]; k++) {   /* H(i, r) x -> (i, c) */
+                    int p = pos[hc_row[k] + (size_t)c * n];
+                    if (p >= 0) { yhn[p] += -I * (hc_val[k] * vh); yan[p] += -I * (hc_val[k] * va); }
+                }
+                for (int k = hr_ptr[c]; k < hr_ptr[c + 1]; k++) {   /* x H(c, j) -> (r, j) */
+                    int p = pos[r + (size_t)hr_col[k] * n];
+                    if (p >= 0) { yhn[p] += I * (vh * hr_val[k]); yan[p] += I * (va * hr_val[k]); }
                 }
             }
             int64_t lnl = m->index_coef_ref[lni - 1];
@@ -287,8 +308,10 @@ void orc_cf_apply(const orc_model *m, const orc_cf *cf, double omega, int isgnw,
             }
             for (int q = 0; q < nz; q++) pos[(ir[q] - 1) + (ic[q] - 1) * n] = -1;
         }
+        free(pos);
+        }
     }
-    free(pos);
+    free(hc_ptr); free(hr_ptr); free(hc_row); free(hr_col); free(hc_val); free(hr_val);
 }
 
 void orc_cf_rhs(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, ozc *bh, ozc *ba)

@@ -69,7 +69,9 @@ def lib():
         L.orc_besselj_ext.argtypes = [C.c_int, C.c_double]
         L.orc_cf_build.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]
         L.orc_cf_free.argtypes = [C.c_void_p]
-        L.orc_cf_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int] + [C.c_void_p] * 4
+        L.orc_cf_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int] + [C.c_void_p] * 4 + [C.c_int]
+        L.orc_cf_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                   C.c_void_p, C.c_void_p, C.POINTER(SolveInfo), C.c_int]
         L.orc_cf_rhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_cf_info.restype = C.c_int64
         L.orc_cf_info.argtypes = [C.c_void_p, C.c_char_p]
@@ -264,15 +266,25 @@ class CF:
             raise KeyError(name)
         return a
 
-    def apply(self, omega, isgnw, xh, xa):
+    def apply(self, omega, isgnw, xh, xa, nthreads=0):
         """(yh, ya) = L_cf (xh, xa); omega in internal units (energy / hbar)."""
         xh = np.ascontiguousarray(xh, dtype=np.complex128)
         xa = np.ascontiguousarray(xa, dtype=np.complex128)
         yh = np.zeros(self.lunkcf, dtype=np.complex128)
         ya = np.zeros(self.lunkcf, dtype=np.complex128)
         lib().orc_cf_apply(self.model.h, self.h, omega, isgnw, xh.ctypes.data, xa.ctypes.data,
-                           yh.ctypes.data, ya.ctypes.data)
+                           yh.ctypes.data, ya.ctypes.data, nthreads)
         return yh, ya
+
+    def tfqmr(self, rho, omega, isgnb, isgnw, crit=1e-10, maxit0=20000, nthreads=0):
+        """The reference algorithm (solve_cf_tfqmr_spa): TFQMR from x = 0 in C."""
+        rho = np.ascontiguousarray(rho, dtype=np.complex128)
+        xh = np.zeros(self.lunkcf, dtype=np.complex128)
+        xa = np.zeros(self.lunkcf, dtype=np.complex128)
+        info = SolveInfo()
+        lib().orc_cf_solve(self.model.h, self.h, rho.ctypes.data, isgnb, isgnw, omega, crit, maxit0, xh.ctypes.data,
+                           xa.ctypes.data, C.byref(info), nthreads)
+        return xh, xa, info
 
     def rhs(self, rho, isgnb):
         rho = np.ascontiguousarray(rho, dtype=np.complex128)
@@ -291,7 +303,9 @@ class CF:
         n = self.lunkcf
 
         def mv(z):
-            yh, ya = self.apply(omega, isgnw, *self._split(np.asarray(z).ravel()))
+            # one thread: OpenMP workers spinning between calls would compete with the BLAS
+            # threads of GMRES's orthogonalisation
+            yh, ya = self.apply(omega, isgnw, *self._split(np.asarray(z).ravel()), nthreads=1)
             return np.concatenate([yh.real, yh.imag, ya.real, ya.imag])
 
         bh, ba = self.rhs(rho, isgnb)

@@ -56,17 +56,21 @@ double orc_dnrm2(int64_t n, const double *x)
 static void axpby(int64_t n, double *z, double a, const double *x, double b, const double *y)
 { for (int64_t i = 0; i < n; i++) z[i] = a * x[i] + b * y[i]; }
 
-typedef struct {
+typedef struct tfq_ctx {
     const orc_model *m; int nthreads; int64_t lnum; double *V[10];
     int iter; double crit; int exited;
+    void (*ax)(struct tfq_ctx *c, const double *x, double *y);   /* the operator */
+    const orc_cf *cf; double omega; int isgnw;
 } tfq_ctx;
+
+static void ax_steady(tfq_ctx *c, const double *x, double *y) { orc_calc_ax(c->m, (const ozc *)x, (ozc *)y, c->nthreads); }
 
 /* solve_tfqmr.f90:194-280: before every AXB requested by dutfx (and at its final
  * return), every iter_show=50 calls, test the true residual ||A x - b|| <= crit. */
 static int tfq_check(tfq_ctx *c)
 {
     if (c->iter % 50 == 0) {
-        orc_calc_ax(c->m, (const ozc *)c->V[1], (ozc *)c->V[9], c->nthreads);
+        c->ax(c, c->V[1], c->V[9]);
         axpby(c->lnum, c->V[9], 1.0, c->V[9], -1.0, c->V[2]);
         double e = orc_dnrm2(c->lnum, c->V[9]);
         if (e <= c->crit) { c->exited = 1; return 1; }
@@ -77,7 +81,7 @@ static int tfq_axb(tfq_ctx *c, int colx, int colb)
 {
     if (tfq_check(c)) return 1;
     c->iter++;
-    orc_calc_ax(c->m, (const ozc *)c->V[colx], (ozc *)c->V[colb], c->nthreads);
+    c->ax(c, c->V[colx], c->V[colb]);
     return 0;
 }
 
@@ -153,7 +157,7 @@ stop:
 int orc_solve_tfqmr(const orc_model *m, double crit, int maxit0, ozc *rho, orc_solve_info *info, int nthreads)
 {
     tfq_ctx c; memset(&c, 0, sizeof c);
-    c.m = m; c.nthreads = nthreads; c.lnum = 2 * (m->lunk + 1); c.crit = crit;
+    c.m = m; c.nthreads = nthreads; c.lnum = 2 * (m->lunk + 1); c.crit = crit; c.ax = ax_steady;
     for (int k = 1; k <= 9; k++) c.V[k] = calloc(c.lnum, sizeof(double));
     /* zmat_herm_coo('u') on the RDO: upper triangle defines the lower one, real diagonal */
     {
@@ -182,6 +186,37 @@ int orc_solve_tfqmr(const orc_model *m, double crit, int maxit0, ozc *rho, orc_s
     if (info) { info->iters = c.iter; info->axb = c.iter; info->ierr = ierr; info->exit_reason = c.exited; info->resid = orc_dnrm2(c.lnum, c.V[9]); }
     for (int k = 1; k <= 9; k++) free(c.V[k]);
     free(xpad);
+    return 0;
+}
+
+/* corrfunc/solve_cf_tfqmr_spa.f90: the vector is [h; a] (qmrvecs_cf), the right-hand side
+ * -(brhoh; brhoa) (lines 185-197), x0 = 0, dutfx with tolerance 1e-3 crit and the driver's
+ * every-50-applies test ||b - L x|| <= crit (lines 56-60, 262-290). */
+static void ax_cf(tfq_ctx *c, const double *x, double *y)
+{
+    int64_t L = c->cf->lunkcf;
+    orc_cf_apply(c->m, c->cf, c->omega, c->isgnw, (const ozc *)x, (const ozc *)x + L, (ozc *)y, (ozc *)y + L, c->nthreads);
+}
+
+int orc_cf_solve(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, int isgnw, double omega, double crit,
+                 int maxit0, ozc *xh, ozc *xa, orc_solve_info *info, int nthreads)
+{
+    int64_t L = cf->lunkcf;
+    tfq_ctx c; memset(&c, 0, sizeof c);
+    c.m = m; c.nthreads = nthreads; c.lnum = 4 * L; c.crit = crit; c.ax = ax_cf;
+    c.cf = cf; c.omega = omega; c.isgnw = isgnw;
+    for (int k = 1; k <= 9; k++) c.V[k] = calloc(c.lnum, sizeof(double));
+    ozc *b = (ozc *)c.V[2];
+    orc_cf_rhs(m, cf, rho, isgnb, b, b + L);
+    for (int64_t k = 0; k < c.lnum; k++) c.V[2][k] = -c.V[2][k];
+    int ierr = 0;
+    if (orc_dnrm2(c.lnum, c.V[2]) > crit) orc_dutfx(&c, maxit0 / 2, crit * 1e-3, &ierr);
+    memcpy(xh, c.V[1], sizeof(ozc) * L);
+    memcpy(xa, (ozc *)c.V[1] + L, sizeof(ozc) * L);
+    ax_cf(&c, c.V[1], c.V[9]);
+    axpby(c.lnum, c.V[9], 1.0, c.V[9], -1.0, c.V[2]);
+    if (info) { info->iters = c.iter; info->axb = c.iter; info->ierr = ierr; info->exit_reason = c.exited; info->resid = orc_dnrm2(c.lnum, c.V[9]); }
+    for (int k = 1; k <= 9; k++) free(c.V[k]);
     return 0;
 }
 

@@ -96,3 +96,18 @@ def test_cf_apply_is_real_linear(level):
     z0, z1 = c.apply(0.0, 2, *x1), c.apply(0.7, 2, *x1)
     assert np.allclose(z1[0] - z0[0], 0.7 * x1[1], atol=1e-12)
     assert np.allclose(z0[0], y0[0]) and np.allclose(z0[1], y0[1])
+
+
+@pytest.mark.parametrize("isgnb, isgnw", [(1, 1), (2, 2)])
+def test_reference_tfqmr_agrees_with_gmres(level, isgnb, isgnw):
+    """The C restatement of solve_cf_tfqmr_spa (TFQMR from x = 0) against an independent GMRES.
+    On this small hierarchy the Krylov space closes and TFQMR stops on an exact zero of
+    rho or sigma (ierr 8) a little above crit, which the reference accepts as its result."""
+    m, rho = level
+    c = of.CF(m, 1, 1)
+    w = 0.4 / of.HBAR
+    xh, xa, info = c.tfqmr(rho, w, isgnb, isgnw, crit=1e-11, maxit0=40000, nthreads=1)
+    assert info.resid <= 1e-9
+    gh, ga, _ = c.solve(rho, w, isgnb, isgnw, tol=1e-13)
+    assert np.linalg.norm(xh - gh) <= 1e-8 * np.linalg.norm(gh)
+    assert np.linalg.norm(xa - ga) <= 1e-8 * np.linalg.norm(ga)
