@@ -21,6 +21,11 @@ of a time propagation in write_tape / read_tape):
                                    fermion/initialize2_spa.f90:24-110).
 hamil_sys.data (form='unformatted', sequential): one record of nrho^2 complex128, column-major
                                    (main/calchs.f90:78-82).
+
+Cached tables (raw streams; logicals 4 bytes, .true. = -1 as Intel writes them):
+  coefindex.data, auxindex.data       : the coupling tables (main/buildcoefindex.f90:683-709)
+  sparse_index.data, sparse_info.data : the per-ADO patterns (fermion/prelude_spa.f90:798-820)
+The readers apply the reference's compatibility checks before the data are used.
 """
 import re
 import struct
@@ -238,6 +243,185 @@ def read_tape(path, model):
     if nunk != model.nunk or lunk != model.lunk or data.size != lunk:
         raise ValueError("resume tape does not match the model's ADO count or stored entries")
     return t, data.copy()
+
+
+# ---- cached tables (Intel form='binary': raw streams; logical = 4 bytes, .true. = -1) ----
+_TRUE, _FALSE = -1, 0
+_COEF_REC = np.dtype([("indexcoef", "<i8"), ("itypecoef", "i1"), ("ifactfcoef", "i1"), ("ifactrcoef", "i1")])
+_HSYS_REC = np.dtype([("irow", "<i4"), ("icol", "<i4"), ("cval", "<c16")])
+_NNZ_REC = np.dtype([("nnz_spa", "<i4"), ("ind_spa", "<i8")])
+_RC_REC = np.dtype([("irow", "<i4"), ("icol", "<i4")])
+
+
+def _lg(v):
+    return _TRUE if v else _FALSE
+
+
+def _truth(v):
+    """Intel's test of a logical: the low bit."""
+    return bool(v & 1)
+
+
+def _head9(model):
+    # ntier, ncor, norbs, nspin, nalf, numfff, ntier0, ndrawer_slow, ncor_slow (lad = F, no psdfff)
+    return (model.ntier, model.ncor, model.norbs, model.nspin, model.nalf, 0, model.ntier, 0, 0)
+
+
+def _lscreen(model):
+    return bool(model.tables.lscreen)
+
+
+def write_coefindex(path, model):
+    """coefindex.data (main/buildcoefindex.f90:683-698): the job flags the reader checks, with
+    the reference's defaults for the options outside the supported subset (lad, lfilter,
+    ltrun_der, lsimple, lomit all F; lwalf T), then lall records of indexcoef (int64),
+    itypecoef, ifactfcoef, ifactrcoef (int8)."""
+    rec = np.zeros(model.lall, dtype=_COEF_REC)
+    rec["indexcoef"] = model.array("indexcoef")
+    rec["itypecoef"] = model.array("itypecoef")
+    rec["ifactfcoef"] = model.array("ifactfcoef")
+    rec["ifactrcoef"] = model.array("ifactrcoef")
+    with open(path, "wb") as f:
+        f.write(struct.pack("<9i", *_head9(model)))
+        f.write(struct.pack("<3i2id", _lg(False), _lg(True), _lg(True), 1, 2, 0.9))   # lad, lad_fast, lset_fast, idegen_fast, ndegen_fast, dratio_fast
+        f.write(struct.pack("<3i", _lg(False), 2, 3))                                 # lfilter, nfilter_count, nfilter_long
+        f.write(struct.pack("<i", _lg(False)))                                        # ltrun_der
+        f.write(struct.pack("<2i", _lg(False), _lg(True)))                            # lsimple, lwalf
+        f.write(struct.pack("<i", _lg(_lscreen(model))))                              # lscreen
+        f.write(struct.pack("<id", _lg(False), 4e-6))                                 # lomit, dfact_omit
+        f.write(struct.pack("<q", model.lall))
+        f.write(rec.tobytes())
+
+
+def read_coefindex(path, model):
+    """The coupling table of a coefindex.data file, with the reader's compatibility checks
+    (main/buildcoefindex.f90:44-159): the nine sizes, then lad, lfilter, ltrun_der, lsimple and
+    lwalf, lscreen and lomit must agree with the job.  Returns a dict of the four arrays."""
+    with open(path, "rb") as f:
+        head = struct.unpack("<9i", f.read(36))
+        if head != _head9(model):
+            raise ValueError(f"coefindex.data incompatible: sizes {head}")
+        lad, _, _, _, _, _ = struct.unpack("<3i2id", f.read(28))
+        lfilter, _, _ = struct.unpack("<3i", f.read(12))
+        (ltrun_der,) = struct.unpack("<i", f.read(4))
+        lsimple, lwalf = struct.unpack("<2i", f.read(8))
+        (lscreen,) = struct.unpack("<i", f.read(4))
+        lomit, _ = struct.unpack("<id", f.read(12))
+        if _truth(lad) or _truth(lfilter) or _truth(ltrun_der) or _truth(lsimple) or not _truth(lwalf) or _truth(lomit):
+            raise ValueError("coefindex.data written for options outside the supported subset")
+        if _truth(lscreen) != _lscreen(model):
+            raise ValueError("coefindex.data incompatible: lscreen differs")
+        (lall,) = struct.unpack("<q", f.read(8))
+        rec = np.frombuffer(f.read(lall * _COEF_REC.itemsize), dtype=_COEF_REC)
+    if rec.size != lall:
+        raise ValueError("coefindex.data is truncated")
+    return {k: rec[k].copy() for k in _COEF_REC.names}
+
+
+def write_auxindex(path, model):
+    """auxindex.data (main/buildcoefindex.f90:700-709, lsimple = F): int64 nunk, then
+    index_coef_ref (int64 per ADO)."""
+    with open(path, "wb") as f:
+        f.write(struct.pack("<q", model.nunk))
+        f.write(model.array("index_coef_ref").astype("<i8").tobytes())
+
+
+def read_auxindex(path, model):
+    with open(path, "rb") as f:
+        (nunk,) = struct.unpack("<q", f.read(8))
+        if nunk != model.nunk:
+            raise ValueError(f"auxindex.data: length {nunk}, expected {model.nunk}")
+        ref = np.frombuffer(f.read(8 * nunk), dtype="<i8")
+    if ref.size != nunk:
+        raise ValueError("auxindex.data is truncated")
+    return ref.copy()
+
+
+def exp_hs(model, alpha=0.31415926, kmax=10):
+    """E0 = 1 + sum_{k <= kmax} (alpha H)^k / k! (utility/calc_exp_hmat.f90), H in internal units."""
+    n = model.nrho
+    h = model.array("hs").reshape(n, n, order="F")
+    out = np.eye(n, dtype=np.complex128)
+    c1 = np.eye(n, dtype=np.complex128)
+    f = 1.0
+    for k in range(1, kmax + 1):
+        f /= k
+        c1 = alpha * (c1 @ h)
+        out = out + f * c1
+    return out
+
+
+def _sparse_flags(model):
+    # nunk, offcor, lequileads, lsimple, lscreen, lproj
+    return struct.pack("<q5i", model.nunk, _lg(False), _lg(False), _lg(False), _lg(_lscreen(model)), _lg(False))
+
+
+def _flags_match(raw, model):
+    if len(raw) != 28:
+        return False
+    nunk, *flags = struct.unpack("<q5i", raw)
+    return nunk == model.nunk and [_truth(v) for v in flags] == [False, False, False, _lscreen(model), False]
+
+
+def write_sparse(index_path, info_path, model):
+    """sparse_index.data and sparse_info.data (fermion/prelude_spa.f90:798-820): the sizes and
+    job flags, the COO of E0 = exp(0.314 H) (|v| >= 1e-32, column-major, as zmat_dns2coo), the
+    (nnz_spa, ind_spa) pairs of every ADO; then lunk and the (irow, icol) pairs of every entry."""
+    n = model.nrho
+    e0 = exp_hs(model)
+    jj, ii = np.nonzero(np.abs(e0.T) >= 1e-32)      # column-major scan
+    hs = np.zeros(ii.size, dtype=_HSYS_REC)
+    hs["irow"], hs["icol"], hs["cval"] = ii + 1, jj + 1, e0[ii, jj]
+    nz = np.zeros(model.nunk, dtype=_NNZ_REC)
+    nz["nnz_spa"], nz["ind_spa"] = model.array("nnz_spa"), model.array("ind_spa")
+    rc = np.zeros(model.lunk, dtype=_RC_REC)
+    rc["irow"], rc["icol"] = model.array("irow_spa"), model.array("icol_spa")
+    with open(index_path, "wb") as f:
+        f.write(struct.pack("<9i", *_head9(model)))
+        f.write(_sparse_flags(model))
+        f.write(struct.pack("<i3i", _lg(False), 1, n, 1))      # lprocc, nproji, nprojf, nprocc
+        f.write(struct.pack("<i", ii.size))
+        f.write(hs.tobytes())
+        f.write(nz.tobytes())
+    with open(info_path, "wb") as f:
+        f.write(_sparse_flags(model))
+        f.write(struct.pack("<q", model.lunk))
+        f.write(rc.tobytes())
+
+
+def read_sparse(index_path, info_path, model):
+    """The per-ADO patterns of a sparse_index.data / sparse_info.data pair, reused only when
+    the reference would reuse them (fermion/prelude_spa.f90:65-133, 463-510): matching sizes
+    and flags, and a cached E0 with the same sparsity as the job's.  Returns a dict of
+    nnz_spa, ind_spa, irow_spa, icol_spa and lunk."""
+    n = model.nrho
+    with open(index_path, "rb") as f:
+        head = struct.unpack("<9i", f.read(36))
+        if head != _head9(model):
+            raise ValueError(f"sparse_index.data incompatible -- 1: {head}")
+        if not _flags_match(f.read(28), model):
+            raise ValueError("sparse_index.data incompatible -- 2")
+        f.read(16)                                              # projection fields (lproj = F)
+        (nnz_h,) = struct.unpack("<i", f.read(4))
+        if nnz_h <= 0 or nnz_h > n * n:
+            raise ValueError(f"error nnz_hsys read from sparse_index.data: {nnz_h}")
+        hs = np.frombuffer(f.read(nnz_h * _HSYS_REC.itemsize), dtype=_HSYS_REC)
+        nz = np.frombuffer(f.read(model.nunk * _NNZ_REC.itemsize), dtype=_NNZ_REC)
+    cached = np.zeros((n, n), dtype=bool)
+    cached[hs["irow"] - 1, hs["icol"] - 1] = np.abs(hs["cval"]) >= 1e-32
+    if not np.array_equal(cached, np.abs(exp_hs(model)) >= 1e-32):
+        raise ValueError("incompatible sparse_index.data: the sparsity of exp(0.314 H) differs")
+    if nz.size != model.nunk:
+        raise ValueError("sparse_index.data is truncated")
+    with open(info_path, "rb") as f:
+        if not _flags_match(f.read(28), model):
+            raise ValueError("sparse_info.data incompatible -- 1")
+        (lunk,) = struct.unpack("<q", f.read(8))
+        rc = np.frombuffer(f.read(lunk * _RC_REC.itemsize), dtype=_RC_REC)
+    if rc.size != lunk:
+        raise ValueError("sparse_info.data is truncated")
+    return {"nnz_spa": nz["nnz_spa"].copy(), "ind_spa": nz["ind_spa"].copy(), "irow_spa": rc["irow"].copy(),
+            "icol_spa": rc["icol"].copy(), "lunk": lunk}
 
 
 def write_hamil_sys(path, hs):

@@ -3,6 +3,8 @@
 The input text below follows the reference's positional records
 (main/evaluatepara.f90:71-84) and namelist groups; the tables built from it must equal
 those of the same model configured directly."""
+import struct
+
 import numpy as np
 import pytest
 
@@ -129,3 +131,52 @@ def test_resume_tape_round_trip_and_layout(tmp_path):
     other = heomq.Model(cf.siam(ntier=4, nmats=2))
     with pytest.raises(ValueError):
         inp.read_tape(path, other)
+
+
+@pytest.mark.parametrize("cfg", [cf.siam(ntier=3), cf.dqd(ntier=3)], ids=["siam", "dqd_lscreen"])
+def test_cached_tables_round_trip_and_layout(tmp_path, cfg):
+    """coefindex.data / auxindex.data (main/buildcoefindex.f90:683-709) and sparse_index.data /
+    sparse_info.data (fermion/prelude_spa.f90:798-820): written in the reference's stream
+    layout, read back through the reference's compatibility checks, equal to the tables."""
+    m = heomq.Model(cfg)
+    ci, ai = tmp_path / "coefindex.data", tmp_path / "auxindex.data"
+    si, sf = tmp_path / "sparse_index.data", tmp_path / "sparse_info.data"
+    inp.write_coefindex(ci, m)
+    inp.write_auxindex(ai, m)
+    inp.write_sparse(si, sf, m)
+    # byte counts of the streams
+    nh = int((np.abs(inp.exp_hs(m)) >= 1e-32).sum())
+    assert ci.stat().st_size == 36 + 28 + 12 + 4 + 8 + 4 + 12 + 8 + 11 * m.lall
+    assert ai.stat().st_size == 8 + 8 * m.nunk
+    assert si.stat().st_size == 36 + 28 + 16 + 4 + 24 * nh + 12 * m.nunk
+    assert sf.stat().st_size == 28 + 8 + 8 * m.lunk
+    raw = ci.read_bytes()
+    assert struct.unpack("<9i", raw[:36]) == (m.ntier, m.ncor, m.norbs, m.nspin, m.nalf, 0, m.ntier, 0, 0)
+    assert struct.unpack("<i", raw[36 + 28 + 12 + 4 + 8:36 + 28 + 12 + 4 + 8 + 4])[0] == (-1 if cfg.get("lscreen") else 0)
+    coef = inp.read_coefindex(ci, m)
+    for k in ("indexcoef", "itypecoef", "ifactfcoef", "ifactrcoef"):
+        np.testing.assert_array_equal(coef[k], m.array(k))
+    np.testing.assert_array_equal(inp.read_auxindex(ai, m), m.array("index_coef_ref"))
+    sp = inp.read_sparse(si, sf, m)
+    assert sp["lunk"] == m.lunk
+    for k in ("nnz_spa", "ind_spa", "irow_spa", "icol_spa"):
+        np.testing.assert_array_equal(sp[k], m.array(k))
+
+
+def test_cached_tables_of_another_job_are_refused(tmp_path):
+    m3, m4 = heomq.Model(cf.siam(ntier=3)), heomq.Model(cf.siam(ntier=4))
+    inp.write_coefindex(tmp_path / "c", m3)
+    inp.write_auxindex(tmp_path / "a", m3)
+    inp.write_sparse(tmp_path / "i", tmp_path / "f", m3)
+    with pytest.raises(ValueError, match="incompatible"):
+        inp.read_coefindex(tmp_path / "c", m4)
+    with pytest.raises(ValueError, match="auxindex"):
+        inp.read_auxindex(tmp_path / "a", m4)
+    with pytest.raises(ValueError, match="incompatible"):
+        inp.read_sparse(tmp_path / "i", tmp_path / "f", m4)
+    # same sizes, different Hamiltonian sparsity: the cached exp(0.314 H) does not match
+    md = heomq.Model(cf.dqd(ntier=3, t=0.0))
+    mt = heomq.Model(cf.dqd(ntier=3, t=0.5))
+    inp.write_sparse(tmp_path / "i2", tmp_path / "f2", md)
+    with pytest.raises(ValueError, match="sparsity"):
+        inp.read_sparse(tmp_path / "i2", tmp_path / "f2", mt)
