@@ -102,7 +102,7 @@ heom_ctx::~heom_ctx()
 {
     dfwd.release();
     dadj.release();
-    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch, d_rdo_pair, d_rdo_upper};
+    void *ptrs[] = {hval64, hval32, hvaldf, es64, d_cur_terms, dx, dy, dz, fx, fy, dscratch, d_rdo_pair, d_rdo_upper, d_ent_rc};
     for (void *p : ptrs) if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -713,6 +713,19 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
         CK(cudaMalloc((void **)&c->fy, sizeof(float2) * N));
         CK(cudaMalloc((void **)&c->dscratch, sizeof(double) * 2048));
         drandn_stream(2 * N, c->rt_host);
+        // (row, col) of every stored entry, 0-based in one byte each, for the per-ADO dense
+        // transforms of the Jacobi sweep; the largest |cb| for its shift
+        if (c->nrho <= 256) {
+            std::vector<uint16_t> rc((size_t)std::max<int64_t>(1, c->lunk));
+            for (int64_t e = 0; e < c->lunk; e++) rc[e] = (uint16_t)((t->irow_spa[e] - 1) | ((t->icol_spa[e] - 1) << 8));
+            CK(cudaMalloc((void **)&c->d_ent_rc, sizeof(uint16_t) * rc.size()));
+            CK(cudaMemcpy(c->d_ent_rc, rc.data(), sizeof(uint16_t) * rc.size(), cudaMemcpyHostToDevice));
+        }
+        {
+            const size_t ncb = (size_t)t->norbs * t->nspin * t->ncor * t->nalf * 2;
+            const cd *cbv = reinterpret_cast<const cd *>(t->cb);
+            for (size_t k = 0; k < ncb; k++) c->cb_abs_max = std::max(c->cb_abs_max, std::abs(cbv[k]));
+        }
         CK(cudaStreamSynchronize(c->stream));
         *out = c.release();
     });

@@ -90,6 +90,8 @@ struct heom_ctx {
     int32_t nz0 = 0, ndiag = 0;
     double reg_scale = 1.0;                         // weight of the regularising blocks
     double cheby_delta = 0.0;                       // spectral width of the Liouville diagonal
+    uint16_t *d_ent_rc = nullptr;                   // 0-based (row | col << 8) of every stored entry
+    double cb_abs_max = 0.0;                        // largest |cb| (the Jacobi shift rule)
     heom::CurrentTerm *d_cur_terms = nullptr;
     int32_t n_cur_terms = 0;
     // scratch vectors (lunk + 1 complex)

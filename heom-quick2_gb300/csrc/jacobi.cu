@@ -1,0 +1,289 @@
+// Jacobi steady-state iteration on GB300 (jacobi/: prelude_jacobi, calc_ax_jacobi_spa_omp,
+// solve_jacobi).
+//
+// One sweep maps x to x' with, for every ADO n (drawers summing to g_n),
+//     x'_n = P_n (ejac - g_n + i L)^-1 (ejac x_n + C_n x),
+// where C_n x are the couplings of n to the neighbouring tiers on the pattern P_n of n and
+// L = [H, .] is the system Liouvillian; its fixed point solves A x = 0 with the trace kept.
+// The reference diagonalises L in Liouville space (nrho^2 x nrho^2) and applies its
+// eigenvectors by two matrix-vector products per ADO.  Here H = U diag(E) U^H is diagonalised
+// once and (ejac - g + i L)^-1 Y = U [(U^H Y U)_ab / (ejac - g + i (E_a - E_b))] U^H: four
+// nrho^3 products per ADO on one thread block, from shared memory.  The couplings come from
+// the steady apply: C_n x = (A x)_n - g_n x_n + i P_n [H, x_n].
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <memory>
+
+#include "context.cuh"
+
+namespace heom {
+
+namespace {
+
+constexpr int kJacThreads = 256;
+constexpr double kDpico = 1e-12;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) { return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }  // conj(a) b
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// one ADO of one instance per block: blockIdx.x = ADO, blockIdx.y = instance
+__global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_t *__restrict__ rc,
+                                                       const double2 *__restrict__ x, const double2 *__restrict__ y,
+                                                       double2 *__restrict__ xn, const double2 *__restrict__ gdiag,
+                                                       const double2 *__restrict__ U, const double *__restrict__ E,
+                                                       const double2 *__restrict__ H, double ejac, int n, int64_t vstride)
+{
+    extern __shared__ double2 sm[];
+    const int nn = n * n;
+    double2 *sU = sm, *sH = sm + nn, *sX = sm + 2 * nn, *sY = sm + 3 * nn, *sT = sm + 4 * nn;
+    double *sE = reinterpret_cast<double *>(sm + 5 * nn);
+    const int a = blockIdx.x, b = blockIdx.y;
+    const int off = __ldg(P.ado_off + a), nz = __ldg(P.ado_off + a + 1) - off;
+    x += (int64_t)b * vstride + off;
+    y += (int64_t)b * vstride + off;
+    xn += (int64_t)b * vstride + off;
+    U += (int64_t)b * nn;
+    H += (int64_t)b * nn;
+    E += (int64_t)b * n;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+        sU[k] = U[k];
+        sH[k] = H[k];
+        sX[k] = make_double2(0, 0);
+        sY[k] = make_double2(0, 0);
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sE[k] = E[k];
+    __syncthreads();
+    for (int q = threadIdx.x; q < nz; q += blockDim.x) {
+        const unsigned w = rc[off + q];
+        sX[(w & 0xFF) + (w >> 8) * n] = x[q];
+    }
+    __syncthreads();
+    const double2 g = gdiag[(int64_t)b * P.nado + a];
+    const double2 d = make_double2(ejac - g.x, -g.y);
+    // Y = ejac x + C x = (ejac - g) x + A x + i P[H, x] on the pattern
+    for (int q = threadIdx.x; q < nz; q += blockDim.x) {
+        const unsigned w = rc[off + q];
+        const int r = w & 0xFF, c = w >> 8;
+        double2 comm = make_double2(0, 0);
+        for (int k = 0; k < n; k++) {
+            comm = cadd(comm, cmul(sH[r + k * n], sX[k + c * n]));
+            const double2 xh = cmul(sX[r + k * n], sH[k + c * n]);
+            comm = make_double2(comm.x - xh.x, comm.y - xh.y);
+        }
+        const double2 v = cadd(cadd(cmul(d, x[q]), y[q]), make_double2(-comm.y, comm.x));
+        sY[r + c * n] = v;
+    }
+    __syncthreads();
+    // T = U^H Y
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+        const int i = k % n, j = k / n;
+        double2 s = make_double2(0, 0);
+        for (int l = 0; l < n; l++) s = cadd(s, cmulc(sU[l + i * n], sY[l + j * n]));
+        sT[k] = s;
+    }
+    __syncthreads();
+    // W = (T U) / (ejac - g + i (E_i - E_j)), into Y
+    const bool dsmall = sqrt(d.x * d.x + d.y * d.y) <= kDpico;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+        const int i = k % n, j = k / n;
+        double2 s = make_double2(0, 0);
+        for (int l = 0; l < n; l++) s = cadd(s, cmul(sT[i + l * n], sU[l + j * n]));
+        const double lam = sE[i] - sE[j];
+        double2 den = make_double2(d.x, d.y + lam);
+        if (dsmall) den = make_double2(0.0, lam);
+        double2 f = make_double2(0, 0);
+        if (!dsmall || fabs(lam) > kDpico) {
+            const double m2 = den.x * den.x + den.y * den.y;
+            f = make_double2(den.x / m2, -den.y / m2);
+        }
+        sY[k] = cmul(s, f);
+    }
+    __syncthreads();
+    // T = U W
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+        const int i = k % n, j = k / n;
+        double2 s = make_double2(0, 0);
+        for (int l = 0; l < n; l++) s = cadd(s, cmul(sU[i + l * n], sY[l + j * n]));
+        sT[k] = s;
+    }
+    __syncthreads();
+    // x'(r, c) = (T U^H)(r, c) on the pattern
+    for (int q = threadIdx.x; q < nz; q += blockDim.x) {
+        const unsigned w = rc[off + q];
+        const int r = w & 0xFF, c = w >> 8;
+        double2 s = make_double2(0, 0);
+        for (int l = 0; l < n; l++) {
+            const double2 u = sU[c + l * n];
+            s = cadd(s, cmul(sT[r + l * n], make_double2(u.x, -u.y)));
+        }
+        xn[q] = s;
+    }
+}
+
+// Hermitian eigen-decomposition by cyclic Jacobi rotations (a phase on column q makes a_pq
+// real, then a real plane rotation removes it): a (column-major) is destroyed, v receives
+// the eigenvectors as columns.
+void herm_eig(int n, std::vector<cd> &a, std::vector<double> &w, std::vector<cd> &v)
+{
+    v.assign((size_t)n * n, cd(0, 0));
+    for (int i = 0; i < n; i++) v[i + (size_t)i * n] = 1.0;
+    auto A = [&](int i, int j) -> cd & { return a[i + (size_t)j * n]; };
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0, tot = 0;
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++) { double t = std::norm(A(i, j)); tot += t; if (i != j) off += t; }
+        if (off <= 1e-30 * std::max(tot, 1e-300)) break;
+        for (int p = 0; p < n; p++)
+            for (int q = p + 1; q < n; q++) {
+                const double r = std::abs(A(p, q));
+                if (r < 1e-300) continue;
+                const cd ph = A(p, q) / r;
+                for (int k = 0; k < n; k++) { A(k, q) *= std::conj(ph); v[k + (size_t)q * n] *= std::conj(ph); }
+                for (int k = 0; k < n; k++) A(q, k) *= ph;
+                const double th = (A(q, q).real() - A(p, p).real()) / (2 * r);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1));
+                const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < n; k++) { cd x = A(k, p), y = A(k, q); A(k, p) = c * x - s * y; A(k, q) = s * x + c * y; }
+                for (int k = 0; k < n; k++) { cd x = A(p, k), y = A(q, k); A(p, k) = c * x - s * y; A(q, k) = s * x + c * y; }
+                for (int k = 0; k < n; k++) {
+                    cd x = v[k + (size_t)p * n], y = v[k + (size_t)q * n];
+                    v[k + (size_t)p * n] = c * x - s * y; v[k + (size_t)q * n] = s * x + c * y;
+                }
+            }
+    }
+    w.resize(n);
+    for (int i = 0; i < n; i++) w[i] = A(i, i).real();
+}
+
+}  // namespace
+}  // namespace heom
+
+using namespace heom;
+
+extern "C" {
+
+int heom_jacobi_shift(heom_ctx *c, double *ejac)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!ejac) fail(HEOM_E_ARG, "null argument");
+        std::vector<cd> a = c->hs_host, v;
+        std::vector<double> e;
+        herm_eig(c->nrho, a, e, v);
+        const double lo = *std::min_element(e.begin(), e.end()), hi = *std::max_element(e.begin(), e.end());
+        // the nonzero eigenvalues of L = [H, .] are the differences E_a - E_b; their span
+        const double gap = hi - lo > kDpico ? 2 * (hi - lo) : 0.0;
+        *ejac = std::max(gap, std::sqrt((double)(c->ntier - 1) * c->cb_abs_max));
+    });
+}
+
+int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Complex *rho, heom_solve_info *info)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!o || !rho) fail(HEOM_E_ARG, "null argument");
+        const int n = c->nrho, nn = n * n;
+        if (n > 32) fail(HEOM_E_UNSUPPORTED, "the Jacobi sweep keeps five nrho x nrho matrices in shared memory: nrho <= 32");
+        if (!c->d_ent_rc) fail(HEOM_E_UNSUPPORTED, "entry coordinates missing");
+        if (ejac <= 0) heom_jacobi_shift(c, &ejac);
+        if (info) *info = heom_solve_info{};
+        const int64_t N = c->lunk + 1;
+        std::vector<cd> h(reinterpret_cast<cd *>(rho), reinterpret_cast<cd *>(rho) + c->lunk);
+        herm_rdo(c, h.data());
+        std::vector<cd> a = c->hs_host, v;
+        std::vector<double> e;
+        herm_eig(n, a, e, v);
+        std::vector<void *> tmp;
+        auto cleanup = [&] { for (void *p : tmp) cudaFree(p); tmp.clear(); };
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        try {
+            double2 *x = nullptr, *xn = nullptr, *y = nullptr, *gd = nullptr, *dU = nullptr, *dH = nullptr;
+            double *dE = nullptr;
+            CK(cudaMalloc((void **)&x, sizeof(double2) * N)); tmp.push_back(x);
+            CK(cudaMalloc((void **)&xn, sizeof(double2) * N)); tmp.push_back(xn);
+            CK(cudaMalloc((void **)&y, sizeof(double2) * N)); tmp.push_back(y);
+            const DevPlan &P = c->dfwd.view;
+            CK(cudaMalloc((void **)&gd, sizeof(double2) * std::max(1, P.nado))); tmp.push_back(gd);
+            CK(cudaMalloc((void **)&dU, sizeof(double2) * nn)); tmp.push_back(dU);
+            CK(cudaMalloc((void **)&dH, sizeof(double2) * nn)); tmp.push_back(dH);
+            CK(cudaMalloc((void **)&dE, sizeof(double) * n)); tmp.push_back(dE);
+            CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, c->stream));
+            CK(cudaMemsetAsync(xn, 0, sizeof(double2) * N, c->stream));
+            CK(cudaMemcpyAsync(x, h.data(), sizeof(double2) * c->lunk, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dU, v.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dH, c->hs_host.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dE, e.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+            DevCoef<double> K = ctx_coefs(c).k64;
+            fill_gdiag<double>(P, K, gd, 1, c->stream);
+            K.gdiag = gd;
+            const size_t smem = sizeof(double2) * 5 * nn + sizeof(double) * n;
+            if (smem > 48 * 1024)
+                CK(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            auto sweep = [&](double2 *from, double2 *to) {
+                launch_apply<double, false>(P, K, from, y, 1, N, nullptr, c->stream);
+                k_jacobi<<<dim3((unsigned)P.nado, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, from, y, to, gd, dU, dE,
+                                                                                   dH, ejac, n, N);
+            };
+            // ||A x - e_trace|| (solve_jacobi.f90:183-190)
+            auto residual = [&](double2 *from) {
+                launch_apply<double, false>(P, K, from, y, 1, N, nullptr, c->stream);
+                std::vector<double2> last(1);
+                CK(cudaMemcpyAsync(last.data(), y + c->lunk, sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                last[0].x -= 1.0;
+                CK(cudaMemcpyAsync(y + c->lunk, last.data(), sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+                return device_norm2(N, y, c->dscratch, c->stream);
+            };
+            // sweeps 50 at a time in one graph: an even count leaves the iterate in x
+            constexpr int kChunk = 50;
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < kChunk; k += 2) { sweep(x, xn); sweep(xn, x); }
+            CK(cudaStreamEndCapture(c->stream, &g));
+            CK(cudaGraphInstantiate(&ge, g, 0));
+            CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+            CK(cudaEventRecord(e0, c->stream));
+            // iteration 0, then chunks of 50; the residual test follows iterations 0, 50, 100, ...
+            sweep(x, xn);
+            CK(cudaMemcpyAsync(x, xn, sizeof(double2) * N, cudaMemcpyDeviceToDevice, c->stream));
+            int iter = 0;
+            double res = residual(x);
+            int64_t launches = 3;
+            while (res > o->crit && iter + kChunk <= std::max(0, o->maxit0)) {
+                CK(cudaGraphLaunch(ge, c->stream));
+                iter += kChunk;
+                launches += 2 * kChunk + 1;
+                res = residual(x);
+            }
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaGraphExecDestroy(ge);
+            cudaGraphDestroy(g);
+            CK(cudaMemcpyAsync(rho, x, sizeof(double2) * c->lunk, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            CK(cudaGetLastError());
+            if (info) {
+                info->iters = iter;
+                info->resid = res;
+                info->converged = res <= o->crit;
+                info->ierr = info->converged ? 0 : 1;
+                info->seconds = ms * 1e-3;
+                info->launches = launches;
+            }
+        } catch (...) {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            cleanup();
+            throw;
+        }
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        cleanup();
+    });
+}
+
+}  // extern "C"

@@ -122,6 +122,8 @@ SIGNATURES = {
     "heom_batch_solve_dev": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_batch_destroy": (None, [C.c_void_p]),
     "heom_batch_current_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
+    "heom_solve_jacobi": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_double, C.c_void_p, _p(SolveInfo)]),
+    "heom_jacobi_shift": (C.c_int, [C.c_void_p, C.c_void_p]),
     "heom_model_cf_pattern": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _p(CfTables)]),
     "heom_cf_create": (C.c_int, [C.c_void_p, _p(Tables), _p(CfTables), _p(C.c_void_p)]),
     "heom_cf_destroy": (None, [C.c_void_p]),
@@ -333,6 +335,24 @@ class Context:
         if check:
             _check(rc)
         return rho, info
+
+    def solve_jacobi(self, rho=None, crit=1e-10, maxit0=20000, ejac=0.0, check=True):
+        """Steady state by the reference's Jacobi sweeps (methodss = 4); ejac in energy / hbar,
+        <= 0 for prelude_jacobi's rule."""
+        if rho is None:
+            rho = self.model.initial_guess()
+        rho = _c128(rho, self.lunk).copy()
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=PREC_FP64)
+        info = SolveInfo()
+        rc = lib().heom_solve_jacobi(self.h, C.byref(o), float(ejac), rho.ctypes.data, C.byref(info))
+        if check:
+            _check(rc)
+        return rho, info
+
+    def jacobi_shift(self):
+        e = C.c_double()
+        _check(lib().heom_jacobi_shift(self.h, C.byref(e)))
+        return e.value
 
     def solve_batch(self, rhos, hs_batch=None, eshift_batch=None, crit=1e-10, maxit0=20000, precision=PREC_FP64,
                     inner_tol=0.0, max_refine=8, inplace=False):

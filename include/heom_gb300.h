@@ -174,6 +174,17 @@ typedef struct {
 /* rho: lunk_spa complex (host), initial guess in, steady state out. */
 int heom_solve_tfqmr(heom_ctx *ctx, const heom_solve_opts *o, double _Complex *rho, heom_solve_info *info);
 
+/* Steady state by Jacobi sweeps (solve_jacobi, jacobi/solve_jacobi.f90:1, methodss = 4):
+ * x_n <- P_n (ejac - g_n + i [H, .])^-1 (ejac x_n + couplings of n), from the Hermitised rho,
+ * with the true residual ||A x - e_trace|| tested after sweep 0 and every 50 sweeps until it
+ * is <= o->crit or o->maxit0 sweeps are done (info->converged tells which).  ejac in
+ * energy / hbar; <= 0 selects the rule of prelude_jacobi (heom_jacobi_shift).  nrho <= 32. */
+int heom_solve_jacobi(heom_ctx *ctx, const heom_solve_opts *o, double ejac, double _Complex *rho,
+                      heom_solve_info *info);
+/* The shift of jacobi/prelude_jacobi.f90:84-111: max(span of the nonzero eigenvalues of
+ * [H, .], sqrt((ntier - 1) max |cb|)). */
+int heom_jacobi_shift(heom_ctx *ctx, double *ejac);
+
 /* Observables of a host rho (td/calcj.f90, main/calcocc.f90).
  * jt: nalf*nspin (ialf fastest) in reference current units; occ: norbs*nspin. */
 int heom_current(heom_ctx *ctx, const double _Complex *rho, double *jt);

@@ -158,6 +158,16 @@ int orc_cf_solve(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb
 /* brhoh, brhoa from the steady rho (lunk entries); isgnb 1: a^dag rho + rho a, 2: a rho + rho a^dag */
 void orc_cf_rhs(const orc_model *m, const orc_cf *cf, const ozc *rho, int isgnb, ozc *bh, ozc *ba);
 int64_t orc_cf_info(const orc_cf *cf, const char *key);
+
+/* Jacobi steady-state iteration (jacobi/prelude_jacobi.f90, calc_ax_jacobi_spa_omp.f90,
+ * solve_jacobi.f90) */
+typedef struct orc_jacobi orc_jacobi;
+void orc_herm_eig(int n, ozc *a, double *w, ozc *v);
+int  orc_jacobi_build(const orc_model *m, double ejac_in, orc_jacobi **out);
+void orc_jacobi_free(orc_jacobi *J);
+double orc_jacobi_ejac(const orc_jacobi *J);
+void orc_jacobi_sweep(const orc_model *m, const orc_jacobi *J, const ozc *x, ozc *xn);
+int  orc_solve_jacobi(const orc_model *m, const orc_jacobi *J, double crit, int maxit0, ozc *rho, orc_solve_info *info);
 int orc_cf_copy(const orc_cf *cf, int64_t nunk, const char *name, void *dst);
 
 #endif

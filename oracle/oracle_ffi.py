@@ -73,6 +73,13 @@ def lib():
         L.orc_cf_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                    C.c_void_p, C.c_void_p, C.POINTER(SolveInfo), C.c_int]
         L.orc_cf_rhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_jacobi_build.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]
+        L.orc_jacobi_free.argtypes = [C.c_void_p]
+        L.orc_jacobi_ejac.restype = C.c_double
+        L.orc_jacobi_ejac.argtypes = [C.c_void_p]
+        L.orc_jacobi_sweep.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_solve_jacobi.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.POINTER(SolveInfo)]
+        L.orc_herm_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_cf_info.restype = C.c_int64
         L.orc_cf_info.argtypes = [C.c_void_p, C.c_char_p]
         L.orc_cf_copy.argtypes = [C.c_void_p, C.c_int64, C.c_char_p, C.c_void_p]
@@ -337,3 +344,41 @@ class CF:
         c5 = 0.5 * self.rdo(xh) + 0.5j * self.rdo(xa)
         d2 = np.trace(a @ c5).real / np.pi / HBAR
         return d1 + d2, d1, d2
+
+
+class Jacobi:
+    """The Jacobi steady-state iteration of the reference (jacobi/) on an oracle model.
+    ejac: the shift in energy / hbar; <= 0 selects prelude_jacobi's rule."""
+
+    def __init__(self, model, ejac=0.0):
+        self.model = model
+        h = C.c_void_p()
+        lib().orc_jacobi_build(model.h, ejac, C.byref(h))
+        self.h = h
+        self.ejac = lib().orc_jacobi_ejac(h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_jacobi_free(self.h)
+            self.h = None
+
+    def sweep(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        xn = np.zeros(self.model.lunk, dtype=np.complex128)
+        lib().orc_jacobi_sweep(self.model.h, self.h, x.ctypes.data, xn.ctypes.data)
+        return xn
+
+    def solve(self, rho, crit=1e-10, maxit0=20000):
+        rho = np.ascontiguousarray(rho, dtype=np.complex128).copy()
+        info = SolveInfo()
+        lib().orc_solve_jacobi(self.model.h, self.h, crit, maxit0, rho.ctypes.data, C.byref(info))
+        return rho, info
+
+
+def herm_eig(a):
+    a = np.array(a, dtype=np.complex128, order="F", copy=True)
+    n = a.shape[0]
+    w = np.zeros(n)
+    v = np.zeros((n, n), dtype=np.complex128, order="F")
+    lib().orc_herm_eig(n, a.ctypes.data, w.ctypes.data, v.ctypes.data)
+    return w, v
