@@ -39,11 +39,14 @@ def parse():
                     help="profiler run of the two fused FP32x2 inner-iteration kernels: 3 warm-up + 2 timed launches each")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
-    ap.add_argument("--workload", default="steady", choices=["steady", "dos"],
-                    help="steady: batched steady states (the headline); dos: spectral function over frequencies")
+    ap.add_argument("--workload", default="steady", choices=["steady", "dos", "jacobi"],
+                    help="steady: batched steady states (the headline); dos: spectral function over frequencies; "
+                         "jacobi: steady state by the reference's Jacobi sweeps")
     ap.add_argument("--freqs", type=int, default=8, help="dos: frequencies per step")
     ap.add_argument("--profile-cf", action="store_true",
                     help="dos: profiler run of the correlation-function apply alone: 3 warm-up + 2 timed launches")
+    ap.add_argument("--profile-jacobi", action="store_true",
+                    help="jacobi: profiler run of the sweep kernels alone: 1 + 3 launches of each")
     return ap.parse_args()
 
 
@@ -498,6 +501,109 @@ def run_dos(args, ws, rank, local, dist):
     return 0
 
 
+JAC_METRIC = "HEOM Jacobi steady solves/s (methodss = 4, FP64)"
+JAC_WORKLOAD = ("steady state of the serial double quantum dot nd=16, tier L=4 (393812 stored entries), V=0.8, "
+                "by Jacobi sweeps with prelude_jacobi's shift to ||A x - e_trace|| <= crit")
+JAC_CRIT = 1e-9
+
+
+def cpu_jacobi_sample(nthreads, sweeps, nsample=2):
+    """The oracle's C restatement of calc_ax_jacobi_spa_omp (Liouville-space eigenvectors,
+    OpenMP over ADOs): `nsample` sweeps timed, scaled to a solve of `sweeps` sweeps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_ffi
+    import heomq.models as models
+
+    os.environ.setdefault("OMP_NUM_THREADS", str(nthreads))
+    m = oracle_ffi.Model(models.dqd(ntier=5, nmats=3, V=0.8))
+    J = oracle_ffi.Jacobi(m)
+    x = m.initial_guess()
+    x = J.sweep(x)
+    t0 = time.perf_counter()
+    for _ in range(nsample):
+        x = J.sweep(x)
+    t_sweep = (time.perf_counter() - t0) / nsample
+    return t_sweep, 1.0 / (t_sweep * sweeps)
+
+
+def run_jacobi(args, ws, rank, local, dist):
+    import torch
+
+    import heomq
+
+    dev = local
+    torch.cuda.set_device(dev)
+    model = heomq.Model(heomq.models.dqd(ntier=5, nmats=3, V=0.8))
+    ctx = heomq.Context(model, device=dev, adjoint=False)
+    if args.profile_jacobi:
+        t_jac, t_app, b, f = ctx.bench_jacobi(reps=3)
+        print(json.dumps({"profile_jacobi": True, "transform_us": t_jac * 1e6, "apply_us": t_app * 1e6}), flush=True)
+        return 0
+    x0 = model.initial_guess()
+    for _ in range(args.warmup):
+        ctx.solve_jacobi(x0, crit=JAC_CRIT, maxit0=20000)
+    clk = clocks_start() if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    dev_s, wall, launches, infos = 0.0, [], 0, []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rho, info = ctx.solve_jacobi(x0, crit=JAC_CRIT, maxit0=20000)
+        wall.append(time.perf_counter() - t0)
+        dev_s += info.seconds
+        launches += info.launches
+        infos.append(info)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = clocks_stop(clk, dev) if rank == 0 else None
+    t_step = max_over_ranks(dev_s / args.steps, dist, device="cuda")
+    value = ws / t_step
+    e2e_value = ws / max_over_ranks(statistics.median(wall), dist, device="cuda")
+    t_jac, t_app, jbytes, jcfma = ctx.bench_jacobi(reps=10)
+    ref, _ = ctx.solve_tfqmr(crit=1e-10, precision=heomq.PREC_MIXED)
+    cur_err = abs(ctx.current(rho)[0].sum() / ctx.current(ref)[0].sum() - 1)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = jbytes / t_jac / 1e9
+    prof = "jacobi_sweep_dqd_L4.md"
+    cpu = None
+    sweeps = infos[-1].iters + 1
+    if rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        t_sweep, v = cpu_jacobi_sample(nthreads, sweeps)
+        cpu = {"value": v, "unit": "solves/s", "cores": nthreads, "kind": "port",
+               "sample": f"2 sweeps of the C restatement of calc_ax_jacobi_spa_omp (Liouville-space eigenvectors, "
+                         f"OpenMP over ADOs, {t_sweep:.2f} s each), scaled by the {sweeps} sweeps of the solve"}
+    if rank == 0:
+        line = {
+            "metric": JAC_METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": JAC_WORKLOAD, "crit": JAC_CRIT, "ejac_eV": ctx.jacobi_shift() * 0.658211928,
+                       "sweeps": sweeps, "resid": infos[-1].resid, "converged": bool(infos[-1].converged),
+                       "current_rel_diff_vs_mixed_tfqmr": cur_err,
+                       "l2": f"inputs larger than L2: 3 vectors x {model.lunk * 16 / 1e6:.1f} MB plus the plan",
+                       "parallelism": f"replicas x{ws}", "apply_us": t_app * 1e6},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": profile_traffic(prof), "peak_kind": peak_kind,
+                         "kernel": "k_jacobi: per-ADO sector transform of one sweep", "kernel_us": t_jac * 1e6,
+                         "alg_bytes_per_launch": jbytes, "complex_fma_per_launch": jcfma,
+                         "fp64_tflops": 8 * jcfma / t_jac / 1e12,
+                         "note": "FP64 small dense products per ADO from shared memory; profiles/" + prof},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": model.lunk * 16,
+                    "d2h_bytes_per_step": model.lunk * 16},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     ws, rank, local, dist = dist_setup(args)
@@ -514,6 +620,8 @@ def main():
         dist.barrier()
     if args.workload == "dos":
         return run_dos(args, ws, rank, local, dist)
+    if args.workload == "jacobi":
+        return run_jacobi(args, ws, rank, local, dist)
     return run_gb300(args, ws, rank, local, dist)
 
 

@@ -7,9 +7,10 @@
 // L = [H, .] is the system Liouvillian; its fixed point solves A x = 0 with the trace kept.
 // The reference diagonalises L in Liouville space (nrho^2 x nrho^2) and applies its
 // eigenvectors by two matrix-vector products per ADO.  Here H = U diag(E) U^H is diagonalised
-// once and (ejac - g + i L)^-1 Y = U [(U^H Y U)_ab / (ejac - g + i (E_a - E_b))] U^H: four
-// nrho^3 products per ADO on one thread block, from shared memory.  The couplings come from
-// the steady apply: C_n x = (A x)_n - g_n x_n + i P_n [H, x_n].
+// once and (ejac - g + i L)^-1 Y = U [(U^H Y U)_ab / (ejac - g + i (E_a - E_b))] U^H: three
+// products per ADO on one thread block, from shared memory, each summing only over the
+// sector block of H its index lies in.  The couplings come from the steady apply:
+// C_n x = (A x)_n - g_n x_n + i P_n [H, x_n].
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -29,16 +30,23 @@ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) { return make_dou
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
 // one ADO of one instance per block: blockIdx.x = ADO, blockIdx.y = instance
+// States are renumbered so that the connected components of the graph of H (its conserved
+// sectors) are contiguous: H, and with it U, are then block diagonal, and every product below
+// runs over the block [lo(i), hi(i)) of the index it sums against.  perm maps a state to
+// its new number; H, U, E arrive in the new numbering.
 __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_t *__restrict__ rc,
                                                        const double2 *__restrict__ x, const double2 *__restrict__ y,
                                                        double2 *__restrict__ xn, const double2 *__restrict__ gdiag,
                                                        const double2 *__restrict__ U, const double *__restrict__ E,
-                                                       const double2 *__restrict__ H, double ejac, int n, int64_t vstride)
+                                                       const double2 *__restrict__ H, const uint8_t *__restrict__ perm,
+                                                       const uint8_t *__restrict__ blo, const uint8_t *__restrict__ bhi,
+                                                       double ejac, int n, int64_t vstride)
 {
     extern __shared__ double2 sm[];
     const int nn = n * n;
     double2 *sU = sm, *sH = sm + nn, *sX = sm + 2 * nn, *sY = sm + 3 * nn, *sT = sm + 4 * nn;
     double *sE = reinterpret_cast<double *>(sm + 5 * nn);
+    uint8_t *sP = reinterpret_cast<uint8_t *>(sE + n), *sLo = sP + n, *sHi = sLo + n;
     const int a = blockIdx.x, b = blockIdx.y;
     const int off = __ldg(P.ado_off + a), nz = __ldg(P.ado_off + a + 1) - off;
     x += (int64_t)b * vstride + off;
@@ -53,11 +61,11 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
         sX[k] = make_double2(0, 0);
         sY[k] = make_double2(0, 0);
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) sE[k] = E[k];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) { sE[k] = E[k]; sP[k] = perm[k]; sLo[k] = blo[k]; sHi[k] = bhi[k]; }
     __syncthreads();
     for (int q = threadIdx.x; q < nz; q += blockDim.x) {
         const unsigned w = rc[off + q];
-        sX[(w & 0xFF) + (w >> 8) * n] = x[q];
+        sX[sP[w & 0xFF] + sP[w >> 8] * n] = x[q];
     }
     __syncthreads();
     const double2 g = gdiag[(int64_t)b * P.nado + a];
@@ -65,10 +73,10 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
     // Y = ejac x + C x = (ejac - g) x + A x + i P[H, x] on the pattern
     for (int q = threadIdx.x; q < nz; q += blockDim.x) {
         const unsigned w = rc[off + q];
-        const int r = w & 0xFF, c = w >> 8;
+        const int r = sP[w & 0xFF], c = sP[w >> 8];
         double2 comm = make_double2(0, 0);
-        for (int k = 0; k < n; k++) {
-            comm = cadd(comm, cmul(sH[r + k * n], sX[k + c * n]));
+        for (int k = sLo[r]; k < sHi[r]; k++) comm = cadd(comm, cmul(sH[r + k * n], sX[k + c * n]));
+        for (int k = sLo[c]; k < sHi[c]; k++) {
             const double2 xh = cmul(sX[r + k * n], sH[k + c * n]);
             comm = make_double2(comm.x - xh.x, comm.y - xh.y);
         }
@@ -80,7 +88,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
     for (int k = threadIdx.x; k < nn; k += blockDim.x) {
         const int i = k % n, j = k / n;
         double2 s = make_double2(0, 0);
-        for (int l = 0; l < n; l++) s = cadd(s, cmulc(sU[l + i * n], sY[l + j * n]));
+        for (int l = sLo[i]; l < sHi[i]; l++) s = cadd(s, cmulc(sU[l + i * n], sY[l + j * n]));
         sT[k] = s;
     }
     __syncthreads();
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
     for (int k = threadIdx.x; k < nn; k += blockDim.x) {
         const int i = k % n, j = k / n;
         double2 s = make_double2(0, 0);
-        for (int l = 0; l < n; l++) s = cadd(s, cmul(sT[i + l * n], sU[l + j * n]));
+        for (int l = sLo[j]; l < sHi[j]; l++) s = cadd(s, cmul(sT[i + l * n], sU[l + j * n]));
         const double lam = sE[i] - sE[j];
         double2 den = make_double2(d.x, d.y + lam);
         if (dsmall) den = make_double2(0.0, lam);
@@ -105,16 +113,16 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
     for (int k = threadIdx.x; k < nn; k += blockDim.x) {
         const int i = k % n, j = k / n;
         double2 s = make_double2(0, 0);
-        for (int l = 0; l < n; l++) s = cadd(s, cmul(sU[i + l * n], sY[l + j * n]));
+        for (int l = sLo[i]; l < sHi[i]; l++) s = cadd(s, cmul(sU[i + l * n], sY[l + j * n]));
         sT[k] = s;
     }
     __syncthreads();
     // x'(r, c) = (T U^H)(r, c) on the pattern
     for (int q = threadIdx.x; q < nz; q += blockDim.x) {
         const unsigned w = rc[off + q];
-        const int r = w & 0xFF, c = w >> 8;
+        const int r = sP[w & 0xFF], c = sP[w >> 8];
         double2 s = make_double2(0, 0);
-        for (int l = 0; l < n; l++) {
+        for (int l = sLo[c]; l < sHi[c]; l++) {
             const double2 u = sU[c + l * n];
             s = cadd(s, cmul(sT[r + l * n], make_double2(u.x, -u.y)));
         }
@@ -179,10 +187,17 @@ int heom_jacobi_shift(heom_ctx *c, double *ejac)
     });
 }
 
-int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Complex *rho, heom_solve_info *info)
+}  // extern "C"
+
+namespace {
+
+// The solve, or with bench_reps > 0 a measurement of its two kernels instead:
+// bench[0..1] = seconds per launch of the sector transform and of the apply,
+// bench[2..3] = the transform's algorithmic bytes and complex multiply-adds per launch.
+void jacobi_run(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Complex *rho, heom_solve_info *info,
+                int bench_reps, double *bench)
 {
-    return guarded([&] {
-        require_ctx(c);
+    {
         if (!o || !rho) fail(HEOM_E_ARG, "null argument");
         const int n = c->nrho, nn = n * n;
         if (n > 32) fail(HEOM_E_UNSUPPORTED, "the Jacobi sweep keeps five nrho x nrho matrices in shared memory: nrho <= 32");
@@ -192,7 +207,37 @@ int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double
         const int64_t N = c->lunk + 1;
         std::vector<cd> h(reinterpret_cast<cd *>(rho), reinterpret_cast<cd *>(rho) + c->lunk);
         herm_rdo(c, h.data());
-        std::vector<cd> a = c->hs_host, v;
+        // sectors: connected components of the graph of H, numbered contiguously
+        std::vector<int> comp(n, -1), order;
+        for (int s0 = 0, nc = 0; s0 < n; s0++) {
+            if (comp[s0] >= 0) continue;
+            std::vector<int> stack{s0};
+            comp[s0] = nc;
+            while (!stack.empty()) {
+                const int i = stack.back();
+                stack.pop_back();
+                for (int j = 0; j < n; j++)
+                    if (comp[j] < 0 && (std::abs(c->hs_host[i + (size_t)j * n]) >= kDsmall || std::abs(c->hs_host[j + (size_t)i * n]) >= kDsmall)) {
+                        comp[j] = nc;
+                        stack.push_back(j);
+                    }
+            }
+            nc++;
+        }
+        for (int cc = 0; cc < n; cc++)
+            for (int i = 0; i < n; i++) if (comp[i] == cc) order.push_back(i);   // new number -> state
+        std::vector<uint8_t> perm(n), blo(n), bhi(n);
+        for (int k = 0; k < n; k++) perm[order[k]] = (uint8_t)k;
+        for (int k = 0; k < n; k++) {
+            int lo = k, hi = k + 1;
+            while (lo > 0 && comp[order[lo - 1]] == comp[order[k]]) lo--;
+            while (hi < n && comp[order[hi]] == comp[order[k]]) hi++;
+            blo[k] = (uint8_t)lo; bhi[k] = (uint8_t)hi;
+        }
+        std::vector<cd> hp((size_t)nn);
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++) hp[i + (size_t)j * n] = c->hs_host[order[i] + (size_t)order[j] * n];
+        std::vector<cd> a = hp, v;
         std::vector<double> e;
         herm_eig(n, a, e, v);
         std::vector<void *> tmp;
@@ -209,22 +254,30 @@ int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double
             CK(cudaMalloc((void **)&dU, sizeof(double2) * nn)); tmp.push_back(dU);
             CK(cudaMalloc((void **)&dH, sizeof(double2) * nn)); tmp.push_back(dH);
             CK(cudaMalloc((void **)&dE, sizeof(double) * n)); tmp.push_back(dE);
+            uint8_t *dperm = nullptr;
+            CK(cudaMalloc((void **)&dperm, 3 * (size_t)n)); tmp.push_back(dperm);
+            std::vector<uint8_t> pb(perm);
+            pb.insert(pb.end(), blo.begin(), blo.end());
+            pb.insert(pb.end(), bhi.begin(), bhi.end());
+            CK(cudaMemcpyAsync(dperm, pb.data(), 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
             CK(cudaMemsetAsync(x, 0, sizeof(double2) * N, c->stream));
             CK(cudaMemsetAsync(xn, 0, sizeof(double2) * N, c->stream));
             CK(cudaMemcpyAsync(x, h.data(), sizeof(double2) * c->lunk, cudaMemcpyHostToDevice, c->stream));
             CK(cudaMemcpyAsync(dU, v.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, c->stream));
-            CK(cudaMemcpyAsync(dH, c->hs_host.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dH, hp.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, c->stream));
             CK(cudaMemcpyAsync(dE, e.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
             DevCoef<double> K = ctx_coefs(c).k64;
             fill_gdiag<double>(P, K, gd, 1, c->stream);
             K.gdiag = gd;
-            const size_t smem = sizeof(double2) * 5 * nn + sizeof(double) * n;
+            const size_t smem = sizeof(double2) * 5 * nn + sizeof(double) * n + 3 * (size_t)n;
             if (smem > 48 * 1024)
                 CK(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             auto sweep = [&](double2 *from, double2 *to) {
                 launch_apply<double, false>(P, K, from, y, 1, N, nullptr, c->stream);
                 k_jacobi<<<dim3((unsigned)P.nado, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, from, y, to, gd, dU, dE,
-                                                                                   dH, ejac, n, N);
+                                                                                   dH, dperm, dperm + n, dperm + 2 * n,
+                                                                                   ejac, n, N);
             };
             // ||A x - e_trace|| (solve_jacobi.f90:183-190)
             auto residual = [&](double2 *from) {
@@ -236,6 +289,45 @@ int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double
                 CK(cudaMemcpyAsync(y + c->lunk, last.data(), sizeof(double2), cudaMemcpyHostToDevice, c->stream));
                 return device_norm2(N, y, c->dscratch, c->stream);
             };
+            if (bench_reps > 0) {
+                cudaEvent_t b0, b1, b2;
+                CK(cudaEventCreate(&b0)); CK(cudaEventCreate(&b1)); CK(cudaEventCreate(&b2));
+                sweep(x, xn);
+                CK(cudaEventRecord(b0, c->stream));
+                for (int r = 0; r < bench_reps; r++)
+                    k_jacobi<<<dim3((unsigned)P.nado, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, x, y, xn, gd, dU, dE, dH, dperm,
+                                                                                       dperm + n, dperm + 2 * n, ejac, n, N);
+                CK(cudaEventRecord(b1, c->stream));
+                for (int r = 0; r < bench_reps; r++) launch_apply<double, false>(P, K, x, y, 1, N, nullptr, c->stream);
+                CK(cudaEventRecord(b2, c->stream));
+                CK(cudaEventSynchronize(b2));
+                CK(cudaGetLastError());
+                float m1 = 0, m2 = 0;
+                cudaEventElapsedTime(&m1, b0, b1);
+                cudaEventElapsedTime(&m2, b1, b2);
+                cudaEventDestroy(b0); cudaEventDestroy(b1); cudaEventDestroy(b2);
+                // per ADO: x, A x read and x' written (16 B each per entry) plus the entry's
+                // coordinates (2 B); the per-instance U, H, E and the ADO diagonal come from L2
+                double s2 = 0;
+                for (int k = 0; k < n; k++) s2 += bhi[k] - blo[k];
+                bench[0] = m1 * 1e-3 / bench_reps;
+                bench[1] = m2 * 1e-3 / bench_reps;
+                bench[2] = (double)c->lunk * (3 * 16 + 2) + (double)P.nado * 16;
+                // complex multiply-adds: three products over the blocks (n * sum_i |block(i)|
+                // each) and, per stored entry, the commutator and the extraction
+                double entries_blk = 0;
+                {
+                    std::vector<uint16_t> rcv((size_t)c->lunk);
+                    CK(cudaMemcpy(rcv.data(), c->d_ent_rc, sizeof(uint16_t) * rcv.size(), cudaMemcpyDeviceToHost));
+                    for (uint16_t w : rcv) {
+                        const int r = perm[w & 0xFF], cc = perm[w >> 8];
+                        entries_blk += (double)(bhi[r] - blo[r]) + 2.0 * (bhi[cc] - blo[cc]);
+                    }
+                }
+                bench[3] = (double)P.nado * 3.0 * n * s2 + entries_blk;
+                cleanup();
+                return;
+            }
             // sweeps 50 at a time in one graph: an even count leaves the iterate in x
             constexpr int kChunk = 50;
             cudaGraph_t g = nullptr;
@@ -283,6 +375,30 @@ int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double
         }
         cudaEventDestroy(e0); cudaEventDestroy(e1);
         cleanup();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Complex *rho, heom_solve_info *info)
+{
+    return guarded([&] {
+        require_ctx(c);
+        jacobi_run(c, o, ejac, rho, info, 0, nullptr);
+    });
+}
+
+int heom_bench_jacobi(heom_ctx *c, double ejac, int32_t reps, double *out)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!out || reps < 1) fail(HEOM_E_ARG, "null output or reps < 1");
+        heom_solve_opts o{};
+        o.crit = 1.0;
+        std::vector<cd> rho((size_t)c->lunk, cd(0, 0));
+        jacobi_run(c, &o, ejac, reinterpret_cast<double _Complex *>(rho.data()), nullptr, reps, out);
     });
 }
 

@@ -124,6 +124,7 @@ SIGNATURES = {
     "heom_batch_current_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
     "heom_solve_jacobi": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_double, C.c_void_p, _p(SolveInfo)]),
     "heom_jacobi_shift": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "heom_bench_jacobi": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "heom_model_cf_pattern": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _p(CfTables)]),
     "heom_cf_create": (C.c_int, [C.c_void_p, _p(Tables), _p(CfTables), _p(C.c_void_p)]),
     "heom_cf_destroy": (None, [C.c_void_p]),
@@ -348,6 +349,12 @@ class Context:
         if check:
             _check(rc)
         return rho, info
+
+    def bench_jacobi(self, ejac=0.0, reps=10):
+        """(transform s, apply s, transform bytes, transform complex multiply-adds) per launch."""
+        out = np.zeros(4)
+        _check(lib().heom_bench_jacobi(self.h, float(ejac), reps, out.ctypes.data))
+        return tuple(out.tolist())
 
     def jacobi_shift(self):
         e = C.c_double()

@@ -325,6 +325,11 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
  * vector read once and written once, plus the plan).  No reference counterpart. */
 int heom_cf_bench_apply(heom_cf *cf, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
 
+/* Measurement hook of the Jacobi sweep: out[0], out[1] = seconds per launch of the sector
+ * transform kernel and of the apply (reps launches each), out[2] = the transform's
+ * algorithmic bytes, out[3] = its complex multiply-adds per launch.  ejac <= 0: the rule. */
+int heom_bench_jacobi(heom_ctx *ctx, double ejac, int32_t reps, double *out /* 4 */);
+
 /* Plan statistics of the forward apply (per instance): [0] stored entries + 1, [1] ADOs
  * with entries, [2] pattern classes, [3] coupling records, [4] gather maps, [5] useful
  * gathers (nonzero map halves), [6] same-tier terms, [7] lower-tier (complex-coefficient)

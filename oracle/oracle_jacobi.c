@@ -143,7 +143,10 @@ void orc_jacobi_sweep(const orc_model *m, const orc_jacobi *J, const ozc *x, ozc
     ozc *xp = calloc(m->lunk + 1, sizeof(ozc)), *y = calloc(m->lunk + 1, sizeof(ozc));
     memcpy(xp, x, sizeof(ozc) * m->lunk);
     orc_calc_ax(m, xp, y, 0);
+#pragma omp parallel
+    {
     ozc *X = calloc(n2, sizeof(ozc)), *Y = calloc(n2, sizeof(ozc)), *Z = calloc(n2, sizeof(ozc)), *T = calloc(n2, sizeof(ozc));
+#pragma omp for schedule(dynamic, 16)
     for (int64_t u = 1; u <= m->nunk; u++) {
         int nz = m->nnz_spa[u - 1];
         if (nz == 0) continue;
@@ -168,7 +171,9 @@ void orc_jacobi_sweep(const orc_model *m, const orc_jacobi *J, const ozc *x, ozc
         jac_transform(J, g, Y, Z, T);
         for (int q = 0; q < nz; q++) xn[st + q] = Z[(m->irow_spa[st + q] - 1) + (size_t)(m->icol_spa[st + q] - 1) * n];
     }
-    free(xp); free(y); free(X); free(Y); free(Z); free(T);
+    free(X); free(Y); free(Z); free(T);
+    }
+    free(xp); free(y);
 }
 
 /* solve_jacobi.f90:100-280: rho (lunk) in/out */

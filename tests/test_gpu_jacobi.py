@@ -50,7 +50,7 @@ def test_jacobi_solve_reaches_the_steady_state(name):
     ejac = 2 * ctx.jacobi_shift()
     rho, info = ctx.solve_jacobi(crit=1e-10, maxit0=40000, ejac=ejac)
     assert info.converged and info.resid <= 1e-10
-    ref, _ = ctx.solve_tfqmr(crit=1e-12, maxit0=40000)
+    ref, _ = ctx.solve_tfqmr(crit=1e-12, maxit0=40000, precision=heomq.PREC_FP64_REFINED, max_refine=16)
     assert abs(ctx.current(rho)[0].sum() / ctx.current(ref)[0].sum() - 1) < 1e-8
     if name != "siam_L3":
         return
