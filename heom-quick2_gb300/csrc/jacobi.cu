@@ -29,7 +29,7 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 cmulc(double2 a, double2 b) { return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }  // conj(a) b
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
-// one ADO of one instance per block: blockIdx.x = ADO, blockIdx.y = instance
+// a persistent block walks the ADOs blockIdx.x, blockIdx.x + gridDim.x, ... of instance blockIdx.y
 // States are renumbered so that the connected components of the graph of H (its conserved
 // sectors) are contiguous: H, and with it U, are then block diagonal, and every product below
 // runs over the block [lo(i), hi(i)) of the index it sums against.  perm maps a state to
@@ -47,25 +47,26 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
     double2 *sU = sm, *sH = sm + nn, *sX = sm + 2 * nn, *sY = sm + 3 * nn, *sT = sm + 4 * nn;
     double *sE = reinterpret_cast<double *>(sm + 5 * nn);
     uint8_t *sP = reinterpret_cast<uint8_t *>(sE + n), *sLo = sP + n, *sHi = sLo + n;
-    const int a = blockIdx.x, b = blockIdx.y;
-    const int off = __ldg(P.ado_off + a), nz = __ldg(P.ado_off + a + 1) - off;
-    x += (int64_t)b * vstride + off;
-    y += (int64_t)b * vstride + off;
-    xn += (int64_t)b * vstride + off;
+    const int b = blockIdx.y;
+    x += (int64_t)b * vstride;
+    y += (int64_t)b * vstride;
+    xn += (int64_t)b * vstride;
     U += (int64_t)b * nn;
     H += (int64_t)b * nn;
     E += (int64_t)b * n;
+    // the instance's H, U and E stay in shared memory while the block walks its ADOs
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) { sU[k] = U[k]; sH[k] = H[k]; }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) { sE[k] = E[k]; sP[k] = perm[k]; sLo[k] = blo[k]; sHi[k] = bhi[k]; }
+    for (int a = blockIdx.x; a < P.nado; a += gridDim.x) {
+    const int off = __ldg(P.ado_off + a), nz = __ldg(P.ado_off + a + 1) - off;
     for (int k = threadIdx.x; k < nn; k += blockDim.x) {
-        sU[k] = U[k];
-        sH[k] = H[k];
         sX[k] = make_double2(0, 0);
         sY[k] = make_double2(0, 0);
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) { sE[k] = E[k]; sP[k] = perm[k]; sLo[k] = blo[k]; sHi[k] = bhi[k]; }
     __syncthreads();
     for (int q = threadIdx.x; q < nz; q += blockDim.x) {
         const unsigned w = rc[off + q];
-        sX[sP[w & 0xFF] + sP[w >> 8] * n] = x[q];
+        sX[sP[w & 0xFF] + sP[w >> 8] * n] = x[off + q];
     }
     __syncthreads();
     const double2 g = gdiag[(int64_t)b * P.nado + a];
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
             const double2 xh = cmul(sX[r + k * n], sH[k + c * n]);
             comm = make_double2(comm.x - xh.x, comm.y - xh.y);
         }
-        const double2 v = cadd(cadd(cmul(d, x[q]), y[q]), make_double2(-comm.y, comm.x));
+        const double2 v = cadd(cadd(cmul(d, x[off + q]), y[off + q]), make_double2(-comm.y, comm.x));
         sY[r + c * n] = v;
     }
     __syncthreads();
@@ -103,8 +104,8 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
         if (dsmall) den = make_double2(0.0, lam);
         double2 f = make_double2(0, 0);
         if (!dsmall || fabs(lam) > kDpico) {
-            const double m2 = den.x * den.x + den.y * den.y;
-            f = make_double2(den.x / m2, -den.y / m2);
+            const double inv = 1.0 / (den.x * den.x + den.y * den.y);
+            f = make_double2(den.x * inv, -den.y * inv);
         }
         sY[k] = cmul(s, f);
     }
@@ -126,7 +127,9 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(DevPlan P, const uint16_
             const double2 u = sU[c + l * n];
             s = cadd(s, cmul(sT[r + l * n], make_double2(u.x, -u.y)));
         }
-        xn[q] = s;
+        xn[off + q] = s;
+    }
+    __syncthreads();   // the next ADO clears sX and sY
     }
 }
 
@@ -273,9 +276,14 @@ void jacobi_run(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Comp
             const size_t smem = sizeof(double2) * 5 * nn + sizeof(double) * n + 3 * (size_t)n;
             if (smem > 48 * 1024)
                 CK(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            // a persistent grid: as many resident blocks as the SMs hold, each walking ADOs
+            int nsm = 0, per_sm = 0;
+            CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi, kJacThreads, smem));
+            const unsigned jgrid = (unsigned)std::max(1, std::min(P.nado, nsm * std::max(1, per_sm)));
             auto sweep = [&](double2 *from, double2 *to) {
                 launch_apply<double, false>(P, K, from, y, 1, N, nullptr, c->stream);
-                k_jacobi<<<dim3((unsigned)P.nado, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, from, y, to, gd, dU, dE,
+                k_jacobi<<<dim3(jgrid, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, from, y, to, gd, dU, dE,
                                                                                    dH, dperm, dperm + n, dperm + 2 * n,
                                                                                    ejac, n, N);
             };
@@ -295,7 +303,7 @@ void jacobi_run(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Comp
                 sweep(x, xn);
                 CK(cudaEventRecord(b0, c->stream));
                 for (int r = 0; r < bench_reps; r++)
-                    k_jacobi<<<dim3((unsigned)P.nado, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, x, y, xn, gd, dU, dE, dH, dperm,
+                    k_jacobi<<<dim3(jgrid, 1), kJacThreads, smem, c->stream>>>(P, c->d_ent_rc, x, y, xn, gd, dU, dE, dH, dperm,
                                                                                        dperm + n, dperm + 2 * n, ejac, n, N);
                 CK(cudaEventRecord(b1, c->stream));
                 for (int r = 0; r < bench_reps; r++) launch_apply<double, false>(P, K, x, y, 1, N, nullptr, c->stream);
