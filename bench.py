@@ -352,7 +352,7 @@ def run_gb300(args, ws, rank, local, dist):
     return 0
 
 
-DOS_METRIC = "HEOM spectral-function frequencies/s (corrfunc frequency domain, FP64)"
+DOS_METRIC = "HEOM spectral-function frequencies/s (corrfunc frequency domain): mixed vs FP64 GPU"
 DOS_WORKLOAD = ("spectral function A(w) of a_(1,up) of the serial double quantum dot nd=16, tier L=4 "
                 "(correlation-function pattern: 670672 entries per component), steady state at V=0.8, "
                 "two FP64 TFQMR solves per frequency to ||b - L x|| <= crit")
@@ -435,8 +435,9 @@ def run_dos(args, ws, rank, local, dist):
         print(json.dumps({"profile_cf": True, "instances": 2 * nf, "apply_us": sec * 1e6, "alg_bytes": alg}), flush=True)
         return 0
     rho, sinfo = ctx.solve_tfqmr(crit=1e-10, precision=heomq.PREC_MIXED)
+    mixed = heomq.PREC_MIXED
     for _ in range(args.warmup):
-        cf.dos(rho, freqs, crit=DOS_CRIT)
+        cf.dos(rho, freqs, crit=DOS_CRIT, precision=mixed)
     clk = clocks_start() if rank == 0 else None
     if dist:
         dist.barrier()
@@ -444,7 +445,7 @@ def run_dos(args, ws, rank, local, dist):
     dev_s, wall_s, launches, infos = 0.0, [], 0, []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        out, info = cf.dos(rho, freqs, crit=DOS_CRIT)
+        out, info = cf.dos(rho, freqs, crit=DOS_CRIT, precision=mixed)
         wall_s.append(time.perf_counter() - t0)
         dev_s += info.seconds
         launches += info.launches
@@ -456,6 +457,9 @@ def run_dos(args, ws, rank, local, dist):
     t_step = max_over_ranks(dev_s / args.steps, dist, device="cuda")
     value = ws * nf / t_step
     e2e_value = ws * nf / max_over_ranks(statistics.median(wall_s), dist, device="cuda")
+    # the FP64 reference algorithm beside (one step, after the timed region)
+    out64, info64 = cf.dos(rho, freqs, crit=DOS_CRIT)
+    dos_err = float(np.max(np.abs(out[:, 0] - out64[:, 0]) / np.abs(out64[:, 0])))
     sec, alg = cf.bench_apply(nbatch=2 * nf, reps=10)
     peak, peak_kind = measured_peak_hbm()
     achieved = alg / sec / 1e9
@@ -464,7 +468,7 @@ def run_dos(args, ws, rank, local, dist):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        applies = 2 * infos[-1].iters
+        applies = 2 * info64.iters
         t_apply, v = cpu_dos_sample(nthreads, applies, napply=20)
         cpu = {"value": v, "unit": "freqs/s", "cores": nthreads, "kind": "port",
                "sample": f"20 applies of the C restatement of calc_ax_cf_spa_omp (OpenMP over ADOs, {t_apply * 1e3:.1f} ms "
@@ -475,8 +479,12 @@ def run_dos(args, ws, rank, local, dist):
         line = {
             "metric": DOS_METRIC, "value": value, "unit": "freqs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32x2+f64", "data": "synthetic",
             "config": {"workload": DOS_WORKLOAD, "freqs_per_step": nf, "freq_range_eV": [-3.0, 3.0], "crit": DOS_CRIT,
+                       "solver": "FP32x2 fused inner TFQMR, FP64 residual refinement",
+                       "fp64": {"freqs_per_s": ws * nf / info64.seconds, "applies_per_solve_max": info64.iters,
+                                "resid_max": info64.resid},
+                       "speedup_mixed_vs_fp64": info64.seconds / t_step, "dos_rel_diff_mixed_vs_fp64": dos_err,
                        "solves_per_step": 2 * nf, "applies_per_solve_max": infos[-1].iters,
                        "resid_max": infos[-1].resid, "converged": bool(infos[-1].converged),
                        "l2": f"inputs larger than L2: {2 * nf} instances x 12 vectors x {2 * cf.lunkcf * 16 / 1e6:.1f} MB",
@@ -484,7 +492,8 @@ def run_dos(args, ws, rank, local, dist):
                        "spectrum_min": float(out[:, 1:3].min()), "steady_resid": sinfo.resid},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": f"k_apply_cf<FP64> over {2 * nf} instances", "kernel_us": sec * 1e6,
+                         "kernel": f"k_apply_cf<FP64> over {2 * nf} instances (the FP64 residual and reference path)",
+                         "kernel_us": sec * 1e6,
                          "alg_bytes_per_launch": alg,
                          "note": "FP64-pipe bound like the steady FP64 apply (GB300 FP64 = 1/64 of FP32): profiles/" + prof},
             "cpu_baseline": cpu,

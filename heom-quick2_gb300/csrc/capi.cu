@@ -256,11 +256,12 @@ void drandn_stream(int64_t n, std::vector<double> &out)
 }
 
 template <typename T>
-void upload_rt_to(heom_ctx *c, typename Num<T>::V *dst, int64_t n)
+void upload_rt_to(heom_ctx *c, typename Num<T>::V *dst, int64_t n, const double *src = nullptr)
 {
     using V = typename Num<T>::V;
+    if (!src) src = c->rt_host.data();
     std::vector<V> rt(n);
-    for (int64_t i = 0; i < n; i++) rt[i] = Num<T>::store_host(Num<T>::from_d(c->rt_host[2 * i], c->rt_host[2 * i + 1]));
+    for (int64_t i = 0; i < n; i++) rt[i] = Num<T>::store_host(Num<T>::from_d(src[2 * i], src[2 * i + 1]));
     CK(cudaMemcpyAsync(dst, rt.data(), sizeof(V) * n, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
 }
@@ -404,10 +405,10 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   int nlim, int max_rounds, bool stall_exit, bool &stalled,
                   int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
                   const std::function<void(const double2 *, double2 *)> &residual,
-                  const std::function<void(const double2 *)> &batch_norms)
+                  const std::function<void(const double2 *)> &batch_norms,
+                  const DevPlan &PV, int64_t N, const double *rt)
 {
     constexpr int kInnerChunk = 25;   // 50 applies between residual checks, as in the reference driver
-    const int64_t N = c->lunk + 1;
     const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-10);
     InnerWork<T> W;
     inner_alloc<T>(W, nbatch, N, c->stream);
@@ -421,16 +422,17 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         if (gd) cudaFree(gd);
     };
     try {
-        upload_rt_to<T>(c, W.rt, N);
-        DevCoef<T> KR = regularised<T>(c, KT);
+        upload_rt_to<T>(c, W.rt, N, rt);
+        // with a given right-hand side the operator is used as it is; the steady problem
+        // (rhs == nullptr) is solved on the regularised operator
+        DevCoef<T> KI = rhs ? KT : regularised<T>(c, KT);
         // per-instance ADO diagonals, so the inner applies do no FP64 arithmetic
-        CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * std::max<int64_t>(1, (int64_t)c->dfwd.view.nado * nbatch)));
-        fill_gdiag<T>(c->dfwd.view, KR, gd, nbatch, c->stream);
-        KR.gdiag = gd;
+        CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * std::max<int64_t>(1, (int64_t)PV.nado * nbatch)));
+        fill_gdiag<T>(PV, KI, gd, nbatch, c->stream);
+        KI.gdiag = gd;
         aux++;
-        const DevCoef<T> KI = rhs ? KT : KR;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        inner_chunk<T>(W, c->dfwd.view, KI, kInnerChunk, c->stream);
+        inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
         CK(cudaStreamEndCapture(c->stream, &graph));
         CK(cudaGraphInstantiate(&gexec, graph, 0));
         std::vector<InnerState> st(nbatch);
@@ -484,6 +486,17 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     } catch (...) { release(); throw; }
     release();
 }
+
+#define HEOM_MIXED_ROUNDS(T)                                                                                       \
+    template void mixed_rounds<T>(heom_ctx *, const heom_solve_opts &, double2 *, int, int64_t, const double2 *,     \
+                                  const DevCoef<double> &, const DevCoef<T> &, double2 *, std::vector<double> &, int, \
+                                  int, bool, bool &, int &, int &, bool &, int &, int64_t &, int64_t &,               \
+                                  const std::function<void(const double2 *, double2 *)> &,                            \
+                                  const std::function<void(const double2 *)> &, const DevPlan &, int64_t,             \
+                                  const double *);
+HEOM_MIXED_ROUNDS(DF)
+HEOM_MIXED_ROUNDS(double)
+#undef HEOM_MIXED_ROUNDS
 
 // Solve A x = rhs (rhs = e_trace when rhs == nullptr) for nbatch instances, in FP64 or
 // mixed precision.  x: device FP64, nbatch vectors with stride vstride (vstride >= lunk+1),
@@ -551,20 +564,23 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             bool stalled = false, unused = false;
             if (o.precision == HEOM_PREC_MIXED)
                 mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, k64, K.kdf, r64, norms, nlim, o.max_refine, true, stalled,
-                                 total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
+                                 total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
+                                 c->dfwd.view, N, c->rt_host.data());
             else if (o.precision == HEOM_PREC_FP64_REFINED)
                 mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim, o.max_refine, false, unused,
-                                     total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
+                                     total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
+                                 c->dfwd.view, N, c->rt_host.data());
             else if (o.precision == HEOM_PREC_MIXED_FP32)
                 mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, k64, K.k32, r64, norms, nlim, o.max_refine, true, stalled,
-                                    total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms);
+                                    total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
+                                 c->dfwd.view, N, c->rt_host.data());
             else fail(HEOM_E_ARG, "unknown precision");
             if (stalled && !converged) {
                 // the remaining rounds with FP64 inner solves on the same regularised operator
                 int more = 0;
                 mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim,
                                      std::max(1, o.max_refine - info.refinements), false, unused, total_iters, last_ierr,
-                                     converged, more, info.launches, aux, residual, batch_norms);
+                                     converged, more, info.launches, aux, residual, batch_norms, c->dfwd.view, N, c->rt_host.data());
                 info.refinements += more;
             }
         }

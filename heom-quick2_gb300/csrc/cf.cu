@@ -136,14 +136,18 @@ struct CfBatchResult {
     int64_t launches = 0;
 };
 
-// FP64 batched TFQMR of L(omega_b) x_b = rhs[rid_b] from x = 0, tolerance 1e-3 crit, true
-// residual test ||b - L x|| <= crit (solve_cf_tfqmr_spa.f90:56-60, 262-290)
+// Solves L(omega_b) x_b = rhs[rid_b] from x = 0 for every instance b.
+// FP64 (the reference algorithm): batched TFQMR with tolerance 1e-3 crit and the true
+// residual test ||b - L x|| <= crit (solve_cf_tfqmr_spa.f90:56-60, 262-290).
+// MIXED: FP64 residuals refined by fused FP32x2 inner TFQMR solves (mixed_rounds) on the
+// operator itself, which has no null space for omega != 0; FP64 inner solves take over for
+// instances whose round fails to halve the residual.
 void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::vector<int> &rid,
-                    const std::vector<std::vector<cd>> &rhs, double crit, int maxit0, CfBatchResult &res)
+                    const std::vector<std::vector<cd>> &rhs, double crit, int maxit0, int precision, CfBatchResult &res)
 {
     heom_ctx *c = cf->ctx;
     const int nb = (int)omega.size();
-    const int64_t L = cf->lunkcf, N = 2 * L + 1;
+    const int64_t L = cf->lunkcf, N = 2 * L + 1, vs = (N + 63) / 64 * 64;
     const int nz0 = cf->nnzcf[0];
     const int nlim = std::max(1, maxit0 / 2);
     res = CfBatchResult();
@@ -154,32 +158,27 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
     CK(cudaMemcpyAsync(cf->d_omega, omega.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
     std::vector<void *> tmp;
     auto cleanup = [&] { for (void *p : tmp) cudaFree(p); tmp.clear(); };
+    auto dmalloc = [&](size_t bytes) { void *p = nullptr; CK(cudaMalloc(&p, bytes)); tmp.push_back(p); return p; };
     TfqWork<double> W;
     try {
-        tfq_alloc<double>(W, nb, N, c->stream);
-        std::vector<double2> rt(N);
-        for (int64_t i = 0; i < N; i++) rt[i] = make_double2(cf->rt_host[2 * i], cf->rt_host[2 * i + 1]);
-        CK(cudaMemcpyAsync(W.rt, rt.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
-        // right-hand sides: each distinct vector uploaded once, then copied per instance
-        double2 *drhs = nullptr;
-        CK(cudaMalloc((void **)&drhs, sizeof(double2) * (size_t)N * rhs.size()));
-        tmp.push_back(drhs);
-        CK(cudaMemsetAsync(drhs, 0, sizeof(double2) * (size_t)N * rhs.size(), c->stream));
+        // B: the right-hand sides, X: the solutions, R: residual scratch (stride vs)
+        double2 *B = (double2 *)dmalloc(sizeof(double2) * (size_t)vs * nb);
+        double2 *X = (double2 *)dmalloc(sizeof(double2) * (size_t)vs * nb);
+        double2 *R = (double2 *)dmalloc(sizeof(double2) * (size_t)vs * nb);
+        CK(cudaMemsetAsync(B, 0, sizeof(double2) * (size_t)vs * nb, c->stream));
+        CK(cudaMemsetAsync(X, 0, sizeof(double2) * (size_t)vs * nb, c->stream));
+        double2 *drhs = (double2 *)dmalloc(sizeof(double2) * (size_t)N * rhs.size());
         for (size_t k = 0; k < rhs.size(); k++)
             CK(cudaMemcpyAsync(drhs + k * N, rhs[k].data(), sizeof(double2) * 2 * L, cudaMemcpyHostToDevice, c->stream));
         for (int b = 0; b < nb; b++)
-            CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, drhs + (size_t)rid[b] * N, sizeof(double2) * N,
+            CK(cudaMemcpyAsync(B + (int64_t)b * vs, drhs + (size_t)rid[b] * N, sizeof(double2) * 2 * L,
                                cudaMemcpyDeviceToDevice, c->stream));
         // per-instance parameter arrays (the kernels index H values and lead shifts by
         // instance): the context's single set replicated nb times
         DevCoef<double> K = cf_coef(cf);
         const DevPlan P = cf->dplan.view;
-        double2 *hv = nullptr;
-        double *es = nullptr;
-        CK(cudaMalloc((void **)&hv, sizeof(double2) * (size_t)std::max(1, P.nh) * nb));
-        tmp.push_back(hv);
-        CK(cudaMalloc((void **)&es, sizeof(double) * 4 * (size_t)nb));
-        tmp.push_back(es);
+        double2 *hv = (double2 *)dmalloc(sizeof(double2) * (size_t)std::max(1, P.nh) * nb);
+        double *es = (double *)dmalloc(sizeof(double) * 4 * (size_t)nb);
         double es_host[4];
         CK(cudaMemcpyAsync(es_host, c->es64, sizeof es_host, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -192,59 +191,98 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
         K.hval = hv;
         K.eshift = es;
         // per-instance ADO diagonals: keeps the lead-shift sums out of the per-entry work
-        double2 *gd = nullptr;
-        CK(cudaMalloc((void **)&gd, sizeof(double2) * (size_t)P.nado * nb));
-        tmp.push_back(gd);
+        double2 *gd = (double2 *)dmalloc(sizeof(double2) * (size_t)P.nado * nb);
         fill_gdiag<double>(P, K, gd, nb, c->stream);
         K.gdiag = gd;
-        const int64_t vs = W.vstride;
         cudaStream_t s = c->stream;
         ApplyFn<double> op = [P, K, nb, vs, s](const double2 *x, double2 *y, const int *act) {
             launch_apply_cf(P, K, x, y, nb, vs, act, s);
         };
-        // B: the right-hand sides; X: the solutions, built up over restarts
-        double2 *B = nullptr, *X = nullptr;
-        CK(cudaMalloc((void **)&B, sizeof(double2) * (size_t)vs * nb));
-        tmp.push_back(B);
-        CK(cudaMalloc((void **)&X, sizeof(double2) * (size_t)vs * nb));
-        tmp.push_back(X);
-        CK(cudaMemcpyAsync(B, W.b, sizeof(double2) * (size_t)vs * nb, cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemsetAsync(X, 0, sizeof(double2) * (size_t)vs * nb, c->stream));
-        // true residuals B - L X (the reference's final norm) into W.s and res.resid
+        // true residuals B - L X (the reference's final norm) into R and res.resid
         auto residuals = [&] {
-            op(X, W.s, nullptr);
-            vec_axpby<double>(vs * nb, W.s, 1.0, B, -1.0, W.s, c->stream);
+            op(X, R, nullptr);
+            vec_axpby<double>(vs * nb, R, 1.0, B, -1.0, R, c->stream);
             double worst = 0;
             for (int b = 0; b < nb; b++) {
-                res.resid[b] = device_norm2(N, W.s + (int64_t)b * vs, c->dscratch, c->stream);
+                res.resid[b] = device_norm2(N, R + (int64_t)b * vs, c->dscratch, c->stream);
                 worst = std::max(worst, res.resid[b]);
             }
             res.launches += 2 + nb;
             return worst;
         };
-        // The reference runs one TFQMR and reports whatever it reached.  TFQMR can stop early
-        // on an exact zero of rho or sigma (ierr 8), which happens on small hierarchies whose
-        // Krylov space closes, so unconverged instances restart from their residual: every
-        // round solves L d = B - L X from d = 0 and adds d to X; converged instances leave at
-        // the round's first residual test.
-        int total = 0;
-        for (int round = 0; round < 8 && total < 2 * nlim; round++) {
-            if (round > 0) CK(cudaMemcpyAsync(W.b, W.s, sizeof(double2) * (size_t)vs * nb, cudaMemcpyDeviceToDevice, c->stream));
-            tfq_start<double>(W, crit * 1e-3, nlim, crit, 0.0, 0, c->stream);
-            int it = 0;
-            run_tfqmr64(c, W, op, nlim, it, res.launches);
-            vec_axpby<double>(vs * nb, X, 1.0, X, 1.0, W.x, c->stream);
-            std::vector<TfqState> st(nb);
-            CK(cudaMemcpyAsync(st.data(), W.st, sizeof(TfqState) * nb, cudaMemcpyDeviceToHost, c->stream));
-            CK(cudaStreamSynchronize(c->stream));
-            int axb = 0;
-            res.ierr = 0;   // of the last round
-            for (auto &sv : st) { axb = std::max(axb, sv.axb); res.ierr = std::max(res.ierr, sv.ierr); }
-            total += axb;
-            res.launches += kTfqStartLaunches + 2;
-            if (residuals() <= crit) break;
+        if (precision == HEOM_PREC_MIXED) {
+            DevCoef<DF> KD = cf->dplan.coef<DF>();
+            float4 *hvd = (float4 *)dmalloc(sizeof(float4) * (size_t)std::max(1, P.nh) * nb);
+            for (int b = 0; b < nb; b++)
+                CK(cudaMemcpyAsync(hvd + (size_t)b * P.nh, c->hvaldf, sizeof(float4) * P.nh, cudaMemcpyDeviceToDevice, c->stream));
+            KD.hval = hvd;
+            KD.eshift = es;
+            KD.h_real = c->h_real;
+            KD.trace_on = 0;
+            KD.cf_omega = cf->d_omega;
+            KD.cf_half = L;
+            heom_solve_opts mo{};
+            mo.crit = crit;
+            mo.maxit0 = maxit0;
+            std::vector<double> norms(nb, 0.0);
+            std::function<void(const double2 *, double2 *)> residual = [&](const double2 *xx, double2 *r) {
+                op(xx, r, nullptr);
+                vec_axpby<double>(vs * nb, r, 1.0, B, -1.0, r, c->stream);
+            };
+            std::function<void(const double2 *)> batch_norms = [&](const double2 *v) {
+                for (int b = 0; b < nb; b++) norms[b] = device_norm2(N, v + (int64_t)b * vs, c->dscratch, c->stream);
+            };
+            bool stalled = false, conv = false, unused = false;
+            int total = 0, ierr = 0, rounds = 0, more = 0;
+            int64_t aux = 0;
+            mixed_rounds<DF>(c, mo, X, nb, vs, B, K, KD, R, norms, nlim, 8, true, stalled, total, ierr, conv, rounds,
+                             res.launches, aux, residual, batch_norms, P, N, cf->rt_host.data());
+            if (stalled && !conv)
+                mixed_rounds<double>(c, mo, X, nb, vs, B, K, K, R, norms, nlim, 8, false, unused, total, ierr, conv, more,
+                                     res.launches, aux, residual, batch_norms, P, N, cf->rt_host.data());
+            res.iters = total;
+            res.ierr = ierr;
+            res.launches += aux;
+            residuals();
+        } else {
+            tfq_alloc<double>(W, nb, N, c->stream);
+            std::vector<double2> rt(N);
+            for (int64_t i = 0; i < N; i++) rt[i] = make_double2(cf->rt_host[2 * i], cf->rt_host[2 * i + 1]);
+            CK(cudaMemcpyAsync(W.rt, rt.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, c->stream));
+            ApplyFn<double> opw = [P, K, nb, s, &W](const double2 *x, double2 *y, const int *act) {
+                launch_apply_cf(P, K, x, y, nb, W.vstride, act, s);
+            };
+            for (int b = 0; b < nb; b++)
+                CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, B + (int64_t)b * vs, sizeof(double2) * N,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+            // The reference runs one TFQMR and reports whatever it reached.  TFQMR can stop early
+            // on an exact zero of rho or sigma (ierr 8), which happens on small hierarchies whose
+            // Krylov space closes, so unconverged instances restart from their residual: every
+            // round solves L d = B - L X from d = 0 and adds d to X; converged instances leave at
+            // the round's first residual test.
+            int total = 0;
+            for (int round = 0; round < 8 && total < 2 * nlim; round++) {
+                if (round > 0)
+                    for (int b = 0; b < nb; b++)
+                        CK(cudaMemcpyAsync(W.b + (int64_t)b * W.vstride, R + (int64_t)b * vs, sizeof(double2) * N,
+                                           cudaMemcpyDeviceToDevice, c->stream));
+                tfq_start<double>(W, crit * 1e-3, nlim, crit, 0.0, 0, c->stream);
+                int it = 0;
+                run_tfqmr64(c, W, opw, nlim, it, res.launches);
+                for (int b = 0; b < nb; b++)
+                    vec_axpby<double>(N, X + (int64_t)b * vs, 1.0, X + (int64_t)b * vs, 1.0, W.x + (int64_t)b * W.vstride, c->stream);
+                std::vector<TfqState> st(nb);
+                CK(cudaMemcpyAsync(st.data(), W.st, sizeof(TfqState) * nb, cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+                int axb = 0;
+                res.ierr = 0;   // of the last round
+                for (auto &sv : st) { axb = std::max(axb, sv.axb); res.ierr = std::max(res.ierr, sv.ierr); }
+                total += axb;
+                res.launches += kTfqStartLaunches + 2 * nb;
+                if (residuals() <= crit) break;
+            }
+            res.iters = total;
         }
-        res.iters = total;
         for (int b = 0; b < nb; b++) {
             CK(cudaMemcpyAsync(res.xh0.data() + (size_t)b * nz0, X + (int64_t)b * vs, sizeof(double2) * nz0,
                                cudaMemcpyDeviceToHost, c->stream));
@@ -404,7 +442,8 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
         if (!rho || !dfreq || !o || nfreq < 1) fail(HEOM_E_ARG, "null argument or no frequency");
         if (isgnb != 1 && isgnb != 2) fail(HEOM_E_ARG, "isgnb must be 1 or 2");
         if (isgnw != 1 && isgnw != 2) fail(HEOM_E_ARG, "isgnw must be 1 or 2");
-        if (o->precision != HEOM_PREC_FP64) fail(HEOM_E_UNSUPPORTED, "correlation-function solves run in FP64");
+        if (o->precision != HEOM_PREC_FP64 && o->precision != HEOM_PREC_MIXED)
+            fail(HEOM_E_UNSUPPORTED, "correlation-function solves run in FP64 or MIXED precision");
         if (info) *info = heom_solve_info{};
         const int n = cf->nrho, nz0 = cf->nnzcf[0];
         std::vector<std::vector<cd>> rhs(1);
@@ -417,7 +456,7 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
                 std::vector<double> w(nb);
                 for (int k = 0; k < nb; k++) w[k] = isgnw == 1 ? dfreq[f0 + k] : -dfreq[f0 + k];
                 CfBatchResult r;
-                cf_solve_batch(cf, w, std::vector<int>(nb, 0), rhs, o->crit, o->maxit0, r);
+                cf_solve_batch(cf, w, std::vector<int>(nb, 0), rhs, o->crit, o->maxit0, o->precision, r);
                 for (int k = 0; k < nb; k++) {
                     std::vector<cd> m;
                     if (zouth) {
@@ -445,7 +484,8 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
     return guarded([&] {
         require_cf(cf);
         if (!rho || !freq_ev || !o || !out || nfreq < 1) fail(HEOM_E_ARG, "null argument or no frequency");
-        if (o->precision != HEOM_PREC_FP64) fail(HEOM_E_UNSUPPORTED, "correlation-function solves run in FP64");
+        if (o->precision != HEOM_PREC_FP64 && o->precision != HEOM_PREC_MIXED)
+            fail(HEOM_E_UNSUPPORTED, "correlation-function solves run in FP64 or MIXED precision");
         if (info) *info = heom_solve_info{};
         const int nz0 = cf->nnzcf[0];
         // instance 2k: isgnb = 2, isgnw = 2 (C_{B^dag B}); 2k+1: isgnb = 1, isgnw = 1 (C_{B B^dag})
@@ -465,7 +505,7 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
                     w[2 * k + 1] = wi; rid[2 * k + 1] = 1;
                 }
                 CfBatchResult r;
-                cf_solve_batch(cf, w, rid, rhs, o->crit, o->maxit0, r);
+                cf_solve_batch(cf, w, rid, rhs, o->crit, o->maxit0, o->precision, r);
                 for (int k = 0; k < nf; k++) {
                     cd tr[2];
                     for (int h = 0; h < 2; h++) {

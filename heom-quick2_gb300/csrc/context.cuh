@@ -58,6 +58,19 @@ double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b);
 // Batched FP64 TFQMR iterations until every instance of W has finished (graph-captured
 // chunks on the context's stream); iters: iterations launched.
 void run_tfqmr64(heom_ctx *c, TfqWork<double> &W, const ApplyFn<double> &apply, int nlim, int &iters, int64_t &launches);
+// Mixed-precision refinement of A x = rhs (rhs == nullptr: the steady problem on the
+// regularised operator) for nbatch instances of N elements on the plan PV: rounds of FP64
+// residual (residual(x, r64)), per-instance norms (batch_norms), and a fused inner TFQMR in
+// the number type T on rhs / ||rhs||, until every norm is <= o.crit.  rt: the shadow vector
+// (2 N reals).
+template <typename T>
+void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, const double2 *rhs,
+                  const DevCoef<double> &K64, const DevCoef<T> &KT, double2 *r64, std::vector<double> &norms,
+                  int nlim, int max_rounds, bool stall_exit, bool &stalled,
+                  int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
+                  const std::function<void(const double2 *, double2 *)> &residual,
+                  const std::function<void(const double2 *)> &batch_norms,
+                  const DevPlan &PV, int64_t N, const double *rt);
 // The reference's shadow-vector stream (tfqmr_double/drandn.f90, SEED = 1): n reals.
 void drandn_host(int64_t n, std::vector<double> &out);
 }  // namespace heom

@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(NTF) k_in_init_fin(InnerWork<T> W, double crit
 }
 
 // B: u1 = A w + beta u2, the pending x / d updates, y = w + beta y2, v = u1 + beta (u2 + beta v)
-template <typename T, bool REG>
+template <typename T, bool REG, bool CF = false>
 __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     FUSED_SETUP
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
-        const A aw = apply_entry<T, false, REG>(P, C, W.w + o, t, b);
+        const A aw = apply_entry<T, false, REG, CF>(P, C, W.w + o, t, b);
         const InnerCoef<T> &k = W.cf[b];
         const A u2 = N::load(W.u2[o + t]), vo = N::load(W.v[o + t]), yo = N::load(W.y[o + t]);
         const A u1 = N::add(aw, N::scale(u2, k.beta));
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(NTF) k_in_b_fin(InnerWork<T> W)
 }
 
 // A: u2 = u1 - alpha A v, w1 = w - alpha u1, w = w1 - alpha u2
-template <typename T, bool REG>
+template <typename T, bool REG, bool CF = false>
 __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     FUSED_SETUP
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
-        const A av = apply_entry<T, false, REG>(P, C, W.v + o, t, b);
+        const A av = apply_entry<T, false, REG, CF>(P, C, W.v + o, t, b);
         const typename N::S al = W.cf[b].alpha;
         const A u1 = N::load(W.u1[o + t]);
         const A u2 = N::sub(u1, N::scale(av, al));
@@ -315,7 +315,7 @@ __global__ void k_in_x(InnerWork<T> W)
 }
 
 // partial ||b - A xs||^2
-template <typename T, bool REG>
+template <typename T, bool REG, bool CF = false>
 __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     using N = Num<T>;
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, Inner
     for (int e = 0; e < kEPT; e++) {
         const int64_t t = t0 + (int64_t)e * NT;
         if (t >= W.N) break;
-        const A r = N::norm(N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG>(P, C, xc + o, t, b)));
+        const A r = N::norm(N::sub(N::load(W.b[o + t]), apply_entry<T, false, REG, CF>(P, C, xc + o, t, b)));
         ee.add(r, r);
     }
     const typename WarpAcc<T>::R ws[1] = {ee.warp_sum()};
@@ -408,11 +408,13 @@ void inner_time(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int reps
     Q.order = nullptr;
     k_in_fill<T><<<g, NT, 0, s>>>(W);
     auto run_b = [&] {
-        if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) k_in_b<T, false, true><<<g, NT, 0, s>>>(Q, C, W);
+        else if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_b<T, false><<<g, NT, 0, s>>>(Q, C, W);
     };
     auto run_a = [&] {
-        if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) k_in_a<T, false, true><<<g, NT, 0, s>>>(Q, C, W);
+        else if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_a<T, false><<<g, NT, 0, s>>>(Q, C, W);
     };
     cudaEvent_t e0, e1;
@@ -488,15 +490,18 @@ void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int ite
     DevPlan Q = P;
     Q.order = nullptr;   // entry order: coalesced epilogue access
     for (int i = 0; i < iters; i++) {
-        if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) k_in_b<T, false, true><<<g, NT, 0, s>>>(Q, C, W);
+        else if (C.reg) k_in_b<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_b<T, false><<<g, NT, 0, s>>>(Q, C, W);
         k_in_b_fin<T><<<nb, NTF, 0, s>>>(W);
-        if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) k_in_a<T, false, true><<<g, NT, 0, s>>>(Q, C, W);
+        else if (C.reg) k_in_a<T, true><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_a<T, false><<<g, NT, 0, s>>>(Q, C, W);
         k_in_a_fin<T><<<nb, NTF, 0, s>>>(W);
     }
     k_in_x<T><<<g, NT, 0, s>>>(W);
-    if (C.reg) k_in_chk<T, true><<<g, NT, 0, s>>>(Q, C, W);
+    if (C.cf_half) k_in_chk<T, false, true><<<g, NT, 0, s>>>(Q, C, W);
+    else if (C.reg) k_in_chk<T, true><<<g, NT, 0, s>>>(Q, C, W);
     else k_in_chk<T, false><<<g, NT, 0, s>>>(Q, C, W);
     k_in_chk_fin<T><<<nb, NTF, 0, s>>>(W);
 }

@@ -484,26 +484,26 @@ class CorrFunc:
                                      ya.ctypes.data, yb.ctypes.data))
         return ya, yb
 
-    def solve_cf_tfqmr_spa(self, rho, isgnb, isgnw, dfreq, crit=1e-10, maxit0=20000):
+    def solve_cf_tfqmr_spa(self, rho, isgnb, isgnw, dfreq, crit=1e-10, maxit0=20000, precision=PREC_FP64):
         """RDO blocks (zouth, zouta), each (nfreq, nrho, nrho), of the solves at every dfreq."""
         w = np.ascontiguousarray(np.atleast_1d(dfreq), dtype=np.float64)
         rho = _c128(rho, self.ctx.lunk)
         n = self.nrho
         zh = np.zeros(w.size * n * n, dtype=np.complex128)
         za = np.zeros(w.size * n * n, dtype=np.complex128)
-        o = SolveOpts(crit=crit, maxit0=maxit0, precision=PREC_FP64)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision)
         info = SolveInfo()
         _check(lib().heom_cf_solve(self.h, rho.ctypes.data, int(isgnb), int(isgnw), w.size, w.ctypes.data, C.byref(o),
                                    zh.ctypes.data, za.ctypes.data, C.byref(info)))
         # column-major nrho x nrho blocks
         return zh.reshape(w.size, n, n).transpose(0, 2, 1), za.reshape(w.size, n, n).transpose(0, 2, 1), info
 
-    def dos(self, rho, freq_ev, crit=1e-10, maxit0=20000):
+    def dos(self, rho, freq_ev, crit=1e-10, maxit0=20000, precision=PREC_FP64):
         """Columns A(w), occupied part, empty part, Re G^r, Im G^r at every frequency (eV)."""
         f = np.ascontiguousarray(np.atleast_1d(freq_ev), dtype=np.float64)
         rho = _c128(rho, self.ctx.lunk)
         out = np.zeros(5 * f.size)
-        o = SolveOpts(crit=crit, maxit0=maxit0, precision=PREC_FP64)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision)
         info = SolveInfo()
         _check(lib().heom_cf_dos(self.h, rho.ctypes.data, f.size, f.ctypes.data, C.byref(o), out.ctypes.data,
                                  C.byref(info)))

@@ -303,7 +303,8 @@ int heom_cf_calc_ax(heom_cf *cf, double dfreq, int32_t isgnw, int64_t ldim, cons
  * brhoa = -i op(a) rho + i rho op'(a) (isgnb = 1: op = a^dag, op' = a; isgnb = 2: the
  * reverse).  rho: steady state (lunk_spa complex, host).  Each solve starts from x = 0,
  * runs TFQMR with tolerance 1e-3 crit and stops at ||b - L x|| <= crit (o->crit,
- * o->maxit0; FP64 only).  zouth, zouta: nfreq dense nrho x nrho RDO blocks (column-major)
+ * o->maxit0).  o->precision HEOM_PREC_FP64 is the reference algorithm; HEOM_PREC_MIXED
+ * refines FP64 residuals with fused FP32x2 inner solves to the same criterion.  zouth, zouta: nfreq dense nrho x nrho RDO blocks (column-major)
  * of the two components, as the reference returns them; either may be NULL. */
 int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_t isgnw, int32_t nfreq,
                   const double *dfreq, const heom_solve_opts *o, double _Complex *zouth, double _Complex *zouta,

@@ -139,3 +139,17 @@ def test_batched_frequencies_match_single_solves():
     for k in (0, 5, 11):
         one, _ = c.dos(rho, freqs[k:k + 1], crit=1e-11, maxit0=40000)
         np.testing.assert_allclose(one[0], out[k], rtol=1e-9, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["siam_L3", "dqd_L2"])
+def test_mixed_precision_spectral_function_matches_fp64(name):
+    """FP32x2 inner solves with FP64 refinement reach the same spectra as the FP64 TFQMR."""
+    m = heomq.Model(CASES[name])
+    ctx = heomq.Context(m, adjoint=False)
+    rho, _ = ctx.solve_tfqmr(crit=1e-11, maxit0=40000)
+    c = heomq.CorrFunc(ctx, 1, 1)
+    freqs = np.linspace(-2.5, 2.5, 9)
+    ref, i64 = c.dos(rho, freqs, crit=1e-11, maxit0=40000)
+    got, imx = c.dos(rho, freqs, crit=1e-11, maxit0=40000, precision=heomq.PREC_MIXED)
+    assert i64.converged and imx.converged and imx.resid <= 1e-11
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-12)
