@@ -432,7 +432,9 @@ def run_dos(args, ws, rank, local, dist):
     freqs = dos_freqs(nf * ws)[rank * nf:(rank + 1) * nf]
     if args.profile_cf:
         sec, alg = cf.bench_apply(nbatch=2 * nf, reps=2)
-        print(json.dumps({"profile_cf": True, "instances": 2 * nf, "apply_us": sec * 1e6, "alg_bytes": alg}), flush=True)
+        (sb, sa), _ = cf.bench_inner(nbatch=2 * nf, reps=2)
+        print(json.dumps({"profile_cf": True, "instances": 2 * nf, "apply_us": sec * 1e6, "alg_bytes": alg,
+                          "k_in_b_us": sb * 1e6, "k_in_a_us": sa * 1e6}), flush=True)
         return 0
     rho, sinfo = ctx.solve_tfqmr(crit=1e-10, precision=heomq.PREC_MIXED)
     mixed = heomq.PREC_MIXED
@@ -461,10 +463,11 @@ def run_dos(args, ws, rank, local, dist):
     out64, info64 = cf.dos(rho, freqs, crit=DOS_CRIT)
     dos_err = float(np.max(np.abs(out[:, 0] - out64[:, 0]) / np.abs(out64[:, 0])))
     sec, alg = cf.bench_apply(nbatch=2 * nf, reps=10)
+    (sb, sa), (bb, ba) = cf.bench_inner(nbatch=2 * nf, reps=10)
     peak, peak_kind = measured_peak_hbm()
-    achieved = alg / sec / 1e9
-    prof = "apply_cf_fp64_dqd_L4_16inst.md"
-    traffic = profile_traffic(prof)
+    achieved = bb / sb / 1e9
+    prof = "inner_cf_fp32x2_dqd_L4_16inst.md"
+    traffic = profile_traffic(prof, "dram_bytes_per_launch_k_in_b")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
@@ -492,10 +495,12 @@ def run_dos(args, ws, rank, local, dist):
                        "spectrum_min": float(out[:, 1:3].min()), "steady_resid": sinfo.resid},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": f"k_apply_cf<FP64> over {2 * nf} instances (the FP64 residual and reference path)",
-                         "kernel_us": sec * 1e6,
-                         "alg_bytes_per_launch": alg,
-                         "note": "FP64-pipe bound like the steady FP64 apply (GB300 FP64 = 1/64 of FP32): profiles/" + prof},
+                         "kernel": f"k_in_b<FP32x2, cf>: apply of w plus the fused vector updates, over {2 * nf} instances",
+                         "kernel_us": sb * 1e6, "alg_bytes_per_launch": bb,
+                         "k_in_a": {"kernel_us": sa * 1e6, "alg_bytes_per_launch": ba, "achieved": ba / sa / 1e9},
+                         "fp64_apply": {"kernel_us": sec * 1e6, "alg_bytes_per_launch": alg, "achieved": alg / sec / 1e9,
+                                        "profile": "profiles/apply_cf_fp64_dqd_L4_16inst.md"},
+                         "note": "issue-bound on the FP32/ALU pipes like the steady inner kernels: profiles/" + prof},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "freqs/s", "h2d_bytes_per_step": model.lunk * 16 + nf * 8,
                     "d2h_bytes_per_step": nf * 5 * 8},

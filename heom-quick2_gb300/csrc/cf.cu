@@ -12,6 +12,7 @@
 
 #include "apply_entry.cuh"
 #include "context.cuh"
+#include "inner.cuh"
 
 namespace heom {
 
@@ -143,7 +144,8 @@ struct CfBatchResult {
 // operator itself, which has no null space for omega != 0; FP64 inner solves take over for
 // instances whose round fails to halve the residual.
 void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::vector<int> &rid,
-                    const std::vector<std::vector<cd>> &rhs, double crit, int maxit0, int precision, CfBatchResult &res)
+                    const std::vector<std::vector<cd>> &rhs, double crit, int maxit0, int precision, CfBatchResult &res,
+                    int bench_reps = 0, double *bench = nullptr)
 {
     heom_ctx *c = cf->ctx;
     const int nb = (int)omega.size();
@@ -221,6 +223,34 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
             KD.trace_on = 0;
             KD.cf_omega = cf->d_omega;
             KD.cf_half = L;
+            if (bench_reps > 0) {
+                // measurement: the two fused inner kernels (B: apply of w with the first half of
+                // the vector updates; A: apply of v with the second half) over the batch
+                InnerWork<DF> IW;
+                inner_alloc<DF>(IW, nb, N, c->stream);
+                float4 *gdd = nullptr;
+                try {
+                    std::vector<float4> rt(N);
+                    for (int64_t i = 0; i < N; i++)
+                        rt[i] = Num<DF>::store_host(Num<DF>::from_d(cf->rt_host[2 * i], cf->rt_host[2 * i + 1]));
+                    CK(cudaMemcpyAsync(IW.rt, rt.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, c->stream));
+                    CK(cudaMalloc((void **)&gdd, sizeof(float4) * (size_t)P.nado * nb));
+                    fill_gdiag<DF>(P, KD, gdd, nb, c->stream);
+                    KD.gdiag = gdd;
+                    CK(cudaStreamSynchronize(c->stream));
+                    float mb = 0, ma = 0;
+                    inner_time<DF>(IW, P, KD, bench_reps, c->stream, mb, ma);
+                    const double v = (double)N * sizeof(float4), pb = plan_read_bytes(cf->plan);
+                    bench[0] = mb * 1e-3;
+                    bench[1] = ma * 1e-3;
+                    bench[2] = nb * (2.0 + 10.0) * v + v + pb;
+                    bench[3] = nb * (2.0 + 3.0) * v + v + pb;
+                } catch (...) { inner_free(IW); if (gdd) cudaFree(gdd); throw; }
+                inner_free(IW);
+                cudaFree(gdd);
+                cleanup();
+                return;
+            }
             heom_solve_opts mo{};
             mo.crit = crit;
             mo.maxit0 = maxit0;
@@ -530,6 +560,19 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
             }
         });
         fill_info(all, o->crit, info);
+    });
+}
+
+int heom_cf_bench_inner(heom_cf *cf, int32_t nbatch, int32_t reps, double *out)
+{
+    return guarded([&] {
+        require_cf(cf);
+        if (nbatch < 1 || reps < 1 || !out) fail(HEOM_E_ARG, "nbatch and reps must be positive");
+        std::vector<double> w(nbatch);
+        for (int b = 0; b < nbatch; b++) w[b] = (b % 2 ? 1.0 : -1.0) * (0.1 + 0.01 * b) / kHbar;
+        std::vector<std::vector<cd>> rhs(1, std::vector<cd>(2 * cf->lunkcf, cd(1e-3, 0)));
+        CfBatchResult r;
+        cf_solve_batch(cf, w, std::vector<int>(nbatch, 0), rhs, 1e-8, 100, HEOM_PREC_MIXED, r, reps, out);
     });
 }
 

@@ -133,6 +133,7 @@ SIGNATURES = {
     "heom_cf_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, _p(SolveOpts),
                                 C.c_void_p, C.c_void_p, _p(SolveInfo)]),
     "heom_cf_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "heom_cf_bench_inner": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "heom_cf_dos": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, _p(SolveOpts), C.c_void_p,
                               _p(SolveInfo)]),
 }
@@ -508,6 +509,12 @@ class CorrFunc:
         _check(lib().heom_cf_dos(self.h, rho.ctypes.data, f.size, f.ctypes.data, C.byref(o), out.ctypes.data,
                                  C.byref(info)))
         return out.reshape(f.size, 5), info
+
+    def bench_inner(self, nbatch=2, reps=20):
+        """((B s, A s), (B bytes, A bytes)) per launch of the fused FP32x2 inner kernels."""
+        out = np.zeros(4)
+        _check(lib().heom_cf_bench_inner(self.h, nbatch, reps, out.ctypes.data))
+        return (out[0], out[1]), (out[2], out[3])
 
     def bench_apply(self, nbatch=1, reps=20):
         """(seconds per launch, algorithmic bytes per launch) of the FP64 cf apply."""

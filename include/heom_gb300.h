@@ -325,6 +325,10 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
  * `nbatch` instances (frequencies) and the algorithmic bytes of one launch (each instance's
  * vector read once and written once, plus the plan).  No reference counterpart. */
 int heom_cf_bench_apply(heom_cf *cf, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
+/* Measurement hook of the mixed-precision cf solve: out[0], out[1] = seconds per launch of
+ * the two fused FP32x2 inner-iteration kernels over `nbatch` instances; out[2], out[3] =
+ * their algorithmic bytes per launch. */
+int heom_cf_bench_inner(heom_cf *cf, int32_t nbatch, int32_t reps, double *out /* 4 */);
 
 /* Measurement hook of the Jacobi sweep: out[0], out[1] = seconds per launch of the sector
  * transform kernel and of the apply (reps launches each), out[2] = the transform's

@@ -141,15 +141,15 @@ def test_batched_frequencies_match_single_solves():
         np.testing.assert_allclose(one[0], out[k], rtol=1e-9, atol=1e-13)
 
 
-@pytest.mark.parametrize("name", ["siam_L3", "dqd_L2"])
-def test_mixed_precision_spectral_function_matches_fp64(name):
+@pytest.mark.parametrize("name, crit", [("siam_L3", 1e-11), ("dqd_L2", 1e-10)])
+def test_mixed_precision_spectral_function_matches_fp64(name, crit):
     """FP32x2 inner solves with FP64 refinement reach the same spectra as the FP64 TFQMR."""
     m = heomq.Model(CASES[name])
     ctx = heomq.Context(m, adjoint=False)
-    rho, _ = ctx.solve_tfqmr(crit=1e-11, maxit0=40000)
+    rho, _ = ctx.solve_tfqmr(crit=1e-11, maxit0=40000, precision=heomq.PREC_MIXED)
     c = heomq.CorrFunc(ctx, 1, 1)
     freqs = np.linspace(-2.5, 2.5, 9)
-    ref, i64 = c.dos(rho, freqs, crit=1e-11, maxit0=40000)
-    got, imx = c.dos(rho, freqs, crit=1e-11, maxit0=40000, precision=heomq.PREC_MIXED)
-    assert i64.converged and imx.converged and imx.resid <= 1e-11
-    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-12)
+    ref, i64 = c.dos(rho, freqs, crit=crit, maxit0=40000)
+    got, imx = c.dos(rho, freqs, crit=crit, maxit0=40000, precision=heomq.PREC_MIXED)
+    assert i64.converged and imx.converged and imx.resid <= crit
+    np.testing.assert_allclose(got, ref, rtol=100 * crit, atol=1e-12)
