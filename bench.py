@@ -540,6 +540,31 @@ def cpu_jacobi_sample(nthreads, sweeps, nsample=2):
     return t_sweep, 1.0 / (t_sweep * sweeps)
 
 
+def run_jacobi_reference(args, ws, rank, dist):
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    sweeps = 451   # the sweeps the same iteration takes on this workload (measured on the GPU path)
+    cpu_jacobi_sample(nthreads, sweeps, nsample=1)
+    vals, per = [], []
+    for _ in range(args.steps):
+        t_sweep, v = cpu_jacobi_sample(nthreads, sweeps, nsample=1)
+        vals.append(v)
+        per.append(t_sweep)
+    value = statistics.median(vals)
+    line = {
+        "metric": JAC_METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": JAC_WORKLOAD, "crit": JAC_CRIT, "sweep_s": statistics.median(per), "sweeps": sweeps},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                         "sample": f"one sweep of the C restatement of calc_ax_jacobi_spa_omp per step, scaled by {sweeps} sweeps"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_jacobi(args, ws, rank, local, dist):
     import torch
 
@@ -624,6 +649,8 @@ def main():
     if args.impl == "reference":
         if args.workload == "dos":
             return run_dos_reference(args, ws, rank, dist)
+        if args.workload == "jacobi":
+            return run_jacobi_reference(args, ws, rank, dist)
         return run_reference(args, ws, rank, dist)
     sys.path.insert(0, ROOT)
     import __graft_entry__
