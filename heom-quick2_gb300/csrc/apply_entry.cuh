@@ -129,6 +129,7 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         if (((e - e0) & 3) == 3) ua = N::norm(ua);
     }
     acc = N::add(acc, CF ? ua : N::mul_i(ua));
+    if (C.pre) acc = N::scale(acc, N::sc((double)__ldg(C.pre + n)));
     return acc;
 }
 

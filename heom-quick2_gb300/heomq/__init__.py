@@ -71,7 +71,8 @@ class CtxOpts(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32), ("inner_tol", C.c_double),
-                ("max_refine", C.c_int32), ("stag_window", C.c_int32)]
+                ("max_refine", C.c_int32), ("stag_window", C.c_int32), ("inner_precond", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
