@@ -437,7 +437,9 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         // left diagonal preconditioning: the inner problem M A d = M r with M = diag(1 / (|g0_n|
         // + ||H||_inf)) per ADO evens out the rows of the hierarchy's tiers (about half the
         // Krylov iterations on the double dot); the FP64 refinement still tests A x = b
-        if (o.inner_precond >= 0) {
+        // (the FP64 inner solves of FP64_REFINED and of the stall fallback stay unscaled: there
+        // the divided target would ask for more than FP64 TFQMR reaches on some models)
+        if (o.inner_precond >= 0 && !std::is_same<T, double>::value) {
             double hn = 0;
             for (int i = 0; i < c->nrho; i++) {
                 double rs = 0;

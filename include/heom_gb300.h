@@ -159,9 +159,10 @@ typedef struct {
                                  inner solves on the same regularised operator */
     int32_t stag_window;      /* MIXED: an inner solve also stops after this many every-50-applies
                                  tests without halving its residual; <= 0 selects 40 */
-    int32_t inner_precond;    /* MIXED: left diagonal preconditioning of the inner solves (the rows
-                                 of ADO n scaled by 1 / (|sum of its damping rates| + ||H||_inf));
-                                 0 (default) or 1 = on, -1 = off */
+    int32_t inner_precond;    /* MIXED, MIXED_FP32: left diagonal preconditioning of the FP32x2 /
+                                 FP32 inner solves (the rows of ADO n scaled by
+                                 1 / (|sum of its damping rates| + ||H||_inf)); 0 (default) or
+                                 1 = on, -1 = off.  FP64 inner solves are not scaled. */
     int32_t reserved;
 } heom_solve_opts;
 
