@@ -328,11 +328,12 @@ class Context:
         return y
 
     def solve_tfqmr(self, rho=None, crit=1e-10, maxit0=20000, precision=PREC_FP64, inner_tol=0.0, max_refine=8,
-                    check=True):
+                    check=True, inner_precond=0):
         if rho is None:
             rho = self.model.initial_guess()
         rho = _c128(rho, self.lunk).copy()
-        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine)
+        o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine,
+                      inner_precond=inner_precond)
         info = SolveInfo()
         rc = lib().heom_solve_tfqmr(self.h, C.byref(o), rho.ctypes.data, C.byref(info))
         if check:

@@ -64,3 +64,17 @@ def test_mixed_batch_converges_on_the_kanamori_model():
     j = np.array([ctx.current(out[b])[0].sum() for b in range(4)])
     j_ref = np.array([ctx.current(ref[b])[0].sum() for b in range(4)])
     assert np.max(np.abs(j - j_ref) / np.abs(j_ref)) <= 1e-7
+
+
+@pytest.mark.parametrize("cfg", [cf.dqd(ntier=4), cf.siam(ntier=5)], ids=["dqd_L3", "siam_L4"])
+def test_inner_preconditioner_keeps_the_answer_and_saves_iterations(cfg):
+    """Left diagonal scaling of the FP32x2 inner solves (inner_precond 0 = default, -1 = off):
+    the same steady state at the FP64 criterion, with fewer operator applies."""
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m)
+    on, i_on = ctx.solve_tfqmr(crit=1e-9, precision=heomq.PREC_MIXED)
+    off, i_off = ctx.solve_tfqmr(crit=1e-9, precision=heomq.PREC_MIXED, inner_precond=-1)
+    assert i_on.converged and i_off.converged and i_on.resid <= 1e-9
+    j_on, j_off = ctx.current(on)[0].sum(), ctx.current(off)[0].sum()
+    assert abs(j_on / j_off - 1) < 1e-8
+    assert i_on.iters < i_off.iters
