@@ -563,6 +563,102 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
     });
 }
 
+int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_t nstep, int32_t ljw,
+                      double _Complex *corr, double _Complex *rdo_h, double _Complex *rdo_a)
+{
+    return guarded([&] {
+        require_cf(cf);
+        if (!rho || !corr || nstep < 0 || !(dt > 0)) fail(HEOM_E_ARG, "null argument, nstep < 0 or dt <= 0");
+        heom_ctx *c = cf->ctx;
+        const int nb = ljw ? 2 : 1, n = cf->nrho, nz0 = cf->nnzcf[0];
+        const int64_t L = cf->lunkcf, N = 2 * L + 1, vs = (N + 63) / 64 * 64;
+        // initial values (initialize_cf.f90:40-170, b_ams_isgn = 2): instance 0 holds B rho
+        // (a rho + rho a^dag), instance 1 B^dag rho (a^dag rho + rho a); cf_rhs returns -(B rho)
+        std::vector<std::vector<cd>> b0(nb);
+        cf_rhs(cf, reinterpret_cast<const cd *>(rho), 2, b0[0]);
+        if (ljw) cf_rhs(cf, reinterpret_cast<const cd *>(rho), 1, b0[1]);
+        std::vector<void *> tmp;
+        auto cleanup = [&] { for (void *p : tmp) cudaFree(p); tmp.clear(); };
+        auto dmalloc = [&](size_t bytes) { void *p = nullptr; CK(cudaMalloc(&p, bytes)); tmp.push_back(p); return p; };
+        try {
+            const size_t vb = sizeof(double2) * (size_t)vs * nb;
+            double2 *x = (double2 *)dmalloc(vb), *acc = (double2 *)dmalloc(vb), *stg = (double2 *)dmalloc(vb), *k = (double2 *)dmalloc(vb);
+            double2 *hist = (double2 *)dmalloc(sizeof(double2) * 2 * (size_t)nz0 * nb * (nstep + 1));
+            CK(cudaMemsetAsync(x, 0, vb, c->stream));
+            for (int b = 0; b < nb; b++) {
+                std::vector<cd> pos(b0[b].size());
+                for (size_t q = 0; q < pos.size(); q++) pos[q] = -b0[b][q];
+                CK(cudaMemcpyAsync(x + (int64_t)b * vs, pos.data(), sizeof(double2) * 2 * L, cudaMemcpyHostToDevice, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
+            }
+            // the operator without frequency terms (lfreq = F), per-instance parameter copies
+            ensure_omega(cf, nb);
+            const double zero[2] = {0.0, 0.0};
+            CK(cudaMemcpyAsync(cf->d_omega, zero, sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream));
+            DevCoef<double> K = cf_coef(cf);
+            const DevPlan P = cf->dplan.view;
+            double2 *hv = (double2 *)dmalloc(sizeof(double2) * (size_t)std::max(1, P.nh) * nb);
+            double *es = (double *)dmalloc(sizeof(double) * 4 * (size_t)nb);
+            double2 *gd = (double2 *)dmalloc(sizeof(double2) * (size_t)P.nado * nb);
+            for (int b = 0; b < nb; b++) {
+                CK(cudaMemcpyAsync(hv + (size_t)b * P.nh, c->hval64, sizeof(double2) * P.nh, cudaMemcpyDeviceToDevice, c->stream));
+                CK(cudaMemcpyAsync(es + 4 * (size_t)b, c->es64, sizeof(double) * 4, cudaMemcpyDeviceToDevice, c->stream));
+            }
+            K.hval = hv;
+            K.eshift = es;
+            fill_gdiag<double>(P, K, gd, nb, c->stream);
+            K.gdiag = gd;
+            const int64_t nv = vs * nb;
+            auto record = [&](int step) {
+                for (int b = 0; b < nb; b++)
+                    for (int h = 0; h < 2; h++)
+                        CK(cudaMemcpyAsync(hist + ((size_t)step * nb * 2 + (size_t)b * 2 + h) * nz0, x + (int64_t)b * vs + h * L,
+                                           sizeof(double2) * nz0, cudaMemcpyDeviceToDevice, c->stream));
+            };
+            // classical RK4 (corrfunc.f90:430-610): x <- x + dt (k1 + 2 k2 + 2 k3 + k4) / 6
+            record(0);
+            for (int step = 1; step <= nstep; step++) {
+                launch_apply_cf(P, K, x, k, nb, vs, nullptr, c->stream);                 // k1
+                vec_axpby<double>(nv, acc, 1.0, x, dt / 6.0, k, c->stream);
+                vec_axpby<double>(nv, stg, 1.0, x, dt / 2.0, k, c->stream);
+                launch_apply_cf(P, K, stg, k, nb, vs, nullptr, c->stream);               // k2
+                vec_axpby<double>(nv, acc, 1.0, acc, dt / 3.0, k, c->stream);
+                vec_axpby<double>(nv, stg, 1.0, x, dt / 2.0, k, c->stream);
+                launch_apply_cf(P, K, stg, k, nb, vs, nullptr, c->stream);               // k3
+                vec_axpby<double>(nv, acc, 1.0, acc, dt / 3.0, k, c->stream);
+                vec_axpby<double>(nv, stg, 1.0, x, dt, k, c->stream);
+                launch_apply_cf(P, K, stg, k, nb, vs, nullptr, c->stream);               // k4
+                vec_axpby<double>(nv, x, 1.0, acc, dt / 6.0, k, c->stream);
+                record(step);
+            }
+            CK(cudaGetLastError());
+            std::vector<cd> hh((size_t)2 * nz0 * nb * (nstep + 1));
+            CK(cudaMemcpyAsync(hh.data(), hist, sizeof(double2) * hh.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            // C(t) = Tr[a (X_h + i X_a) / 2] and, with ljw, conj(Tr[a^dag (Y_h + i Y_a) / 2]) (corrfunc.f90:378-416)
+            std::vector<cd> z(nz0), m;
+            for (int step = 0; step <= nstep; step++) {
+                for (int b = 0; b < 2; b++) {
+                    cd val(0, 0);
+                    if (b < nb) {
+                        const cd *xh = hh.data() + ((size_t)step * nb * 2 + (size_t)b * 2) * nz0, *xa = xh + nz0;
+                        for (int q = 0; q < nz0; q++) z[q] = 0.5 * xh[q] + cd(0, 0.5) * xa[q];
+                        rdo_dense(cf, z.data(), m);
+                        val = b == 0 ? trace_op(cf, m, false) : std::conj(trace_op(cf, m, true));
+                    }
+                    reinterpret_cast<cd *>(corr)[2 * (size_t)step + b] = val;
+                }
+                if (rdo_h || rdo_a) {
+                    const cd *xh = hh.data() + ((size_t)step * nb * 2) * nz0, *xa = xh + nz0;
+                    if (rdo_h) { rdo_dense(cf, xh, m); std::copy(m.begin(), m.end(), reinterpret_cast<cd *>(rdo_h) + (size_t)step * n * n); }
+                    if (rdo_a) { rdo_dense(cf, xa, m); std::copy(m.begin(), m.end(), reinterpret_cast<cd *>(rdo_a) + (size_t)step * n * n); }
+                }
+            }
+        } catch (...) { cleanup(); throw; }
+        cleanup();
+    });
+}
+
 int heom_cf_bench_inner(heom_cf *cf, int32_t nbatch, int32_t reps, double *out)
 {
     return guarded([&] {

@@ -135,6 +135,8 @@ SIGNATURES = {
                                 C.c_void_p, C.c_void_p, _p(SolveInfo)]),
     "heom_cf_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_cf_bench_inner": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "heom_cf_propagate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]),
     "heom_cf_dos": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, _p(SolveOpts), C.c_void_p,
                               _p(SolveInfo)]),
 }
@@ -511,6 +513,21 @@ class CorrFunc:
         _check(lib().heom_cf_dos(self.h, rho.ctypes.data, f.size, f.ctypes.data, C.byref(o), out.ctypes.data,
                                  C.byref(info)))
         return out.reshape(f.size, 5), info
+
+    def propagate(self, rho, dt, nstep, ljw=True, rdo=False):
+        """Time-domain correlation functions (corrfunc lfreq_dos = F): corr (nstep+1, 2) and, with
+        rdo, the RDO blocks of X_h and X_a at every step (nstep+1, nrho, nrho).  dt in 1/(energy/hbar)."""
+        rho = _c128(rho, self.ctx.lunk)
+        corr = np.zeros(2 * (nstep + 1), dtype=np.complex128)
+        n = self.nrho
+        rh = np.zeros((nstep + 1) * n * n, dtype=np.complex128) if rdo else None
+        ra = np.zeros((nstep + 1) * n * n, dtype=np.complex128) if rdo else None
+        _check(lib().heom_cf_propagate(self.h, rho.ctypes.data, float(dt), int(nstep), int(bool(ljw)), corr.ctypes.data,
+                                       None if rh is None else rh.ctypes.data, None if ra is None else ra.ctypes.data))
+        corr = corr.reshape(nstep + 1, 2)
+        if not rdo:
+            return corr
+        return corr, rh.reshape(nstep + 1, n, n).transpose(0, 2, 1), ra.reshape(nstep + 1, n, n).transpose(0, 2, 1)
 
     def bench_inner(self, nbatch=2, reps=20):
         """((B s, A s), (B bytes, A bytes)) per launch of the fused FP32x2 inner kernels."""

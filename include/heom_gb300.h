@@ -315,6 +315,15 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
                   const double *dfreq, const heom_solve_opts *o, double _Complex *zouth, double _Complex *zouta,
                   heom_solve_info *info);
 
+/* The time-domain branch of corrfunc (corrfunc/corrfunc.f90:364-630, lfreq_dos = F): X(0) = B rho
+ * (a rho + rho a^dag on the cf pattern) propagated by RK4 steps of dt under the cf operator
+ * without frequency terms; with ljw also Y(0) = B^dag rho.  corr[2k], corr[2k+1] receive
+ * Tr[a (X_h + i X_a)/2] and conj(Tr[a^dag (Y_h + i Y_a)/2]) (0 without ljw) at t = k dt,
+ * k = 0..nstep.  rdo_h, rdo_a (optional): the dense RDO blocks of X_h, X_a at every step
+ * ((nstep + 1) nrho^2 complex each). */
+int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_t nstep, int32_t ljw,
+                      double _Complex *corr, double _Complex *rdo_h, double _Complex *rdo_a);
+
 /* The frequency-domain spectral function of corrfunc (corrfunc/corrfunc.f90:146-217,
  * lfreq_dos with ljw_dos): for every frequency freq_ev[k] (eV) the two solves
  * (isgnb, isgnw) = (2, 2) and (1, 1), batched together, and

@@ -153,3 +153,52 @@ def test_mixed_precision_spectral_function_matches_fp64(name, crit):
     got, imx = c.dos(rho, freqs, crit=crit, maxit0=40000, precision=heomq.PREC_MIXED)
     assert i64.converged and imx.converged and imx.resid <= crit
     np.testing.assert_allclose(got, ref, rtol=100 * crit, atol=1e-12)
+
+
+def test_time_domain_matches_oracle_rk4():
+    """corrfunc's time-domain branch: RK4 of X(0) = B rho under the cf operator (no frequency
+    terms) against the same RK4 on the oracle's operator, and C(t) = Tr[a (X_h + i X_a)/2]."""
+    cfg = CASES["siam_L3"]
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m, adjoint=False)
+    ref = of.Model(cfg)
+    rho, _ = ctx.solve_tfqmr(crit=1e-11, maxit0=40000, precision=heomq.PREC_MIXED)
+    c, r = heomq.CorrFunc(ctx, 1, 1), of.CF(ref, 1, 1)
+    dt, nstep = 0.02, 12
+    corr = c.propagate(rho, dt, nstep, ljw=True)
+    a = ref.dense_op(1, 1)
+    for isgnb, col in ((2, 0), (1, 1)):
+        xh, xa = r.rhs(rho, isgnb)
+        for k in range(nstep + 1):
+            z = 0.5 * r.rdo(xh) + 0.5j * r.rdo(xa)
+            want = np.trace(a @ z) if col == 0 else np.conj(np.trace(a.conj().T @ z))
+            assert abs(corr[k, col] - want) <= 1e-11 * max(1.0, abs(want)), (isgnb, k)
+            k1 = r.apply(0.0, 1, xh, xa)
+            k2 = r.apply(0.0, 1, xh + dt / 2 * k1[0], xa + dt / 2 * k1[1])
+            k3 = r.apply(0.0, 1, xh + dt / 2 * k2[0], xa + dt / 2 * k2[1])
+            k4 = r.apply(0.0, 1, xh + dt * k3[0], xa + dt * k3[1])
+            xh = xh + dt / 6 * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0])
+            xa = xa + dt / 6 * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1])
+
+
+def test_time_and_frequency_domains_agree():
+    """The frequency-domain solution is the Laplace transform of the time-domain one: with
+    L_w = L + w J for isgnw = 2 (J (h, a) = (a, -h), which commutes with L),
+    X_h(w) = int cos(wt) X_h(t) + sin(wt) X_a(t) dt and X_a(w) = int cos(wt) X_a(t) - sin(wt) X_h(t) dt."""
+    m = heomq.Model(CASES["level_L2"])
+    ctx = heomq.Context(m, adjoint=False)
+    rho, _ = ctx.solve_tfqmr(crit=1e-11, maxit0=40000, precision=heomq.PREC_MIXED)
+    c = heomq.CorrFunc(ctx, 1, 1)
+    dt, nstep = 0.01, 4000
+    _, xh_t, xa_t = c.propagate(rho, dt, nstep, ljw=False, rdo=True)
+    t = dt * np.arange(nstep + 1)
+    w_simp = np.ones(nstep + 1)
+    w_simp[1:-1:2], w_simp[2:-1:2] = 4, 2
+    w_simp *= dt / 3
+    for w in (0.4, 1.3):
+        cw, sw = np.cos(w * t)[:, None, None], np.sin(w * t)[:, None, None]
+        lap_h = np.tensordot(w_simp, cw * xh_t + sw * xa_t, axes=1)
+        lap_a = np.tensordot(w_simp, cw * xa_t - sw * xh_t, axes=1)
+        zh, za, info = c.solve_cf_tfqmr_spa(rho, 2, 2, [w], crit=1e-12, maxit0=40000)
+        scale = np.linalg.norm(zh[0]) + np.linalg.norm(za[0])
+        assert np.linalg.norm(lap_h - zh[0]) + np.linalg.norm(lap_a - za[0]) <= 1e-6 * scale, w
