@@ -635,7 +635,8 @@ int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_
             std::vector<cd> hh((size_t)2 * nz0 * nb * (nstep + 1));
             CK(cudaMemcpyAsync(hh.data(), hist, sizeof(double2) * hh.size(), cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
-            // C(t) = Tr[a (X_h + i X_a) / 2] and, with ljw, conj(Tr[a^dag (Y_h + i Y_a) / 2]) (corrfunc.f90:378-416)
+            // C(t) = Tr[A (X_h + i X_a) / 2] and, with ljw, conj(Tr[A^dag (Y_h + i Y_a) / 2]) with
+            // A = a^dag (a_ams_isgn = 1, initialize_cf.f90:211-217; corrfunc.f90:378-416)
             std::vector<cd> z(nz0), m;
             for (int step = 0; step <= nstep; step++) {
                 for (int b = 0; b < 2; b++) {
@@ -644,7 +645,7 @@ int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_
                         const cd *xh = hh.data() + ((size_t)step * nb * 2 + (size_t)b * 2) * nz0, *xa = xh + nz0;
                         for (int q = 0; q < nz0; q++) z[q] = 0.5 * xh[q] + cd(0, 0.5) * xa[q];
                         rdo_dense(cf, z.data(), m);
-                        val = b == 0 ? trace_op(cf, m, false) : std::conj(trace_op(cf, m, true));
+                        val = b == 0 ? trace_op(cf, m, true) : std::conj(trace_op(cf, m, false));
                     }
                     reinterpret_cast<cd *>(corr)[2 * (size_t)step + b] = val;
                 }

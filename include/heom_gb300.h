@@ -318,7 +318,8 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
 /* The time-domain branch of corrfunc (corrfunc/corrfunc.f90:364-630, lfreq_dos = F): X(0) = B rho
  * (a rho + rho a^dag on the cf pattern) propagated by RK4 steps of dt under the cf operator
  * without frequency terms; with ljw also Y(0) = B^dag rho.  corr[2k], corr[2k+1] receive
- * Tr[a (X_h + i X_a)/2] and conj(Tr[a^dag (Y_h + i Y_a)/2]) (0 without ljw) at t = k dt,
+ * Tr[a^dag (X_h + i X_a)/2] and conj(Tr[a (Y_h + i Y_a)/2]) (0 without ljw) at t = k dt
+ * (at t = 0: <a^dag a> and <a a^dag>),
  * k = 0..nstep.  rdo_h, rdo_a (optional): the dense RDO blocks of X_h, X_a at every step
  * ((nstep + 1) nrho^2 complex each). */
 int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_t nstep, int32_t ljw,

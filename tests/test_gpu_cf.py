@@ -166,12 +166,15 @@ def test_time_domain_matches_oracle_rk4():
     c, r = heomq.CorrFunc(ctx, 1, 1), of.CF(ref, 1, 1)
     dt, nstep = 0.02, 12
     corr = c.propagate(rho, dt, nstep, ljw=True)
+    # t = 0: <a^dag a> = n_up and <a a^dag> = 1 - n_up
+    n_up = ctx.occupation(rho)[0, 0]
+    assert abs(corr[0, 0] - n_up) < 1e-12 and abs(corr[0, 1] - (1 - n_up)) < 1e-12
     a = ref.dense_op(1, 1)
     for isgnb, col in ((2, 0), (1, 1)):
         xh, xa = r.rhs(rho, isgnb)
         for k in range(nstep + 1):
             z = 0.5 * r.rdo(xh) + 0.5j * r.rdo(xa)
-            want = np.trace(a @ z) if col == 0 else np.conj(np.trace(a.conj().T @ z))
+            want = np.trace(a.conj().T @ z) if col == 0 else np.conj(np.trace(a @ z))
             assert abs(corr[k, col] - want) <= 1e-11 * max(1.0, abs(want)), (isgnb, k)
             k1 = r.apply(0.0, 1, xh, xa)
             k2 = r.apply(0.0, 1, xh + dt / 2 * k1[0], xa + dt / 2 * k1[1])
