@@ -391,6 +391,18 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
     info.seconds = ms * 1e-3;
 }
 
+// ||H||_inf of the context's Hamiltonian (the scale of the inner preconditioner)
+double hs_inf_norm(heom_ctx *c)
+{
+    double hn = 0;
+    for (int i = 0; i < c->nrho; i++) {
+        double rs = 0;
+        for (int j = 0; j < c->nrho; j++) rs += std::abs(c->hs_host[i + (size_t)j * c->nrho]);
+        hn = std::max(hn, rs);
+    }
+    return std::max(hn, 1e-300);
+}
+
 // Mixed-precision refinement: rounds of (hermitise x, FP64 residual r = rhs - A x, inner
 // TFQMR on A~ d = r / ||r|| in the number type T, x += ||r|| d) until ||r|| <= crit.  A~ is
 // the regularised operator (DevCoef::reg): it agrees with A on vectors whose RDO block is
@@ -440,14 +452,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         // (the FP64 inner solves of FP64_REFINED and of the stall fallback stay unscaled: there
         // the divided target would ask for more than FP64 TFQMR reaches on some models)
         if (o.inner_precond >= 0 && !std::is_same<T, double>::value) {
-            double hn = 0;
-            for (int i = 0; i < c->nrho; i++) {
-                double rs = 0;
-                for (int j = 0; j < c->nrho; j++) rs += std::abs(c->hs_host[i + (size_t)j * c->nrho]);
-                hn = std::max(hn, rs);
-            }
             CK(cudaMalloc((void **)&pre, sizeof(float) * std::max(1, PV.nado)));
-            fill_pre(PV, K64.g0, std::max(hn, 1e-300), pre, c->stream);
+            fill_pre(PV, K64.g0, hs_inf_norm(c), pre, c->stream);
             KI.pre = pre;
             aux++;
             // the inner solve measures M (b - A d): ||b - A d|| <= ||M^-1|| ||M (b - A d)||, so
@@ -1014,6 +1020,7 @@ struct BenchInputs {
     std::vector<void *> blocks;
     void *hv = nullptr, *gdiag = nullptr;
     double *es = nullptr;
+    float *pre = nullptr;   // the inner preconditioner of the mixed solves
     ~BenchInputs() { for (void *p : blocks) cudaFree(p); }
     void *alloc(size_t n) { void *p = nullptr; CK(cudaMalloc(&p, n)); blocks.push_back(p); return p; }
 };
@@ -1035,6 +1042,10 @@ void bench_inputs(heom_ctx *c, int precision, int nbatch, BenchInputs &I)
         else CK(cudaMemcpyAsync((float2 *)I.hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
     }
     I.gdiag = I.alloc(16 * std::max<size_t>(1, (size_t)c->dfwd.view.nado * nbatch));
+    if (precision == HEOM_PREC_MIXED || precision == HEOM_PREC_MIXED_FP32) {
+        I.pre = (float *)I.alloc(sizeof(float) * std::max(1, c->dfwd.view.nado));
+        fill_pre(c->dfwd.view, c->dfwd.g0_64, hs_inf_norm(c), I.pre, c->stream);
+    }
     if (precision == HEOM_PREC_MIXED) {
         DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = I.es;
         fill_gdiag<DF>(c->dfwd.view, K, (float4 *)I.gdiag, nbatch, c->stream);
@@ -1055,6 +1066,7 @@ template <typename T> DevCoef<T> bench_coef(heom_ctx *c, const BenchInputs &I)
     K.hval = (const typename Num<T>::V *)I.hv;
     K.eshift = I.es;
     K.gdiag = (const typename Num<T>::V *)I.gdiag;
+    K.pre = I.pre;
     return K;
 }
 
