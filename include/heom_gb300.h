@@ -294,6 +294,7 @@ typedef struct heom_cf heom_cf;
  * nnzcf_spa etc., e.g. from the Fortran prelude_cf_spa, or heom_model_cf_pattern).
  * t: the same tables the context was created from.  The arrays are read here only. */
 int  heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf, heom_cf **out);
+/* A heom_cf uses its context's stream and parameters: destroy it before the context. */
 void heom_cf_destroy(heom_cf *cf);
 int64_t heom_cf_lunk(const heom_cf *cf);
 
