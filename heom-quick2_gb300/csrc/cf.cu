@@ -380,8 +380,8 @@ int batch_cap(heom_cf *cf)
     const double per = 10.0 * 16.0 * (double)(2 * cf->lunkcf + 64);
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = (size_t)8 << 30;
-    const double budget = std::min(0.5 * (double)fr, 64.0 * (1ull << 30));
-    return (int)std::max(2.0, std::min(256.0, std::floor(budget / per)));
+    const double room = std::min(0.5 * (double)fr, 64.0 * (1ull << 30));
+    return (int)std::max(2.0, std::min(256.0, std::floor(room / per)));
 }
 
 }  // namespace

@@ -1,7 +1,7 @@
 /*
  * heom_oracle.h -- CPU FP64 restatement of HEOM-QUICK2's sparse-mode HEOM path.
  *
- * TEST INFRASTRUCTURE ONLY.  This oracle is the checker for the GB300 library:
+ * TEST INFRASTRUCTURE ONLY.  The GB300 library's results are tested against it:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
  * The product path never calls it.
  *

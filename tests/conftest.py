@@ -15,7 +15,7 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built():
-    """Build the oracle (the checker) and the product's CUDA library (no-op when current)."""
+    """Build the oracle and the product's CUDA library (no-op when current)."""
     import build_lib
     import oracle_ffi
 
