@@ -237,6 +237,10 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
                     CK(cudaMalloc((void **)&gdd, sizeof(float4) * (size_t)P.nado * nb));
                     fill_gdiag<DF>(P, KD, gdd, nb, c->stream);
                     KD.gdiag = gdd;
+                    // with the inner preconditioner of the mixed solves
+                    float *pre = (float *)dmalloc(sizeof(float) * std::max(1, P.nado));
+                    fill_pre(P, K.g0, hs_inf_norm(c), pre, c->stream);
+                    KD.pre = pre;
                     CK(cudaStreamSynchronize(c->stream));
                     float mb = 0, ma = 0;
                     inner_time<DF>(IW, P, KD, bench_reps, c->stream, mb, ma);

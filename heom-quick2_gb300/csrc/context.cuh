@@ -71,6 +71,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   const std::function<void(const double2 *, double2 *)> &residual,
                   const std::function<void(const double2 *)> &batch_norms,
                   const DevPlan &PV, int64_t N, const double *rt);
+// ||H||_inf of the context's Hamiltonian (the scale of the inner preconditioner)
+double hs_inf_norm(heom_ctx *c);
 // The reference's shadow-vector stream (tfqmr_double/drandn.f90, SEED = 1): n reals.
 void drandn_host(int64_t n, std::vector<double> &out);
 }  // namespace heom
