@@ -374,7 +374,8 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
             tfq_run<double>(c, W, op, nlim, it, info.launches);
             vec_axpby<double>(N, x, 1.0, x, 1.0, W.x, c->stream);
             TfqState st;
-            CK(cudaMemcpy(&st, W.st, sizeof(TfqState), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(&st, W.st, sizeof(TfqState), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
             info.iters += st.axb;
             info.ierr = st.ierr;
             info.refinements = round + 1;
@@ -458,8 +459,10 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             aux++;
             // the inner solve measures M (b - A d): ||b - A d|| <= ||M^-1|| ||M (b - A d)||, so
             // its target is divided by the condition number of M relative to the scaling of b
+            // (c->stream is non-blocking: the read is queued behind fill_pre on that stream)
             std::vector<float> ph(std::max(1, PV.nado));
-            CK(cudaMemcpy(ph.data(), pre, sizeof(float) * ph.size(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(ph.data(), pre, sizeof(float) * ph.size(), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
             const float lo = *std::min_element(ph.begin(), ph.end()), hi = *std::max_element(ph.begin(), ph.end());
             pre_kappa = lo > 0 ? (double)hi / lo : 1.0;
             pre_max = hi;
@@ -588,7 +591,8 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                 for (int b = 0; b < nbatch; b++)
                     vec_axpby<double>(N, x + (int64_t)b * vstride, 1.0, x + (int64_t)b * vstride, 1.0, W.x + (int64_t)b * W.vstride, c->stream), aux++;
                 std::vector<TfqState> st(nbatch);
-                CK(cudaMemcpy(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpyAsync(st.data(), W.st, sizeof(TfqState) * nbatch, cudaMemcpyDeviceToHost, c->stream));
+                CK(cudaStreamSynchronize(c->stream));
                 int axb = 0;
                 for (auto &sv : st) { axb = std::max(axb, sv.axb); last_ierr = sv.ierr; }
                 total_iters = axb;
@@ -653,7 +657,7 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
         int dev = opts ? opts->device : 0;
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(HEOM_E_CUDA, "no CUDA device available");
-        CK(cudaSetDevice(dev));
+        DeviceScope dsc(dev);
         std::unique_ptr<heom_ctx> c(new heom_ctx());
         c->device = dev;
         CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -777,12 +781,19 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
             const cd *cbv = reinterpret_cast<const cd *>(t->cb);
             for (size_t k = 0; k < ncb; k++) c->cb_abs_max = std::max(c->cb_abs_max, std::abs(cbv[k]));
         }
-        CK(cudaStreamSynchronize(c->stream));
+        // the set-up copies above are synchronous copies from pageable memory, whose DMA may
+        // still be in flight on return; kernels on the non-blocking stream are not ordered
+        // after them, so wait for the whole device once here
+        CK(cudaDeviceSynchronize());
         *out = c.release();
     });
 }
 
-void heom_ctx_destroy(heom_ctx *ctx) { delete ctx; }
+void heom_ctx_destroy(heom_ctx *ctx)
+{
+    if (!ctx) return;
+    try { heom::DeviceScope dsc(ctx->device); delete ctx; } catch (...) { delete ctx; }
+}
 
 int64_t heom_ctx_lunk(const heom_ctx *ctx) { return ctx ? ctx->lunk : -1; }
 
@@ -790,6 +801,7 @@ int heom_calc_ax(heom_ctx *c, int64_t ldim, const double _Complex *x, double _Co
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (ldim != c->lunk) fail(HEOM_E_ARG, "ldim does not match lunk_spa");
         if (!x || !y) fail(HEOM_E_ARG, "null vector");
         int64_t N = c->lunk + 1;
@@ -805,6 +817,7 @@ int heom_calc_ax_dev(heom_ctx *c, const void *dx, void *dy)
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         launch_apply<double, false>(c->dfwd.view, ctx_coef<double>(c, false), (const double2 *)dx, (double2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(c->stream));
@@ -815,6 +828,7 @@ int heom_calc_ax_fp32_dev(heom_ctx *c, const void *dx, void *dy)
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         launch_apply<float, false>(c->dfwd.view, ctx_coef<float>(c, false), (const float2 *)dx, (float2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(c->stream));
@@ -825,6 +839,7 @@ int heom_calc_atrx(heom_ctx *c, int64_t ldim, const double _Complex *x, double _
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!c->has_adj) fail(HEOM_E_ARG, "context built without the adjoint plan");
         if (ldim != c->lunk) fail(HEOM_E_ARG, "ldim does not match lunk_spa");
         int64_t N = c->lunk + 1;
@@ -840,6 +855,7 @@ int heom_calc_atrx_dev(heom_ctx *c, const void *dx, void *dy)
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!c->has_adj) fail(HEOM_E_ARG, "context built without the adjoint plan");
         launch_apply<double, true>(c->dadj.view, ctx_coef<double>(c, true), (const double2 *)dx, (double2 *)dy, 1, c->lunk + 1, nullptr, c->stream);
         CK(cudaGetLastError());
@@ -851,6 +867,7 @@ int heom_calcderiv(heom_ctx *c, double t, const double _Complex *x, double _Comp
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!x || !y) fail(HEOM_E_ARG, "null vector");
         double es[4];
         for (int k = 0; k < 4; k++) {
@@ -875,6 +892,7 @@ int heom_solve_tfqmr(heom_ctx *c, const heom_solve_opts *o, double _Complex *rho
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!o || !rho) fail(HEOM_E_ARG, "null argument");
         int64_t N = c->lunk + 1;
         std::vector<cd> x(N, 0.0);
@@ -918,6 +936,7 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (nbatch < 1 || !out) fail(HEOM_E_ARG, "bad batch arguments");
         *out = nullptr;
         std::unique_ptr<heom_batch> B(new heom_batch());
@@ -954,19 +973,25 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
         CK(cudaMemcpy(B->hdf, hdf.data(), sizeof(float4) * hdf.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(B->e64, e64.data(), sizeof(double) * e64.size(), cudaMemcpyHostToDevice));
         B->h_real = all_real;
+        CK(cudaDeviceSynchronize());   // the pageable copies above, before any kernel reads them
         *out = B.release();
     });
 }
 
 int64_t heom_batch_stride(const heom_batch *b) { return b ? b->vs : -1; }
 
-void heom_batch_destroy(heom_batch *b) { delete b; }
+void heom_batch_destroy(heom_batch *b)
+{
+    if (!b) return;
+    try { heom::DeviceScope dsc(b->ctx->device); delete b; } catch (...) { delete b; }
+}
 
 int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, heom_solve_info *info)
 {
     return guarded([&] {
         if (!B || !o || !x_dev) fail(HEOM_E_ARG, "null argument");
         heom_ctx *c = B->ctx;
+        DeviceScope dsc(c->device);
         DevCoef<double> K64 = c->dfwd.coef<double>(); K64.hval = B->h64; K64.eshift = B->e64; K64.h_real = B->h_real;
         DevCoef<DF> KDF = c->dfwd.coef<DF>(); KDF.hval = B->hdf; KDF.eshift = B->e64; KDF.h_real = B->h_real;
         DevCoef<float> K32 = c->dfwd.coef<float>(); K32.hval = B->h32; K32.eshift = B->e64; K32.h_real = B->h_real;
@@ -986,6 +1011,7 @@ int heom_solve_batch(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batc
     void *dxb = nullptr;
     rc = guarded([&] {
         if (!o || !rho_batch) fail(HEOM_E_ARG, "null argument");
+        DeviceScope dsc(c->device);
         const int64_t vs = B->vs;
         CK(cudaMalloc(&dxb, sizeof(double2) * (size_t)vs * nbatch));
         CK(cudaMemsetAsync(dxb, 0, sizeof(double2) * (size_t)vs * nbatch, c->stream));
@@ -999,13 +1025,14 @@ int heom_solve_batch(heom_ctx *c, int32_t nbatch, const double _Complex *hs_batc
     if (rc == 0) rc = heom_batch_solve_dev(B, o, dxb, info);
     if (rc == 0 || rc == HEOM_E_NOCONV) {
         int rc2 = guarded([&] {
+            DeviceScope dsc(c->device);
             CK(cudaMemcpy2DAsync(rho_batch, sizeof(double2) * c->lunk, dxb, sizeof(double2) * B->vs, sizeof(double2) * c->lunk,
                                  nbatch, cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
         });
         if (rc == 0) rc = rc2;
     }
-    if (dxb) cudaFree(dxb);
+    if (dxb) guarded([&] { DeviceScope dsc(c->device); cudaFree(dxb); });
     heom_batch_destroy(B);
     return rc;
 }
@@ -1108,6 +1135,7 @@ int heom_bench_apply(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (reps < 1) reps = 1;
         if (nbatch < 1) nbatch = 1;
         const int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64;
@@ -1150,6 +1178,7 @@ int heom_bench_inner(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (reps < 1) reps = 1;
         if (nbatch < 1) nbatch = 1;
         BenchInputs I;

@@ -402,7 +402,7 @@ int heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf
             fail(HEOM_E_ARG, "tables do not belong to this context");
         if (cft->iorbs < 1 || cft->iorbs > t->norbs || cft->ispin < 1 || cft->ispin > t->nspin)
             fail(HEOM_E_ARG, "invalid spin-orbital");
-        CK(cudaSetDevice(ctx->device));
+        DeviceScope dsc(ctx->device);
         std::unique_ptr<heom_cf> cf(new heom_cf());
         cf->ctx = ctx;
         cf->iorbs = cft->iorbs; cf->ispin = cft->ispin; cf->nrho = t->nrho;
@@ -436,12 +436,16 @@ int heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf
         CK(cudaMemsetAsync(cf->dx, 0, sizeof(double2) * N, ctx->stream));
         ensure_omega(cf.get(), 2);
         drandn_host(2 * N, cf->rt_host);
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaDeviceSynchronize());   // the plan's pageable set-up copies, before any kernel reads them
         *out = cf.release();
     });
 }
 
-void heom_cf_destroy(heom_cf *cf) { delete cf; }
+void heom_cf_destroy(heom_cf *cf)
+{
+    if (!cf) return;
+    try { heom::DeviceScope dsc(cf->ctx->device); delete cf; } catch (...) { delete cf; }
+}
 
 int64_t heom_cf_lunk(const heom_cf *cf) { return cf ? cf->lunkcf : -1; }
 
@@ -450,6 +454,7 @@ int heom_cf_calc_ax(heom_cf *cf, double dfreq, int32_t isgnw, int64_t ldim, cons
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (ldim != cf->lunkcf) fail(HEOM_E_ARG, "ldim does not match lunkcf_spa");
         if (!rcga || !rcgb || !rhsa || !rhsb) fail(HEOM_E_ARG, "null vector");
         if (isgnw != 1 && isgnw != 2) fail(HEOM_E_ARG, "isgnw must be 1 or 2");
@@ -473,6 +478,7 @@ int heom_cf_solve(heom_cf *cf, const double _Complex *rho, int32_t isgnb, int32_
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (!rho || !dfreq || !o || nfreq < 1) fail(HEOM_E_ARG, "null argument or no frequency");
         if (isgnb != 1 && isgnb != 2) fail(HEOM_E_ARG, "isgnb must be 1 or 2");
         if (isgnw != 1 && isgnw != 2) fail(HEOM_E_ARG, "isgnw must be 1 or 2");
@@ -517,6 +523,7 @@ int heom_cf_dos(heom_cf *cf, const double _Complex *rho, int32_t nfreq, const do
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (!rho || !freq_ev || !o || !out || nfreq < 1) fail(HEOM_E_ARG, "null argument or no frequency");
         if (o->precision != HEOM_PREC_FP64 && o->precision != HEOM_PREC_MIXED)
             fail(HEOM_E_UNSUPPORTED, "correlation-function solves run in FP64 or MIXED precision");
@@ -572,6 +579,7 @@ int heom_cf_propagate(heom_cf *cf, const double _Complex *rho, double dt, int32_
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (!rho || !corr || nstep < 0 || !(dt > 0)) fail(HEOM_E_ARG, "null argument, nstep < 0 or dt <= 0");
         heom_ctx *c = cf->ctx;
         const int nb = ljw ? 2 : 1, n = cf->nrho, nz0 = cf->nnzcf[0];
@@ -668,6 +676,7 @@ int heom_cf_bench_inner(heom_cf *cf, int32_t nbatch, int32_t reps, double *out)
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (nbatch < 1 || reps < 1 || !out) fail(HEOM_E_ARG, "nbatch and reps must be positive");
         std::vector<double> w(nbatch);
         for (int b = 0; b < nbatch; b++) w[b] = (b % 2 ? 1.0 : -1.0) * (0.1 + 0.01 * b) / kHbar;
@@ -681,6 +690,7 @@ int heom_cf_bench_apply(heom_cf *cf, int32_t nbatch, int32_t reps, double *secon
 {
     return guarded([&] {
         require_cf(cf);
+        DeviceScope dsc(cf->ctx->device);
         if (nbatch < 1 || reps < 1) fail(HEOM_E_ARG, "nbatch and reps must be positive");
         heom_ctx *c = cf->ctx;
         const int64_t N = 2 * cf->lunkcf + 1, vs = (N + 63) / 64 * 64;

@@ -9,6 +9,24 @@ namespace heom {
 void cuda_check(cudaError_t e, const char *what);
 #define CK(call) ::heom::cuda_check((call), #call)
 
+// Makes device `dev` current for the lifetime of the object and gives the caller's current
+// device back on exit: an entry point called with a context of another device neither
+// launches on the wrong device nor leaves the caller's device selection changed.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) CK(cudaSetDevice(dev));
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 // Device copy of one HostPlan plus its coefficient tables in both precisions.
 struct PlanDev {
     DevPlan view;

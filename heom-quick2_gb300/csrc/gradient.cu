@@ -94,7 +94,7 @@ extern "C" int heom_steady_gradient(heom_ctx *c, const heom_grad_opts *o, const 
         require_ctx(c);
         if (!o || !rho || !dI) fail(HEOM_E_ARG, "null argument");
         if (!c->has_adj) fail(HEOM_E_ARG, "the context was created without the adjoint plan");
-        CK(cudaSetDevice(c->device));
+        DeviceScope dsc(c->device);
         const int64_t N = c->lunk + 1;
         std::vector<void *> blocks;
         auto dalloc2 = [&](int64_t n) { void *p = nullptr; CK(cudaMalloc(&p, sizeof(double2) * n)); blocks.push_back(p); return (double2 *)p; };

@@ -179,6 +179,7 @@ int heom_jacobi_shift(heom_ctx *c, double *ejac)
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!ejac) fail(HEOM_E_ARG, "null argument");
         std::vector<cd> a = c->hs_host, v;
         std::vector<double> e;
@@ -394,6 +395,7 @@ int heom_solve_jacobi(heom_ctx *c, const heom_solve_opts *o, double ejac, double
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         jacobi_run(c, o, ejac, rho, info, 0, nullptr);
     });
 }
@@ -402,6 +404,7 @@ int heom_bench_jacobi(heom_ctx *c, double ejac, int32_t reps, double *out)
 {
     return guarded([&] {
         require_ctx(c);
+        DeviceScope dsc(c->device);
         if (!out || reps < 1) fail(HEOM_E_ARG, "null output or reps < 1");
         heom_solve_opts o{};
         o.crit = 1.0;

@@ -11,7 +11,9 @@
 // reads back, so nothing has to start at zero.  The first call on a device looks up the
 // array's device address (cudaGetSymbolAddress, with that device current); make that
 // first call before any stream capture.  Two calls that overlap in time (two host threads,
-// or two contexts on one device) share the scratch and race: serialise them.
+// or two contexts on one device) share the scratch and race: serialise them.  The kernel
+// runs on the context's non-blocking stream, which is not ordered after the caller's
+// streams, so the states must be complete when the call is made.
 #include <mutex>
 
 #include "context.cuh"
@@ -79,7 +81,7 @@ extern "C" int heom_batch_current_static(heom_ctx *c, const void *x_dev, int32_t
         if (vstride < c->lunk + 1) fail(HEOM_E_ARG, "vstride is shorter than lunk + 1");
         const int ns = c->nalf * c->nspin;
         if (ns > kSlots) fail(HEOM_E_ARG, "more than 4 lead/spin slots");
-        CK(cudaSetDevice(c->device));
+        DeviceScope dsc(c->device);
         double *scr = scratch_on(c->device);
         k_batch_current<<<nbatch, kThreads, 0, c->stream>>>((const double2 *)x_dev, vstride, c->d_cur_terms,
                                                             c->n_cur_terms, ns, scr);

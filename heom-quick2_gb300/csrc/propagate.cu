@@ -217,7 +217,7 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
         require_ctx(c);
         if (!rho || nstep < 0 || !(dt > 0)) fail(HEOM_E_ARG, "bad propagation arguments");
         if (method != HEOM_PROP_RK4 && method != HEOM_PROP_CHEBYSHEV) fail(HEOM_E_ARG, "unknown propagation method");
-        CK(cudaSetDevice(c->device));
+        DeviceScope dsc(c->device);
         const int ns = c->nalf * c->nspin;
         PropBuffers B(c, 5, (int64_t)nstep * ns);
         B.dt = dt;

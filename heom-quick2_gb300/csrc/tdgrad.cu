@@ -88,7 +88,7 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
         require_ctx(c);
         if (!rho0 || !integral || !dintegral || nstep < 1 || !(dt > 0)) fail(HEOM_E_ARG, "bad arguments");
         if (!c->has_adj) fail(HEOM_E_ARG, "the context was created without the adjoint plan");
-        CK(cudaSetDevice(c->device));
+        DeviceScope dsc(c->device);
         const int ck = checkpoint_every > 0 ? checkpoint_every : 32;
         const int64_t N = c->lunk + 1, L = c->lunk;
         const int ns = c->nalf * c->nspin;

@@ -21,6 +21,13 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libheom_gb300.so")
 
 PREC_FP64, PREC_MIXED, PREC_MIXED_FP32, PREC_FP64_REFINED = 0, 1, 2, 3
+# instances per call of heom_batch_current_static (the size of its static device scratch)
+STATIC_CURRENT_MAX = 4096
+
+
+def static_current_chunks(n, limit=STATIC_CURRENT_MAX):
+    """(first instance, count) of the consecutive calls that cover n instances."""
+    return [(b0, min(limit, n - b0)) for b0 in range(0, n, limit)]
 PROP_RK4, PROP_CHEBYSHEV = 0, 1
 ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "out of memory", -4: "unsupported",
           -5: "TFQMR breakdown", -6: "not converged", -7: "device wait timed out"}
@@ -571,12 +578,17 @@ class Batch:
         return info
 
     def currents_static(self, x_dev, nbatch=None, vstride=None):
-        """Lead currents jt[b, ialf, ispin] of device states, without device allocation."""
+        """Lead currents jt[b, ialf, ispin] of device states, without device allocation.
+
+        The C entry point takes at most STATIC_CURRENT_MAX instances per call; larger batches
+        go through it in consecutive chunks of the same device array."""
         n = self.nbatch if nbatch is None else nbatch
+        vs = self.stride if vstride is None else vstride
         ns = self.ctx.model.nalf * self.ctx.model.nspin
         jt = np.zeros(n * ns)
-        _check(lib().heom_batch_current_static(self.ctx.h, C.c_void_p(x_dev), n,
-                                                self.stride if vstride is None else vstride, jt.ctypes.data))
+        for b0, cnt in static_current_chunks(n):
+            _check(lib().heom_batch_current_static(self.ctx.h, C.c_void_p(x_dev + b0 * vs * 16), cnt, vs,
+                                                    jt[b0 * ns:].ctypes.data))
         return jt.reshape(n, self.ctx.model.nspin, self.ctx.model.nalf).transpose(0, 2, 1)
 
     def close(self):

@@ -7,7 +7,9 @@
  * that owns the device copies.  All entry points return 0 on success or a
  * negative HEOM_E* code and never abort; heom_last_error() describes the failure.
  * A context is single-stream and not thread-safe, like the reference routines
- * (whose SAVE counters make them non-reentrant).
+ * (whose SAVE counters make them non-reentrant).  Every entry point makes the
+ * context's device current for the duration of the call and gives the caller's
+ * current device back on return.
  *
  * Complex data are double _Complex / float _Complex, i.e. interleaved (re, im),
  * which is complex(c_double_complex) in ISO_C_BINDING.  Table values keep the
@@ -252,7 +254,9 @@ void heom_batch_destroy(heom_batch *b);
  * serves callers that must not allocate between solver rounds or time steps (cudaFree
  * synchronises the whole device).  The first call on a device does a one-time address
  * lookup and should come before any stream capture; calls that overlap in time share the
- * scratch and race. */
+ * scratch and race.  The kernel runs on the context's own (non-blocking) stream, which is
+ * not ordered after the caller's streams: x_dev must be complete when the call is made
+ * (e.g. the caller synchronises the stream that wrote it). */
 int heom_batch_current_static(heom_ctx *ctx, const void *x_dev, int32_t nbatch, int64_t vstride, double *jt);
 
 /* Measurement hook: time `reps` back-to-back applies on `nbatch` instances on device, in

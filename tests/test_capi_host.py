@@ -67,3 +67,37 @@ def test_context_without_a_device_fails_loudly():
     with pytest.raises(heomq.HeomError) as e:
         heomq.Context(m)
     assert "device" in str(e.value).lower() or "cuda" in str(e.value).lower()
+
+
+def test_static_currents_are_requested_in_chunks_of_the_scratch_size(monkeypatch):
+    """Batches above the static scratch's 4096 instances go through the C entry point in
+    consecutive chunks: each call gets the offset device address, its count and the matching
+    slice of the host output (the C call is replaced by a recorder; nothing runs on a device)."""
+    assert heomq.static_current_chunks(4096) == [(0, 4096)]
+    assert heomq.static_current_chunks(9000) == [(0, 4096), (4096, 4096), (8192, 808)]
+    assert heomq.static_current_chunks(0) == []
+
+    calls = []
+
+    class FakeLib:
+        @staticmethod
+        def heom_batch_current_static(h, xptr, n, vs, out_ptr):
+            calls.append((xptr.value, n, vs, out_ptr))
+            return 0
+
+    class FakeModel:
+        nalf, nspin = 2, 2
+
+    class FakeCtx:
+        h = None
+        model = FakeModel()
+
+    monkeypatch.setattr(heomq, "lib", lambda: FakeLib)
+    b = heomq.Batch.__new__(heomq.Batch)
+    b.ctx, b.nbatch, b.stride = FakeCtx(), 9000, 128
+    jt = b.currents_static(1 << 20)
+    assert jt.shape == (9000, 2, 2)
+    assert [(x - (1 << 20)) // (128 * 16) for x, _, _, _ in calls] == [0, 4096, 8192]
+    assert [n for _, n, _, _ in calls] == [4096, 4096, 808]
+    assert all(vs == 128 for _, _, vs, _ in calls)
+    assert calls[1][3] - calls[0][3] == 4096 * 4 * 8   # output slice of the second chunk
