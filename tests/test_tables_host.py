@@ -170,3 +170,17 @@ def test_correlation_function_pattern_rejects_a_bad_spin_orbital(pair):
     p, _ = pair
     with pytest.raises(heomq.HeomError):
         p.cf_pattern(p.norbs + 1, 1)
+
+
+def test_initial_guess_matches_oracle(pair):
+    """heom_model_initial_guess (main/analyze_hs.f90:144-283 + fermion/initialize1_spa.f90:32-236)
+    against orc_initial_guess: the Boltzmann RDO at the lead-1 temperature on the RDO pattern,
+    every ADO zero.  The two diagonalise H with different eigensolvers, so the entries agree
+    to rounding; the ADO part is exactly zero in both."""
+    p, o = pair
+    g, h = p.initial_guess(), o.initial_guess()
+    nz = int(o.get("nnz_spa")[0])
+    assert g.shape == h.shape
+    np.testing.assert_allclose(g[:nz], h[:nz], rtol=0, atol=1e-12)
+    assert not np.any(g[nz:]) and not np.any(h[nz:])
+    assert abs(sum(g[q] for q in range(nz) if p.array("irow_spa")[q] == p.array("icol_spa")[q]) - 1) < 1e-12
