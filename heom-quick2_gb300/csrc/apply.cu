@@ -41,12 +41,13 @@ __global__ void k_fill_gdiag(DevPlan P, DevCoef<T> C, typename Num<T>::V *gdiag)
 }
 
 template <typename T>
-void fill_gdiag(const DevPlan &P, const DevCoef<T> &C, typename Num<T>::V *gdiag, int nbatch, cudaStream_t s)
+void fill_gdiag(const DevPlan &P, DevCoef<T> &C, typename Num<T>::V *ws, int nbatch, cudaStream_t s)
 {
     dim3 grid((unsigned)std::max(1, std::min(1024, (P.nado + 255) / 256)), (unsigned)nbatch);
     DevCoef<T> K = C;
     K.gdiag = nullptr;
-    k_fill_gdiag<T><<<grid, 256, 0, s>>>(P, K, gdiag);
+    k_fill_gdiag<T><<<grid, 256, 0, s>>>(P, K, ws);
+    C.gdiag = ws;
 }
 
 template <typename T, bool ADJ>
@@ -92,9 +93,9 @@ void scale_rows(const DevPlan &P, const float *pre, typename Num<T>::V *v, int n
 template void scale_rows<double>(const DevPlan &, const float *, double2 *, int, int64_t, cudaStream_t);
 template void scale_rows<float>(const DevPlan &, const float *, float2 *, int, int64_t, cudaStream_t);
 template void scale_rows<DF>(const DevPlan &, const float *, float4 *, int, int64_t, cudaStream_t);
-template void fill_gdiag<double>(const DevPlan &, const DevCoef<double> &, double2 *, int, cudaStream_t);
-template void fill_gdiag<float>(const DevPlan &, const DevCoef<float> &, float2 *, int, cudaStream_t);
-template void fill_gdiag<DF>(const DevPlan &, const DevCoef<DF> &, float4 *, int, cudaStream_t);
+template void fill_gdiag<double>(const DevPlan &, DevCoef<double> &, double2 *, int, cudaStream_t);
+template void fill_gdiag<float>(const DevPlan &, DevCoef<float> &, float2 *, int, cudaStream_t);
+template void fill_gdiag<DF>(const DevPlan &, DevCoef<DF> &, float4 *, int, cudaStream_t);
 template void launch_apply<double, false>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
 template void launch_apply<double, true>(const DevPlan &, const DevCoef<double> &, const double2 *, double2 *, int, int64_t, const int *, cudaStream_t);
 template void launch_apply<float, false>(const DevPlan &, const DevCoef<float> &, const float2 *, float2 *, int, int64_t, const int *, cudaStream_t);

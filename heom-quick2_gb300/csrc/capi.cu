@@ -92,7 +92,12 @@ void PlanDev::release()
 
 template <> DevCoef<double> PlanDev::coef<double>() const { DevCoef<double> c; c.g0 = g0_64; c.cl = cl_64; c.cr = cr_64; return c; }
 template <> DevCoef<float> PlanDev::coef<float>() const { DevCoef<float> c; c.g0 = g0_32; c.cl = cl_32; c.cr = cr_32; return c; }
-template <> DevCoef<DF> PlanDev::coef<DF>() const { DevCoef<DF> c; c.g0 = g0_df; c.cl = cl_df; c.cr = cr_df; return c; }
+template <> DevCoef<DF> PlanDev::coef<DF>() const
+{
+    DevCoef<DF> c;
+    c.g0 = g0_df; c.cl = cl_df; c.cr = cr_df;
+    return c;
+}
 
 }  // namespace heom
 
@@ -109,6 +114,7 @@ heom_ctx::~heom_ctx()
 
 struct heom_batch {
     heom_ctx *ctx = nullptr;
+    int device = 0;   // the context's device (destroy may run after the context is gone)
     int nbatch = 0;
     int64_t vs = 0;
     double2 *h64 = nullptr;
@@ -443,9 +449,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         // (rhs == nullptr) is solved on the regularised operator
         DevCoef<T> KI = rhs ? KT : regularised<T>(c, KT);
         // per-instance ADO diagonals, so the inner applies do no FP64 arithmetic
-        CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * std::max<int64_t>(1, (int64_t)PV.nado * nbatch)));
+        CK(cudaMalloc((void **)&gd, sizeof(typename Num<T>::V) * gdiag_elems<T>(PV, nbatch)));
         fill_gdiag<T>(PV, KI, gd, nbatch, c->stream);
-        KI.gdiag = gd;
         aux++;
         // left diagonal preconditioning: the inner problem M A d = M r with M = diag(1 / (|g0_n|
         // + ||H||_inf)) per ADO evens out the rows of the hierarchy's tiers (about half the
@@ -572,9 +577,8 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         double2 *gd64 = nullptr;
         CK(cudaMalloc((void **)&gd64, sizeof(double2) * std::max<int64_t>(1, (int64_t)PV.nado * nbatch)));
         tmp.push_back(gd64);
-        fill_gdiag<double>(PV, K.k64, gd64, nbatch, c->stream);
+        fill_gdiag<double>(PV, k64, gd64, nbatch, c->stream);
         aux++;
-        k64.gdiag = gd64;
         if (o.precision == HEOM_PREC_FP64) {
             TfqWork<double> W;
             tfq_alloc<double>(W, nbatch, N, c->stream);
@@ -835,6 +839,69 @@ int heom_calc_ax_fp32_dev(heom_ctx *c, const void *dx, void *dy)
     });
 }
 
+}  // extern "C"
+
+namespace {
+// y = the operator of the mixed-precision inner solves (regularised; rows scaled by the inner
+// preconditioner when precond) in the number type T, on device vectors of lunk + 1 values
+template <typename T>
+void inner_operator(heom_ctx *c, bool precond, const void *dx, void *dy)
+{
+    const DevPlan &P = c->dfwd.view;
+    DevCoef<T> K = regularised<T>(c, ctx_coef<T>(c, false));
+    typename Num<T>::V *ws = nullptr;
+    float *pre = nullptr;
+    CK(cudaMalloc((void **)&ws, sizeof(typename Num<T>::V) * gdiag_elems<T>(P, 1)));
+    try {
+        fill_gdiag<T>(P, K, ws, 1, c->stream);
+        if (precond) {
+            CK(cudaMalloc((void **)&pre, sizeof(float) * std::max(1, P.nado)));
+            fill_pre(P, c->dfwd.g0_64, hs_inf_norm(c), pre, c->stream);
+            K.pre = pre;
+        }
+        launch_apply<T, false>(P, K, (const typename Num<T>::V *)dx, (typename Num<T>::V *)dy, 1, c->lunk + 1, nullptr,
+                               c->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(c->stream));
+    } catch (...) { cudaFree(ws); if (pre) cudaFree(pre); throw; }
+    CK(cudaFree(ws));
+    if (pre) CK(cudaFree(pre));
+}
+}  // namespace
+
+extern "C" {
+
+int heom_calc_ax_inner_dev(heom_ctx *c, int32_t precision, int32_t precond, const void *dx, void *dy)
+{
+    return guarded([&] {
+        require_ctx(c);
+        DeviceScope dsc(c->device);
+        if (!dx || !dy) fail(HEOM_E_ARG, "null vector");
+        if (precision == HEOM_PREC_MIXED) inner_operator<DF>(c, precond != 0, dx, dy);
+        else if (precision == HEOM_PREC_MIXED_FP32) inner_operator<float>(c, precond != 0, dx, dy);
+        else if (precision == HEOM_PREC_FP64_REFINED || precision == HEOM_PREC_FP64) inner_operator<double>(c, precond != 0, dx, dy);
+        else fail(HEOM_E_ARG, "unknown precision");
+    });
+}
+
+int heom_calc_ax_fp32x2_dev(heom_ctx *c, const void *dx, void *dy)
+{
+    return guarded([&] {
+        require_ctx(c);
+        DeviceScope dsc(c->device);
+        DevCoef<DF> K = ctx_coef<DF>(c, false);
+        float4 *ws = nullptr;
+        CK(cudaMalloc((void **)&ws, sizeof(float4) * gdiag_elems<DF>(c->dfwd.view, 1)));
+        try {
+            fill_gdiag<DF>(c->dfwd.view, K, ws, 1, c->stream);
+            launch_apply<DF, false>(c->dfwd.view, K, (const float4 *)dx, (float4 *)dy, 1, c->lunk + 1, nullptr, c->stream);
+            CK(cudaGetLastError());
+            CK(cudaStreamSynchronize(c->stream));
+        } catch (...) { cudaFree(ws); throw; }
+        CK(cudaFree(ws));
+    });
+}
+
 int heom_calc_atrx(heom_ctx *c, int64_t ldim, const double _Complex *x, double _Complex *y)
 {
     return guarded([&] {
@@ -941,6 +1008,7 @@ int heom_batch_create(heom_ctx *c, int32_t nbatch, const double _Complex *hs_bat
         *out = nullptr;
         std::unique_ptr<heom_batch> B(new heom_batch());
         B->ctx = c;
+        B->device = c->device;
         B->nbatch = nbatch;
         int64_t N = c->lunk + 1;
         B->vs = (N + 63) / 64 * 64;
@@ -983,7 +1051,7 @@ int64_t heom_batch_stride(const heom_batch *b) { return b ? b->vs : -1; }
 void heom_batch_destroy(heom_batch *b)
 {
     if (!b) return;
-    try { heom::DeviceScope dsc(b->ctx->device); delete b; } catch (...) { delete b; }
+    try { heom::DeviceScope dsc(b->device); delete b; } catch (...) { delete b; }
 }
 
 int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, heom_solve_info *info)
@@ -1068,13 +1136,13 @@ void bench_inputs(heom_ctx *c, int precision, int nbatch, BenchInputs &I)
         else if (precision == HEOM_PREC_MIXED) CK(cudaMemcpyAsync((float4 *)I.hv + b * nh, hdf.data(), 16 * nh, cudaMemcpyHostToDevice, c->stream));
         else CK(cudaMemcpyAsync((float2 *)I.hv + b * nh, h32.data(), 8 * nh, cudaMemcpyHostToDevice, c->stream));
     }
-    I.gdiag = I.alloc(16 * std::max<size_t>(1, (size_t)c->dfwd.view.nado * nbatch));
+    I.gdiag = I.alloc(16 * (size_t)gdiag_elems<DF>(c->dfwd.view, nbatch));
     if (precision == HEOM_PREC_MIXED || precision == HEOM_PREC_MIXED_FP32) {
         I.pre = (float *)I.alloc(sizeof(float) * std::max(1, c->dfwd.view.nado));
         fill_pre(c->dfwd.view, c->dfwd.g0_64, hs_inf_norm(c), I.pre, c->stream);
     }
     if (precision == HEOM_PREC_MIXED) {
-        DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = I.es;
+        DevCoef<DF> K = main_coef<DF>(c, false); K.eshift = I.es; K.hval = (const float4 *)I.hv;
         fill_gdiag<DF>(c->dfwd.view, K, (float4 *)I.gdiag, nbatch, c->stream);
     } else if (precision == HEOM_PREC_MIXED_FP32) {
         DevCoef<float> K = main_coef<float>(c, false); K.eshift = I.es;

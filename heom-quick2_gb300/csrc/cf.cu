@@ -47,6 +47,7 @@ using namespace heom;
 
 struct heom_cf {
     heom_ctx *ctx = nullptr;
+    int device = 0;   // the context's device (destroy may run after the context is gone)
     int iorbs = 0, ispin = 0, nrho = 0;
     int64_t lunkcf = 0, nunk = 0;
     // host copies: cf pattern, steady pattern (for the right-hand sides), a_{iorbs,ispin}
@@ -195,7 +196,6 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
         // per-instance ADO diagonals: keeps the lead-shift sums out of the per-entry work
         double2 *gd = (double2 *)dmalloc(sizeof(double2) * (size_t)P.nado * nb);
         fill_gdiag<double>(P, K, gd, nb, c->stream);
-        K.gdiag = gd;
         cudaStream_t s = c->stream;
         ApplyFn<double> op = [P, K, nb, vs, s](const double2 *x, double2 *y, const int *act) {
             launch_apply_cf(P, K, x, y, nb, vs, act, s);
@@ -234,9 +234,8 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
                     for (int64_t i = 0; i < N; i++)
                         rt[i] = Num<DF>::store_host(Num<DF>::from_d(cf->rt_host[2 * i], cf->rt_host[2 * i + 1]));
                     CK(cudaMemcpyAsync(IW.rt, rt.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, c->stream));
-                    CK(cudaMalloc((void **)&gdd, sizeof(float4) * (size_t)P.nado * nb));
+                    CK(cudaMalloc((void **)&gdd, sizeof(float4) * (size_t)gdiag_elems<DF>(P, nb)));
                     fill_gdiag<DF>(P, KD, gdd, nb, c->stream);
-                    KD.gdiag = gdd;
                     // with the inner preconditioner of the mixed solves
                     float *pre = (float *)dmalloc(sizeof(float) * std::max(1, P.nado));
                     fill_pre(P, K.g0, hs_inf_norm(c), pre, c->stream);
@@ -405,6 +404,7 @@ int heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf
         DeviceScope dsc(ctx->device);
         std::unique_ptr<heom_cf> cf(new heom_cf());
         cf->ctx = ctx;
+        cf->device = ctx->device;
         cf->iorbs = cft->iorbs; cf->ispin = cft->ispin; cf->nrho = t->nrho;
         cf->lunkcf = cft->lunkcf_spa; cf->nunk = t->nunk;
         const int64_t nu = t->nunk, L = cft->lunkcf_spa;
@@ -444,7 +444,7 @@ int heom_cf_create(heom_ctx *ctx, const heom_tables *t, const heom_cf_tables *cf
 void heom_cf_destroy(heom_cf *cf)
 {
     if (!cf) return;
-    try { heom::DeviceScope dsc(cf->ctx->device); delete cf; } catch (...) { delete cf; }
+    try { heom::DeviceScope dsc(cf->device); delete cf; } catch (...) { delete cf; }
 }
 
 int64_t heom_cf_lunk(const heom_cf *cf) { return cf ? cf->lunkcf : -1; }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "numeric.cuh"
@@ -54,6 +55,10 @@ struct DevCoef {
     const float *pre = nullptr;
 };
 
+// Elements of type Num<T>::V that fill_gdiag needs for nbatch instances (the ADO diagonals).
+template <typename T>
+inline int64_t gdiag_elems(const DevPlan &P, int nbatch) { return std::max<int64_t>(1, (int64_t)P.nado * nbatch); }
+
 // pre[n] = 1 / (|g0[n]| + hnorm): the inverse size of ADO n's diagonal block
 void fill_pre(const DevPlan &P, const double2 *g0, double hnorm, float *pre, cudaStream_t s);
 // v[t] *= pre[ent_ado[t]] for the stored entries t < lunk of nbatch vectors of stride vstride
@@ -62,9 +67,10 @@ void scale_rows(const DevPlan &P, const float *pre, typename Num<T>::V *v, int n
 
 // y = A x (ADJ = false) or y = A^H x (ADJ = true) for nbatch instances (gridDim.y);
 // vstride = complex elements between instance vectors; active[b] == 0 skips instance b.
-// gdiag[b * nado + n] = g0_scale g0[n] + i sum_k cnt_k(n) eshift[b][k]
+// fill_gdiag writes into ws (gdiag_elems<T> elements) the per-instance ADO diagonals
+// g[b][n] = g0_scale g0[n] + i sum_k cnt_k(n) eshift[b][k] and points C.gdiag at them.
 template <typename T>
-void fill_gdiag(const DevPlan &P, const DevCoef<T> &C, typename Num<T>::V *gdiag, int nbatch, cudaStream_t s);
+void fill_gdiag(const DevPlan &P, DevCoef<T> &C, typename Num<T>::V *ws, int nbatch, cudaStream_t s);
 
 template <typename T, bool ADJ>
 void launch_apply(const DevPlan &P, const DevCoef<T> &C, const typename Num<T>::V *x, typename Num<T>::V *y,

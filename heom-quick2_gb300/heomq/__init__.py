@@ -115,6 +115,8 @@ SIGNATURES = {
     "heom_calc_ax_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "heom_calc_atrx_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "heom_calc_ax_fp32_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_calc_ax_fp32x2_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_calc_ax_inner_dev": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_solve_tfqmr": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_current": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "heom_occupation": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -309,6 +311,7 @@ class Context:
         _check(lib().heom_ctx_create(C.byref(model.tables), C.byref(o), C.byref(h)))
         self.h = h
         self.lunk = model.lunk
+        self.device = device
 
     def close(self):
         if getattr(self, "h", None) and _lib is not None:
@@ -329,6 +332,43 @@ class Context:
         y = np.zeros(self.lunk, dtype=np.complex128)
         _check(lib().heom_calcderiv(self.h, float(t), x.ctypes.data, y.ctypes.data))
         return y
+
+    def _device_apply(self, fn, x, precision):
+        """Run a device-vector apply fn(dx, dy) on x (lunk + 1 complex values) in the number
+        type of `precision`: FP32x2 splits x into FP32 high and low parts (float4 per value)."""
+        import torch
+
+        x = _c128(x, self.lunk + 1)
+        if precision == PREC_MIXED:
+            parts = []
+            for comp in (x.real, x.imag):
+                hi = comp.astype(np.float32)
+                parts.append((hi, (comp - hi.astype(np.float64)).astype(np.float32)))
+            v = np.stack([parts[0][0], parts[1][0], parts[0][1], parts[1][1]], axis=1)
+        elif precision == PREC_MIXED_FP32:
+            v = np.stack([x.real, x.imag], axis=1).astype(np.float32)
+        else:
+            v = np.stack([x.real, x.imag], axis=1)
+        with torch.cuda.device(self.device):
+            xd = torch.from_numpy(np.ascontiguousarray(v)).to(f"cuda:{self.device}")
+            yd = torch.zeros_like(xd)
+            torch.cuda.synchronize(self.device)
+            _check(fn(C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr())))
+            y = yd.cpu().numpy().astype(np.float64)
+        if precision == PREC_MIXED:
+            return (y[:, 0] + y[:, 2]) + 1j * (y[:, 1] + y[:, 3])
+        return y[:, 0] + 1j * y[:, 1]
+
+    def calc_ax_fp32x2(self, x):
+        """y = A x in the FP32x2 arithmetic of the mixed-precision inner solves (the unregularised
+        operator): x is split into FP32 high and low parts, y returned as hi + lo in FP64."""
+        return self._device_apply(lambda dx, dy: lib().heom_calc_ax_fp32x2_dev(self.h, dx, dy), x, PREC_MIXED)
+
+    def calc_ax_inner(self, x, precision=PREC_MIXED, precond=True):
+        """The operator of the mixed-precision inner solves (regularised, rows scaled by the inner
+        preconditioner when precond) in the arithmetic of `precision`, on a host vector."""
+        return self._device_apply(lambda dx, dy: lib().heom_calc_ax_inner_dev(self.h, precision, int(precond), dx, dy),
+                                  x, precision)
 
     def calc_atrx(self, x):
         x = _c128(x, self.lunk + 1)
@@ -584,6 +624,8 @@ class Batch:
         go through it in consecutive chunks of the same device array."""
         n = self.nbatch if nbatch is None else nbatch
         vs = self.stride if vstride is None else vstride
+        if n < 1 or n > self.nbatch:
+            raise HeomError(-1, f"nbatch {n} outside 1..{self.nbatch} (the vectors of this batch)")
         ns = self.ctx.model.nalf * self.ctx.model.nspin
         jt = np.zeros(n * ns)
         for b0, cnt in static_current_chunks(n):

@@ -145,6 +145,19 @@ int heom_calc_atrx(heom_ctx *ctx, int64_t ldim, const double _Complex *x, double
 int heom_calc_ax_dev(heom_ctx *ctx, const void *dx, void *dy);
 int heom_calc_atrx_dev(heom_ctx *ctx, const void *dx, void *dy);
 int heom_calc_ax_fp32_dev(heom_ctx *ctx, const void *dx, void *dy);
+/* The FP32x2 apply of the mixed-precision inner solves (the unregularised operator): dx, dy
+ * hold lunk_spa + 1 values as float4 (re_hi, im_hi, re_lo, im_lo), each value hi + lo.  No
+ * reference counterpart (the reference has no mixed precision); it exposes the packed
+ * double-float kernel for checks against the FP64 apply. */
+int heom_calc_ax_fp32x2_dev(heom_ctx *ctx, const void *dx, void *dy);
+/* The operator of the mixed-precision inner solves: the regularised operator (A on the
+ * Hermitian part of the RDO block, the regularising blocks on the rest, the trace unknown on
+ * the RDO diagonal) with, when precond != 0, every row of ADO n scaled by the inner
+ * preconditioner 1 / (|sum of its damping rates| + ||H||_inf).  precision selects the number
+ * type of dx, dy (lunk_spa + 1 values each): HEOM_PREC_MIXED float4 (FP32x2, as in
+ * heom_calc_ax_fp32x2_dev), HEOM_PREC_MIXED_FP32 float2, HEOM_PREC_FP64(_REFINED) double2.
+ * No reference counterpart; it lets the inner arithmetic be checked against FP64. */
+int heom_calc_ax_inner_dev(heom_ctx *ctx, int32_t precision, int32_t precond, const void *dx, void *dy);
 
 /* Steady state by TFQMR (solve_tfqmr, tfqmr_double/solve_tfqmr.f90:1). */
 typedef struct {

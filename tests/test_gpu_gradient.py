@@ -123,3 +123,52 @@ def test_autograd_wrappers_match_the_entry_points():
     jp = hag.chebyshev_current_integral(torch.tensor(1.3 + h, dtype=torch.float64), m, rho_eq, 0.05, 40, 8).item()
     jm = hag.chebyshev_current_integral(torch.tensor(1.3 - h, dtype=torch.float64), m, rho_eq, 0.05, 40, 8).item()
     assert abs(amp.grad.item() - (jp - jm) / (2 * h)) <= 1e-6 * abs((jp - jm) / (2 * h))
+
+
+def test_full_size_gradients_match_central_differences():
+    """The adjoint gradients at the size of the gradient configuration: the serial double dot
+    at tier 4 with Pade M = 3 (393 812 entries).  Steady dI_L/d{V, Gamma, U} against central
+    differences (h = 1e-4, steady states refined to 1e-12) within 1e-6; the gradient of
+    int I_L dt over 1000 Chebyshev steps of 0.05 from the V = 0 steady state under the step
+    bias 0.8, with checkpoints every 32 steps (td/chebyshev.f90:160-200 run backwards),
+    against central differences of two forward runs (h = 1e-5) within 1e-6."""
+    p0 = dict(V=0.8, gamma=0.5, U=2.0, eps=-1.0)
+
+    def cfg(**over):
+        p = dict(p0)
+        p.update(over)
+        return cf.dqd(ntier=5, nmats=3, **p)
+
+    def current(c):
+        ctx = heomq.Context(heomq.Model(c), adjoint=False)
+        rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+        assert info.converged
+        return ctx.current(rho)[0].sum()
+
+    m = heomq.Model(cfg())
+    du, de = m.get("dhs_du", m.nrho ** 2, np.complex128), m.get("dhs_deps", m.nrho ** 2, np.complex128)
+    ctx = heomq.Context(m, dhs=(du, de))
+    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    assert info.converged
+    deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / HB
+    dI, _ = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF, crit=1e-12)
+    for k, key in enumerate(("V", "gamma", "U")):
+        h = 1e-4 * max(1.0, abs(p0[key]))
+        fd = (current(cfg(**{key: p0[key] + h})) - current(cfg(**{key: p0[key] - h}))) / (2 * h)
+        assert abs(dI[k] - fd) <= 1e-6 * abs(fd), (key, dI[k], fd)
+    ctx.close()
+
+    c0 = heomq.Context(heomq.Model(cfg(V=0.0)), adjoint=False)
+    rho_eq, _ = c0.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    amps, tchar = m.field()
+    ctx = heomq.Context(m)
+    J, dJ = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32)
+
+    def integral(scale):
+        c = heomq.Context(m, adjoint=False, amps=scale * amps, tchar=tchar)
+        _, jt = c.propagate(rho_eq, 0.0, 0.05, 1000, method=heomq.PROP_CHEBYSHEV, currents=True)
+        return 0.05 * jt[:, 0::m.nalf].sum()
+
+    assert abs(J / integral(1.0) - 1) < 1e-12
+    fd = (integral(1 + 1e-5) - integral(1 - 1e-5)) / 2e-5
+    assert abs(dJ - fd) <= 1e-6 * abs(fd), (dJ, fd)

@@ -41,8 +41,16 @@ def test_static_currents_match_heom_current_twice(cfg):
 
 
 def test_static_currents_reject_oversize_batches():
+    """The C entry point refuses more than 4096 instances and a stride shorter than a vector
+    before it launches anything (the buffer here holds one instance); the Python wrapper
+    refuses to read beyond its own batch."""
     m, ctx, batch, x = _batch_states(cf.siam(ntier=3, nmats=2), [0.4])
+    jt = np.zeros(4097 * 4)
+    rc = heomq.lib().heom_batch_current_static(ctx.h, x.data_ptr(), 4097, batch.stride, jt.ctypes.data)
+    assert rc == -1 and "4096" in heomq.lib().heom_last_error().decode()
+    rc = heomq.lib().heom_batch_current_static(ctx.h, x.data_ptr(), 1, m.lunk, jt.ctypes.data)
+    assert rc == -1
     with pytest.raises(heomq.HeomError):
-        batch.currents_static(x.data_ptr(), nbatch=4097)
-    with pytest.raises(heomq.HeomError):
-        batch.currents_static(x.data_ptr(), vstride=m.lunk)
+        batch.currents_static(x.data_ptr(), nbatch=2)
+    # the context still works after the refusals
+    np.testing.assert_array_equal(batch.currents_static(x.data_ptr()), batch.currents_static(x.data_ptr()))
