@@ -33,6 +33,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="bias points per solve (per GPU)")
     ap.add_argument("--crit", type=float, default=1e-9)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the records of the other configurations (crit 1e-10, the 128-instance sweep, "
+                         "the Kanamori batch, the gradients) that follow the headline")
     ap.add_argument("--profile", action="store_true",
                     help="profiler run: warm-up solves, then one timed mixed solve; prints one short line")
     ap.add_argument("--profile-inner", action="store_true",
@@ -161,6 +164,182 @@ def cpu_reference(cfgs, nthreads, crit):
     return dt, m.current(rho)[0].sum(), info
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), and its logical core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not name:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return name or "unknown", os.cpu_count() or 1
+
+
+def cpu_one_thread_sample(cfg, applies_per_solve, napply=3):
+    """The oracle's apply on one host thread: napply applies timed, scaled to one solve by the
+    applies the FP64 TFQMR takes (the vector updates of TFQMR are a few percent beside them)."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_ffi
+
+    m = oracle_ffi.Model(cfg)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(m.lunk + 1) + 1j * rng.standard_normal(m.lunk + 1)
+    m.calc_ax(x, nthreads=1)
+    t0 = time.perf_counter()
+    for _ in range(napply):
+        x = m.calc_ax(x * 1e-3, nthreads=1)
+    t_apply = (time.perf_counter() - t0) / napply
+    return t_apply, 1.0 / (t_apply * applies_per_solve)
+
+
+def sweep_record(crit):
+    """The batched I-V sweep: 128 single-orbital instances with uneven hierarchies (seed
+    20261203: V ~ U[-1, 1], U in {1, 2, 3}, eps = -U/2, tier in {2, 3, 4}), solved group by
+    group (heomq.sweep); wall time includes the host set-up of the tables.  Errors against the
+    same sweep refined in FP64 to ||b - A x|| <= 1e-12."""
+    import numpy as np
+
+    import heomq
+    from heomq import sweep
+
+    cfgs = heomq.models.iv_sweep(128, seed=20261203)
+    out = {"instances": len(cfgs), "groups": len(sweep.group_instances(cfgs)), "crit": crit}
+    ref, _ = sweep.solve_sweep(cfgs, crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    for key, prec in (("mixed", heomq.PREC_MIXED), ("fp64", heomq.PREC_FP64)):
+        sweep.solve_sweep(cfgs, crit=crit, precision=prec)            # warm-up
+        t0 = time.perf_counter()
+        cur, infos = sweep.solve_sweep(cfgs, crit=crit, precision=prec)
+        wall = time.perf_counter() - t0
+        dev = sum(i.seconds for i in infos)
+        out[key] = {"wall_s": wall, "device_s": dev, "solves_per_s": len(cfgs) / wall,
+                    "worst_current_rel_err": float(np.max(np.abs(cur - ref) / np.abs(ref))),
+                    "converged": all(bool(i.converged) for i in infos)}
+    return out
+
+
+def kanamori_record(crit):
+    """The three-orbital Kanamori impurity (nd = 64, tier 2, Pade M = 6, T = 0.05), four bias
+    points in one batch, mixed precision against the plain FP64 TFQMR (which stalls near 4e-8
+    on this batch), and both against FP64 inner solves refined to 1e-12."""
+    import numpy as np
+    import torch
+
+    import heomq
+
+    m = heomq.Model(heomq.models.HUND_L2)
+    ctx = heomq.Context(m, adjoint=False)
+    Vs = [0.4 + 0.8 * b / 3 for b in range(4)]
+    hb = 0.658211928
+    es = np.array([[V / 2, V / 2, -V / 2, -V / 2] for V in Vs]) / hb
+    es = np.ascontiguousarray(es.reshape(4, 2, 2).transpose(0, 2, 1).reshape(4, 4))
+    batch = heomq.Batch(ctx, eshift_batch=es, nbatch=4)
+    L = m.lunk
+    x0 = torch.zeros((4, batch.stride), dtype=torch.complex128, device="cuda")
+    x0[:, :L] = torch.from_numpy(m.initial_guess()).cuda()
+    x = torch.empty_like(x0)
+
+    def solve(prec, c, refine=8):
+        x.copy_(x0)
+        torch.cuda.synchronize()
+        info = batch.solve_dev(x.data_ptr(), crit=c, precision=prec, max_refine=refine, check=False)
+        return info, np.array([ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(4)])
+
+    iref, ref = solve(heomq.PREC_FP64_REFINED, 1e-12, 16)
+    out = {"workload": "Kanamori 3-orbital nd=64, tier 2 (7477 ADOs, 464968 entries), M=6, T=0.05, 4 bias points",
+           "crit": crit, "reference_resid": iref.resid}
+    for key, prec in (("mixed", heomq.PREC_MIXED), ("fp64", heomq.PREC_FP64)):
+        info, cur = solve(prec, crit)
+        out[key] = {"device_s": info.seconds, "applies": info.iters, "converged": bool(info.converged),
+                    "resid": info.resid, "worst_current_rel_err": float(np.max(np.abs(cur - ref) / np.abs(ref)))}
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["device_s"] / out["mixed"]["device_s"]
+    batch.close()
+    ctx.close()
+    return out
+
+
+def gradient_record():
+    """Adjoint gradients on the headline model (double dot, tier 4, M = 3): the steady
+    dI_L/d{V, Gamma, U, eps} by the adjoint solve, against central differences (h = 1e-4,
+    steady states refined to 1e-12); and the gradient of int I_L dt over 1000 Chebyshev steps of
+    0.05 from the V = 0 steady state under the step bias 0.8, with checkpoints every 32 steps,
+    against central differences of two forward runs (h = 1e-5)."""
+    import heomq
+
+    hb = 0.658211928
+    p0 = dict(V=0.8, gamma=0.5, U=2.0, eps=-1.0)
+
+    def cfg(**over):
+        p = dict(p0)
+        p.update(over)
+        return heomq.models.dqd(ntier=5, nmats=3, **p)
+
+    def current(c):
+        m = heomq.Model(c)
+        ctx = heomq.Context(m, adjoint=False)
+        rho, _ = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+        return ctx.current(rho)[0].sum()
+
+    m = heomq.Model(cfg())
+    nd2 = m.nrho ** 2
+    import numpy as np
+
+    du, de = m.get("dhs_du", nd2, np.complex128), m.get("dhs_deps", nd2, np.complex128)
+    ctx = heomq.Context(m, dhs=(du, de))
+    rho, _ = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / hb
+    t0 = time.perf_counter()
+    dI, ainfo = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF,
+                                    crit=1e-12)
+    t_adj = time.perf_counter() - t0
+    steady = {"adjoint_s": t_adj, "adjoint_applies": ainfo.iters, "dI": dict(zip(("V", "gamma", "U", "eps"), map(float, dI)))}
+    rel = {}
+    for k, key in enumerate(("V", "gamma", "U")):
+        h = 1e-4 * max(1.0, abs(p0[key]))
+        fd = (current(cfg(**{key: p0[key] + h})) - current(cfg(**{key: p0[key] - h}))) / (2 * h)
+        rel[key] = abs(dI[k] - fd) / abs(fd)
+    steady["rel_err_vs_central_differences"] = rel
+    ctx.close()
+    # time-dependent: from the V = 0 steady state, 1000 Chebyshev steps of 0.05 under the step bias
+    m0 = heomq.Model(cfg(V=0.0))
+    c0 = heomq.Context(m0, adjoint=False)
+    rho_eq, _ = c0.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    c0.close()
+    amps, tchar = m.field()
+    ctx = heomq.Context(m)
+    t0 = time.perf_counter()
+    J, dJ = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32)
+    t_grad = time.perf_counter() - t0
+
+    def integral(scale):
+        c = heomq.Context(m, adjoint=False, amps=scale * amps, tchar=tchar)
+        t = time.perf_counter()
+        _, jt = c.propagate(rho_eq, 0.0, 0.05, 1000, method=heomq.PROP_CHEBYSHEV, currents=True)
+        dt = time.perf_counter() - t
+        c.close()
+        return 0.05 * jt[:, 0::m.nalf].sum(), dt
+
+    jp, t_fwd = integral(1 + 1e-5)
+    jm, _ = integral(1 - 1e-5)
+    fd = (jp - jm) / 2e-5
+    ctx.close()
+    td = {"steps": 1000, "dt": 0.05, "checkpoint_every": 32, "forward_s": t_fwd, "gradient_s": t_grad,
+          "dJ_dA": dJ, "central_difference": fd, "rel_err": abs(dJ - fd) / abs(fd)}
+    return {"model": "serial double dot nd=16, tier 4, M=3", "steady": steady, "chebyshev": td}
+
+
 def run_reference(args, ws, rank, dist):
     import heomq.models as models
 
@@ -182,6 +361,7 @@ def run_reference(args, ws, rank, dist):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": WORKLOAD, "batch": 1, "crit": args.crit, "solver": "TFQMR FP64 (oracle restatement)"},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                         "cpu_model": cpu_model()[0],
                          "sample": "one full FP64 TFQMR solve of one bias point per step (OpenMP over ADOs)"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -271,21 +451,22 @@ def run_gb300(args, ws, rank, local, dist):
 
     # FP64 timing beside (one step, after the timed region)
     t64 = info64.seconds
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: every step copies the initial guesses
+    # and the lead shifts in (the batch shares the context's H, which is not sent) and the
+    # steady states out; the median over the same number of steps as the headline
     pinned = torch.empty((B, L), dtype=torch.complex128, pin_memory=True)
     rhos = pinned.numpy()
-    hs_b = None
     e2e_times = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(args.steps):
         rhos[:] = x0h
         t0 = time.perf_counter()
-        out, info_e = ctx.solve_batch(rhos, hs_batch=hs_b, eshift_batch=es_cm, crit=args.crit,
-                                      precision=heomq.PREC_MIXED, inplace=True)
+        out, info_e = ctx.solve_batch(rhos, eshift_batch=es_cm, crit=args.crit, precision=heomq.PREC_MIXED,
+                                      inplace=True)
         jt = [ctx.current(out[b])[0].sum() for b in range(B)]
         e2e_times.append(time.perf_counter() - t0)
-    e2e_value = ws * B / statistics.median(e2e_times)
-    h2d = B * L * 16 + B * 4 * 8 + B * model.nrho ** 2 * 16
-    d2h = B * L * 16
+    e2e_value = ws * B / max_over_ranks(statistics.median(e2e_times), dist, device="cuda")
+    h2d = rhos.nbytes + es_cm.nbytes
+    d2h = rhos.nbytes
 
     # roofline of the dominant kernel: the first fused kernel of an inner TFQMR iteration
     # (apply of w + the first half of the vector updates) over the batch; the second one and
@@ -307,11 +488,31 @@ def run_gb300(args, ws, rank, local, dist):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        nthreads = os.cpu_count() or 1
-        dt, jcpu, _ = cpu_reference([heomq.models.dqd(ntier=5, nmats=3, V=Vs[0])], nthreads, args.crit)
-        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": nthreads, "kind": "port",
+        model_name, nthreads = cpu_model()
+        cfg0 = heomq.models.dqd(ntier=5, nmats=3, V=Vs[0])
+        dt, jcpu, cinfo = cpu_reference([cfg0], nthreads, args.crit)
+        t1, v1 = cpu_one_thread_sample(cfg0, info64.iters)
+        cpu = {"value": 1.0 / dt, "unit": "solves/s", "cores": nthreads, "kind": "port", "cpu_model": model_name,
                "sample": f"one FP64 TFQMR solve of one bias point (V={Vs[0]:.2f}) by the C oracle, OpenMP over ADOs",
-               "current_rel_diff_vs_gpu_fp64": abs(jcpu - cur64[0]) / abs(cur64[0])}
+               "current_rel_diff_vs_gpu_fp64": abs(jcpu - cur64[0]) / abs(cur64[0]),
+               "one_thread": {"value": v1, "unit": "solves/s", "cores": 1, "apply_s": t1,
+                              "sample": f"3 applies of the oracle on one thread, scaled by the {info64.iters} "
+                                        "applies of the FP64 TFQMR solve"}}
+    configs = None
+    if rank == 0 and not args.no_configs:
+        # the criterion of the mixed-versus-FP64 configuration (FP64 refinement to 1e-10)
+        ts, c10 = [], None
+        for _ in range(3):
+            i10 = step(heomq.PREC_MIXED, crit=1e-10)
+            ts.append(i10.seconds)
+        c10 = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
+        configs = {
+            "crit_1e-10": {"solves_per_s": B / statistics.median(ts), "applies_per_solve": i10.iters,
+                           "resid": i10.resid, "current_rel_err": max(abs(a - b) / abs(b) for a, b in zip(c10, curt))},
+            "iv_sweep_128": sweep_record(args.crit),
+            "kanamori_nd64": kanamori_record(args.crit),
+            "gradients_dqd_L4": gradient_record(),
+        }
 
     if rank == 0:
         line = {
@@ -328,7 +529,7 @@ def run_gb300(args, ws, rank, local, dist):
                        "speedup_mixed_vs_fp64": (ws * B / t_step) / (ws * B / t64),
                        "current_rel_err_mixed": err, "current_rel_err_fp64": err64,
                        "current_reference": "steady state refined with FP64 inner solves to ||b - A x|| <= 1e-12",
-                       "current_reference_resid": info_ref.resid},
+                       "current_reference_resid": info_ref.resid, "other_configurations": configs},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_in_b<FP32x2, regularised>: apply of w plus the fused vector updates, over the batch",

@@ -22,6 +22,7 @@ struct heom_model {
     int norbs = 0, nspin = 0, nalf = 0, nmats = 0, ntier = 0, ncor = 0, nopr = 0, nvar = 0, nrho = 0, nams = 0;
     std::vector<double> cpcoef;
     std::vector<cd> cppole;                       // (nmats, 2)
+    std::vector<cd> psfcoef, psfpole;             // Prony scheme: the caller's fitted table (npsf)
     std::vector<cd> cb, cdd, cgama, cgamma;
     std::vector<double> dipm, eleadinfty, amps, tcharv, hybrid;
     std::vector<int32_t> mpm, morbs, mspin, ilead, mcor, mopr, iredex, indexdraw, jredex, jomit;
@@ -245,24 +246,39 @@ void build_hs(heom_model &m) {
 void build_coefficients(heom_model &m) {
     const heom_params &p = m.p;
     const double hb = heom::kHbar;
-    m.ncor = 1 + m.nmats;
+    const bool psf = p.npsf > 0;
+    double width[2] = {p.bandwidth[0], p.bandwidth[1]};
+    if (psf) {
+        // psfjob (main/evaluatepara.f90:256-722, 1187-1189): the npsf fitted terms replace the
+        // Drude pole and the Pade terms; the band half-width is rpsf * T, centred at 0
+        if (p.npsf > 64 || !p.psf_coef || !p.psf_pole || !(p.tpsf > 0) || !(p.rpsf > 0))
+            heom::fail(HEOM_E_ARG, "the Prony scheme needs 1..64 coefficients and poles, tpsf > 0 and rpsf > 0");
+        const cd *zc = reinterpret_cast<const cd *>(p.psf_coef), *zp = reinterpret_cast<const cd *>(p.psf_pole);
+        m.psfcoef.assign(zc, zc + p.npsf);
+        m.psfpole.assign(zp, zp + p.npsf);
+        m.nmats = p.npsf;
+        m.ncor = m.nmats;
+        for (int a = 0; a < m.nalf; a++) width[a] = p.temperature[a] * p.rpsf;
+    } else {
+        m.ncor = 1 + m.nmats;
+        pade(m.nmats, m.cpcoef, m.cppole);
+    }
     m.nopr = 2 * m.norbs * m.nspin * m.nalf;
     m.nvar = m.nopr * m.ncor;
     m.nrho = 1;
     for (int k = 0; k < m.norbs; k++) m.nrho *= 2 * m.nspin;
-    pade(m.nmats, m.cpcoef, m.cppole);
     std::vector<double> zxip((size_t)m.nalf * m.norbs), lw((size_t)m.nalf * m.norbs);
     for (int a = 0; a < m.nalf; a++)
         for (int o = 0; o < m.norbs; o++) {
             lw[a * m.norbs + o] = p.linewidth[a][o];
-            zxip[a * m.norbs + o] = p.linewidth[a][o] * p.bandwidth[a] * p.bandwidth[a] * 0.5;
+            zxip[a * m.norbs + o] = p.linewidth[a][o] * width[a] * width[a] * 0.5;
         }
     if (p.doubledot) {
         if (m.norbs != 2 || m.nalf != 2) heom::fail(HEOM_E_ARG, "doubledot needs norbs=2 and nalf=2");
         lw[0 * 2 + 1] = 0; lw[1 * 2 + 0] = 0;
         std::fill(zxip.begin(), zxip.end(), 0.0);
-        zxip[0] = p.linewidth[0][0] * p.bandwidth[0] * p.bandwidth[0] * 0.5;
-        zxip[1 * 2 + 1] = p.linewidth[1][1] * p.bandwidth[1] * p.bandwidth[1] * 0.5;
+        zxip[0] = p.linewidth[0][0] * width[0] * width[0] * 0.5;
+        zxip[1 * 2 + 1] = p.linewidth[1][1] * width[1] * width[1] * 0.5;
     }
     m.hybrid.resize(lw.size());
     for (size_t k = 0; k < lw.size(); k++) m.hybrid[k] = lw[k] / hb;
@@ -273,10 +289,15 @@ void build_coefficients(heom_model &m) {
         for (int s = 1; s <= m.nspin; s++)
             for (int o = 1; o <= m.norbs; o++)
                 for (int a = 1; a <= m.nalf; a++) {
-                    double T = p.temperature[a - 1], W = p.bandwidth[a - 1], zx = zxip[(a - 1) * m.norbs + (o - 1)];
+                    double T = p.temperature[a - 1], W = width[a - 1], zx = zxip[(a - 1) * m.norbs + (o - 1)];
                     for (int k = 1; k <= m.ncor; k++) {
                         size_t id = cbidx(m, o, s, k, a, sg);
-                        if (k == 1) {   // Drude pole of the Lorentzian band, Pade-expanded Fermi function
+                        if (psf) {      // fitted exponential k: T / tpsf (zpole, zcoef 2 zxip / W^2)
+                            const double sc = T / p.tpsf;
+                            m.cgama[id] = sc * m.psfpole[k - 1];
+                            m.cb[id] = sc * m.psfcoef[k - 1] * (zx / (W * W) * 2.0);
+                            m.cdd[id] = std::conj(m.cb[id]);
+                        } else if (k == 1) {   // Drude pole of the Lorentzian band, Pade-expanded Fermi function
                             m.cgama[id] = cd(-W, 0) / hb;
                             cd f1 = fermi_pade(m, sg, cd(0, W / T));
                             cd f2 = fermi_pade(m, 3 - sg, cd(0, W / T));

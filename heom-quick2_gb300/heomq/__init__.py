@@ -68,6 +68,8 @@ class Params(C.Structure):
         ("uu1", C.c_double), ("uu2", C.c_double), ("u12", C.c_double), ("t12", C.c_double),
         ("kan_u", C.c_double), ("kan_j", C.c_double), ("kan_eps", C.c_double),
         ("hs_in", C.c_void_p), ("tchar", (C.c_double * 2) * 2),
+        ("npsf", C.c_int32), ("tpsf", C.c_double), ("rpsf", C.c_double), ("psf_coef", C.c_void_p),
+        ("psf_pole", C.c_void_p),
     ]
 
 
@@ -197,7 +199,30 @@ def make_params(cfg):
     p.model = cfg["model"]
     for k in ("eup", "edown", "uu", "e1up", "e1down", "e2up", "e2down", "uu1", "uu2", "u12", "t12", "kan_u", "kan_j", "kan_eps"):
         setattr(p, k, float(cfg.get(k, 0.0)))
+    psf = cfg.get("psf")
+    if psf:
+        # Prony scheme (psfjob): the fitted table the caller supplies (coefficients, poles, the
+        # fit's reference temperature tpsf and band ratio rpsf)
+        p._psf = (_c128(psf["coef"]), _c128(psf["pole"]))
+        p.npsf = len(p._psf[0])
+        p.tpsf, p.rpsf = float(psf["tpsf"]), float(psf["rpsf"])
+        p.psf_coef, p.psf_pole = p._psf[0].ctypes.data, p._psf[1].ctypes.data
     return p
+
+
+def psf_table_from_pade(nmats, W, T, tpsf=1.0):
+    """The Drude pole and the [nmats-1/nmats] Pade terms of a Lorentzian band of half-width W at
+    temperature T written as a Prony table (coefficients, poles) for the same band: the
+    exponentials of the Pade scheme in the form the Prony scheme takes them (one set of poles
+    for both signs, cb = T / tpsf coef linewidth, cgama = T / tpsf pole).  A table in the
+    reference's itype_psf form is used the same way."""
+    m = Model(dict(norbs=1, nspin=2, nalf=1, nmats=nmats, ntier=2, bandwidth=[W, W], linewidth=[[1.0], [1.0]],
+                   temperature=[T, T], engyshift=[[0.0, 0.0], [0.0, 0.0]], model=1))
+    ncor = nmats + 1
+    cb = m.array("cb").reshape(1, 2, ncor, 1, 2, order="F")          # cb(norbs, nspin, ncor, nalf, nsgn)
+    cgamma = m.array("cgamma")[:ncor]                                 # sign +, spin 1: the ncor drawers
+    s = T / tpsf
+    return {"coef": cb[0, 0, :, 0, 0] / s, "pole": cgamma / s, "tpsf": tpsf, "rpsf": W / T}   # linewidth 1
 
 
 class Model:

@@ -125,16 +125,25 @@ def parse(text):
     return pos, groups, tchar
 
 
-def to_config(text, hamil_sys=None):
+def to_config(text, hamil_sys=None, psf_tables=None):
     """Model configuration (heomq.Model argument) and solver options of an input file.
-    hamil_sys: H (nrho x nrho, internal units) when $hamil_sys lreadhs = T."""
+    hamil_sys: H (nrho x nrho, internal units) when $hamil_sys lreadhs = T.
+    psf_tables: for $jobinfo psfjob = T, the fitted Prony tables by itype_psf ({itype: {"coef",
+    "pole", "tpsf", "rpsf"}}, the contents of main/zpout_psf.f90's tables); the reference's own
+    tables are not part of this library."""
     pos, g, tchar = parse(text)
     job = g.get("jobinfo", {})
     if not job.get("lsparse", False):
         raise ValueError("only the sparse path (lsparse = T) is supported")
-    if not job.get("psdjob", False):
-        raise ValueError("only the Pade spectrum decomposition (psdjob = T) is supported")
-    for flag in ("mfdjob", "pfdjob", "psfjob", "psdlor", "psdfff", "lsimple", "ltrun_der"):
+    psf = None
+    if job.get("psfjob", False):
+        itype = int(job.get("itype_psf", 1))                       # main/main.f90:177 default
+        if not psf_tables or itype not in psf_tables:
+            raise ValueError(f"psfjob = T needs the fitted Prony table itype_psf = {itype} (psf_tables)")
+        psf = psf_tables[itype]
+    elif not job.get("psdjob", False):
+        raise ValueError("only the Pade (psdjob = T) and Prony (psfjob = T) decompositions are supported")
+    for flag in ("mfdjob", "pfdjob", "psdlor", "psdfff", "lsimple", "ltrun_der"):
         if job.get(flag, False):
             raise ValueError(f"{flag} = T is not supported")
     if g.get("adiabatic", {}).get("lad", False):
@@ -148,6 +157,9 @@ def to_config(text, hamil_sys=None):
                engyshift=pos["engyshift"], lscreen=int(bool(job.get("lscreen", False))),
                doubledot=int(bool(g.get("ddots", {}).get("doubledot", False))),
                tchar=(tchar if tchar else 0.0))
+    if psf is not None:
+        cfg["psf"] = psf
+        cfg["nmats"] = len(psf["coef"])
     hs = None
     if g.get("hamil_sys", {}).get("lreadhs", False):
         if hamil_sys is None:
@@ -169,11 +181,11 @@ def to_config(text, hamil_sys=None):
     return cfg, hs, opts
 
 
-def model_from_input(text, hamil_sys=None):
+def model_from_input(text, hamil_sys=None, psf_tables=None):
     """heomq.Model of an input file, with its solver options."""
     from . import Model
 
-    cfg, hs, opts = to_config(text, hamil_sys)
+    cfg, hs, opts = to_config(text, hamil_sys, psf_tables)
     return Model(cfg, hs=hs), opts
 
 

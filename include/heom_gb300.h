@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define HEOM_ABI_VERSION 2
+#define HEOM_ABI_VERSION 3
 
 enum {
     HEOM_OK = 0,
@@ -98,6 +98,15 @@ typedef struct {
     double kan_u, kan_j, kan_eps;
     const double _Complex *hs_in;     /* model 9: nrho*nrho, internal units */
     double tchar[2][2];               /* fieldtype = 0 switch-on time of the lead shift */
+    /* Prony scheme (psfjob, main/zpout_psf.f90; cb, cd, cgama at main/evaluatepara.f90:1993-2000):
+     * npsf > 0 replaces the Drude pole and the Pade terms by npsf fitted exponentials (nmats is
+     * then taken as npsf).  The caller supplies the fitted table: psf_coef and psf_pole (zcoef and
+     * zpole of zpout_psf; one set of poles serves both signs), the fit's reference temperature
+     * tpsf and its band ratio rpsf (band half-width rpsf * T, centred at 0).  The reference's
+     * built-in itype_psf tables are not part of this library. */
+    int32_t npsf;
+    double tpsf, rpsf;
+    const double _Complex *psf_coef, *psf_pole;
 } heom_params;
 
 typedef struct heom_model heom_model;

@@ -55,6 +55,12 @@ typedef struct {
     const ozc *hs_in;                            /* model READHS: nrho*nrho, internal units */
     double tchar[ORC_MAXALF][2];                 /* fieldtype=0 switch-on time */
     unsigned long long pattern_seed;             /* seed of the random mixing in the pattern build */
+    /* Prony scheme (psfjob, main/zpout_psf.f90): npsf > 0 replaces the Drude pole and the Pade
+     * terms by npsf fitted exponentials, zcoef = psf_coef, zpole = psf_pole (the same for both
+     * signs), fitted at temperature tpsf for a band of half-width rpsf * T centred at 0 */
+    int npsf;
+    double tpsf, rpsf;
+    const ozc *psf_coef, *psf_pole;
 } orc_params;
 
 typedef struct {
@@ -64,6 +70,10 @@ typedef struct {
     /* Pade decomposition (main/zpout_psd.f90) */
     double cpcoef[ORC_MAXMATS];
     ozc cppole[ORC_MAXMATS][2];
+    /* Prony scheme (main/zpout_psf.f90): fitted coefficients and poles, npsf of them */
+    int npsf;
+    double tpsf;
+    ozc psfcoef[ORC_MAXMATS], psfpole[ORC_MAXMATS];
     /* bath coefficients, laid out as cb(norbs,nspin,ncor,nalf,nsgn) */
     ozc *cb, *cd, *cgama;
     ozc *cgamma; double *dipm;                       /* per drawer */

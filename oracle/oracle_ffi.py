@@ -25,6 +25,7 @@ class Params(C.Structure):
         ("uu1", C.c_double), ("uu2", C.c_double), ("u12", C.c_double), ("t12", C.c_double),
         ("kan_u", C.c_double), ("kan_j", C.c_double), ("kan_eps", C.c_double),
         ("hs_in", C.c_void_p), ("tchar", (C.c_double * 2) * MAXALF), ("pattern_seed", C.c_ulonglong),
+        ("npsf", C.c_int), ("tpsf", C.c_double), ("rpsf", C.c_double), ("psf_coef", C.c_void_p), ("psf_pole", C.c_void_p),
     ]
 
 
@@ -105,6 +106,13 @@ def make_params(cfg):
     for k in ("eup", "edown", "uu", "e1up", "e1down", "e2up", "e2down", "uu1", "uu2", "u12", "t12", "kan_u", "kan_j", "kan_eps"):
         setattr(p, k, float(cfg.get(k, 0.0)))
     p.pattern_seed = int(cfg.get("pattern_seed", 20261203))
+    psf = cfg.get("psf")
+    if psf:
+        # Prony scheme: the fitted table (coefficients, poles) the caller supplies
+        p._psf = (np.ascontiguousarray(psf["coef"], dtype=np.complex128), np.ascontiguousarray(psf["pole"], dtype=np.complex128))
+        p.npsf = len(p._psf[0])
+        p.tpsf, p.rpsf = float(psf["tpsf"]), float(psf["rpsf"])
+        p.psf_coef, p.psf_pole = p._psf[0].ctypes.data, p._psf[1].ctypes.data
     return p
 
 
@@ -116,6 +124,7 @@ class Model:
         if hs is not None:
             self._hs = np.ascontiguousarray(np.asarray(hs, dtype=np.complex128).reshape(-1, order="F"))
             p.hs_in = self._hs.ctypes.data
+        self._params = p
         h = C.c_void_p()
         if lib().orc_build(C.byref(p), C.byref(h)) != 0:
             raise RuntimeError("oracle build failed: " + lib().orc_last_error().decode())

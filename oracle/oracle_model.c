@@ -359,22 +359,38 @@ static int orc_build_coefficients(orc_model *m, const orc_params *p)
     const double hb = ORC_HBAR;
     m->nsgn = 2;
     m->ndrude = 1;             /* yshift = 1e10 > bandwidth (evaluatepara.f90:978,1166-1185) */
+    double width[ORC_MAXALF];
+    for (int a = 0; a < m->nalf; a++) width[a] = p->bandwidth[a];
+    m->npsf = p->npsf > 0 ? p->npsf : 0;
+    if (m->npsf) {
+        /* psfjob (evaluatepara.f90:256-722, 1187-1189): nmats = npsf fitted terms, no Drude
+         * pole, bandwidth = dinvbeta * rpsf, band centre 0 */
+        if (m->npsf > ORC_MAXMATS || !p->psf_coef || !p->psf_pole || !(p->tpsf > 0) || !(p->rpsf > 0)) {
+            orc_set_error("psfjob needs 1..64 coefficients and poles, tpsf > 0, rpsf > 0");
+            return -1;
+        }
+        m->ndrude = 0;
+        m->nmats = m->npsf;
+        m->tpsf = p->tpsf;
+        for (int k = 0; k < m->npsf; k++) { m->psfcoef[k] = p->psf_coef[k]; m->psfpole[k] = p->psf_pole[k]; }
+        for (int a = 0; a < m->nalf; a++) width[a] = p->temperature[a] * p->rpsf;
+    }
     m->ncor = m->ndrude + m->nmats;
     m->nopr = m->nsgn * m->norbs * m->nspin * m->nalf;
     m->nvar = m->nopr * m->ncor;
     m->nrho = 1; for (int k = 0; k < m->norbs; k++) m->nrho *= m->nspin * 2;
-    orc_pade(m->nmats, m->cpcoef, m->cppole);
+    if (!m->npsf) orc_pade(m->nmats, m->cpcoef, m->cppole);
     /* zxip (offcor = F) */
     for (int a = 0; a < m->nalf; a++) for (int o = 0; o < m->norbs; o++)
-        m->zxip[a][o] = p->linewidth[a][o] * p->bandwidth[a] * p->bandwidth[a] * 0.5;
+        m->zxip[a][o] = p->linewidth[a][o] * width[a] * width[a] * 0.5;
     double lw[ORC_MAXALF][ORC_MAXORB];
     for (int a = 0; a < m->nalf; a++) for (int o = 0; o < m->norbs; o++) lw[a][o] = p->linewidth[a][o];
     if (p->doubledot) {
         if (m->norbs != 2 || m->nalf != 2) { orc_set_error("doubledot needs norbs=2,nalf=2"); return -1; }
         lw[0][1] = 0.0; lw[1][0] = 0.0;
         for (int a = 0; a < 2; a++) for (int o = 0; o < 2; o++) m->zxip[a][o] = 0.0;
-        m->zxip[0][0] = lw[0][0] * p->bandwidth[0] * p->bandwidth[0] * 0.5;
-        m->zxip[1][1] = lw[1][1] * p->bandwidth[1] * p->bandwidth[1] * 0.5;
+        m->zxip[0][0] = lw[0][0] * width[0] * width[0] * 0.5;
+        m->zxip[1][1] = lw[1][1] * width[1] * width[1] * 0.5;
     }
     for (int a = 0; a < m->nalf; a++) for (int o = 0; o < m->norbs; o++) m->hybrid[a][o] = lw[a][o] / hb;
     size_t ncb = (size_t)m->norbs * m->nspin * m->ncor * m->nalf * m->nsgn;
@@ -382,10 +398,17 @@ static int orc_build_coefficients(orc_model *m, const orc_params *p)
     const double dpm[2] = {1.0, -1.0};
     for (int ni = 1; ni <= 2; ni++) for (int nm = 1; nm <= m->nspin; nm++) for (int nk = 1; nk <= m->norbs; nk++)
     for (int nj = 1; nj <= m->nalf; nj++) for (int np = 1; np <= m->ncor; np++) {
-        double T = p->temperature[nj - 1], beta = 1.0 / T, W = p->bandwidth[nj - 1];
+        double T = p->temperature[nj - 1], beta = 1.0 / T, W = width[nj - 1];
         double zx = m->zxip[nj - 1][nk - 1], gp = W, dwp = 0.0;
         size_t id = CBIDX(m, nk, nm, np, nj, ni);
-        if (np <= m->ndrude) {
+        if (m->npsf) {
+            /* PSF scheme (evaluatepara.f90:1993-2000): cgama = T / tpsf zpole, cb = T / tpsf zcoef
+             * 2 zxip / W^2, cd = conj(cb); the same fit serves both signs (zpout_psf.f90) */
+            const double s = T / m->tpsf;
+            m->cgama[id] = s * m->psfpole[np - 1];
+            m->cb[id] = s * m->psfcoef[np - 1] * (zx / (W * W) * 2.0);
+            m->cd[id] = conj(m->cb[id]);
+        } else if (np <= m->ndrude) {
             m->cgama[id] = (-gp + I * dpm[ni - 1] * dwp) / hb;
             ozc c1 = beta * (dpm[ni - 1] * dwp + I * gp);
             ozc f1 = orc_fermifunc(m, ni, c1);

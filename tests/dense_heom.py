@@ -114,6 +114,20 @@ def lorentz_psd_bath(couplings, W, T, mus, npade):
     return out
 
 
+def exponential_bath(couplings, mus, terms):
+    """Drawers of leads whose correlation functions are given as sums of exponentials in the
+    lead's own frame, C^sigma(t) = g sum_m eta_m exp(-gamma_m t) for both signs (a Prony fit of
+    a band centred at the lead's chemical potential; terms = [(eta_m, gamma_m)] per unit
+    coupling g, rates in 1/ps): the bias moves each exponent by -sigma i mu_alpha / hbar."""
+    out = []
+    for (alpha, mu), g in sorted(couplings.items()):
+        ma = mus[alpha]
+        for sigma in (1, -1):
+            for k, (eta, gam) in enumerate(terms):
+                out.append(Drawer(sigma, alpha, mu, k, gam - sigma * 1j * ma / HBAR, g * eta))
+    return out
+
+
 def discrete_bath(modes):
     """Drawers of discrete bath modes: modes = [(mu, t_k, eps_k, occupation f_k)].  Then
     C^+(t) = sum |t|^2 f e^{i eps t}, C^-(t) = sum |t|^2 (1 - f) e^{-i eps t}: one drawer per

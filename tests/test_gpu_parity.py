@@ -14,6 +14,7 @@ CASES = {
     "dqd_L2": cf.dqd(ntier=3),
     "dqd_L4": cf.CFG1,
     "hund_L2": cf.CFG4,
+    "dqd_L2_prony": dict(cf.dqd(ntier=3, nmats=1, T=0.3), psf=cf.prony_table()),
 }
 
 

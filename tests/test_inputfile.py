@@ -104,9 +104,26 @@ def test_lower_tier_state_seeds_a_higher_tier_job(tmp_path):
     assert not np.any(seeded[low.lunk:])
 
 
+def test_prony_job_reads_the_callers_table():
+    """$jobinfo psfjob = T itype_psf = 3: the fitted table of that type comes from the caller
+    (the reference's built-in tables are not part of the library); without it the job is
+    refused.  Restating the input's own Pade decomposition as a Prony table gives the Pade
+    job's coefficient tables to rounding."""
+    text = SIAM_INPUT.replace("psdjob=T", "psdjob=F psfjob=T itype_psf=3")
+    with pytest.raises(ValueError):
+        inp.to_config(text)
+    tab = heomq.psf_table_from_pade(4, 10.0, 0.1, tpsf=1.5)
+    m, _ = inp.model_from_input(text, psf_tables={3: tab})
+    ref, _ = inp.model_from_input(SIAM_INPUT)
+    for k in ("cb", "cd", "cgamma"):
+        assert np.abs(m.array(k) - ref.array(k)).max() <= 1e-13 * np.abs(ref.array(k)).max(), k
+    for k in TABLES:
+        np.testing.assert_array_equal(m.array(k), ref.array(k), err_msg=k)
+
+
 def test_unsupported_options_are_refused():
     with pytest.raises(ValueError):
-        inp.to_config(SIAM_INPUT.replace("psdjob=T", "psdjob=F psfjob=T"))
+        inp.to_config(SIAM_INPUT.replace("psdjob=T", "psdjob=F pfdjob=T"))
     with pytest.raises(ValueError):
         inp.to_config(SIAM_INPUT.replace("methodss=2", "methodss=0"))
     with pytest.raises(ValueError):
