@@ -42,6 +42,7 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         if (REG) s = N::add(s, N::from_d(0.0, C.reg_scale * N::im(N::load(x[t]))));
         return s;
     }
+    if (C.tier_lim && t >= __ldg(&C.tier_lim[b].y)) return N::zero();   // beyond the instance's tier
     const int n = __ldg(P.ent_ado + t);
     const int off = __ldg(P.ado_off + n);
     const int p = (int)(t - off);
@@ -112,7 +113,8 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
     }
     // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
     A ua = N::zero();
-    const int eu = C.unit_on ? e1 : em;
+    // the last kept tier of a truncated instance has no higher-tier couplings
+    const int eu = (C.unit_on && (ADJ || !C.tier_lim || off < __ldg(&C.tier_lim[b].x))) ? e1 : em;
     for (int e = em; e < eu; e++) {
         const int4 rec = __ldg(P.coup + e);
         const uint32_t mw = __ldg(P.maps + rec.y + p);

@@ -122,7 +122,18 @@ struct heom_batch {
     float2 *h32 = nullptr;
     double *e64 = nullptr;
     int h_real = 0;
-    ~heom_batch() { if (h64) cudaFree(h64); if (hdf) cudaFree(hdf); if (h32) cudaFree(h32); if (e64) cudaFree(e64); }
+    // truncated instances (heom_batch_set_tiers): per instance (first entry of its last kept
+    // tier, one past its last kept entry); nullptr = all at the context's depth
+    int2 *tier_lim = nullptr;
+    std::vector<int2> tier_lim_host;
+    ~heom_batch()
+    {
+        if (h64) cudaFree(h64);
+        if (hdf) cudaFree(hdf);
+        if (h32) cudaFree(h32);
+        if (e64) cudaFree(e64);
+        if (tier_lim) cudaFree(tier_lim);
+    }
 };
 
 namespace heom {
@@ -472,6 +483,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             pre_kappa = lo > 0 ? (double)hi / lo : 1.0;
             pre_max = hi;
         }
+        W.tier_lim = KI.tier_lim;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
         CK(cudaStreamEndCapture(c->stream, &graph));
@@ -582,6 +594,7 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
         if (o.precision == HEOM_PREC_FP64) {
             TfqWork<double> W;
             tfq_alloc<double>(W, nbatch, N, c->stream);
+            W.tier_lim = k64.tier_lim;
             try {
                 upload_rt(c, W);
                 // b = rhs - A x0 per instance, stored with the workspace stride
@@ -772,6 +785,15 @@ int heom_ctx_create(const heom_tables *t, const heom_ctx_opts *opts, heom_ctx **
         CK(cudaMalloc((void **)&c->fy, sizeof(float2) * N));
         CK(cudaMalloc((void **)&c->dscratch, sizeof(double) * 2048));
         drandn_stream(2 * N, c->rt_host);
+        {
+            // stored entries before each tier's first ADO (ADOs that store nothing count zero)
+            c->tier_entry.assign((size_t)t->ntier + 1, c->lunk);
+            int64_t acc = 0, u = 1;
+            for (int it = 1; it <= t->ntier; it++) {
+                for (; u < t->nfirst[it - 1]; u++) acc += t->nnz_spa[u - 1];
+                c->tier_entry[it - 1] = acc;
+            }
+        }
         // (row, col) of every stored entry, 0-based in one byte each, for the per-ADO dense
         // transforms of the Jacobi sweep; the largest |cb| for its shift
         if (c->nrho <= 256) {
@@ -1054,6 +1076,33 @@ void heom_batch_destroy(heom_batch *b)
     try { heom::DeviceScope dsc(b->device); delete b; } catch (...) { delete b; }
 }
 
+int heom_batch_set_tiers(heom_batch *B, const int32_t *ntier)
+{
+    return guarded([&] {
+        if (!B) fail(HEOM_E_ARG, "null batch");
+        heom_ctx *c = B->ctx;
+        require_ctx(c);
+        DeviceScope dsc(c->device);
+        if (!ntier) {   // back to the whole hierarchy for every instance
+            if (B->tier_lim) cudaFree(B->tier_lim);
+            B->tier_lim = nullptr;
+            B->tier_lim_host.clear();
+            return;
+        }
+        std::vector<int2> lim(B->nbatch);
+        for (int b = 0; b < B->nbatch; b++) {
+            const int nt = ntier[b];
+            if (nt < 1 || nt > c->ntier)
+                fail(HEOM_E_ARG, "instance tier count outside 1 .. the context's ntier");
+            lim[b] = make_int2((int)c->tier_entry[nt - 1], (int)c->tier_entry[nt]);
+        }
+        if (!B->tier_lim) CK(cudaMalloc((void **)&B->tier_lim, sizeof(int2) * B->nbatch));
+        CK(cudaMemcpyAsync(B->tier_lim, lim.data(), sizeof(int2) * B->nbatch, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        B->tier_lim_host = lim;
+    });
+}
+
 int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, heom_solve_info *info)
 {
     return guarded([&] {
@@ -1063,6 +1112,15 @@ int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, h
         DevCoef<double> K64 = c->dfwd.coef<double>(); K64.hval = B->h64; K64.eshift = B->e64; K64.h_real = B->h_real;
         DevCoef<DF> KDF = c->dfwd.coef<DF>(); KDF.hval = B->hdf; KDF.eshift = B->e64; KDF.h_real = B->h_real;
         DevCoef<float> K32 = c->dfwd.coef<float>(); K32.hval = B->h32; K32.eshift = B->e64; K32.h_real = B->h_real;
+        if (B->tier_lim) {
+            K64.tier_lim = KDF.tier_lim = K32.tier_lim = B->tier_lim;
+            // a truncated instance's entries beyond its tier start (and stay) zero
+            for (int b = 0; b < B->nbatch; b++) {
+                const int64_t y = B->tier_lim_host[b].y;
+                if (y < c->lunk)
+                    CK(cudaMemsetAsync((double2 *)x_dev + (int64_t)b * B->vs + y, 0, sizeof(double2) * (size_t)(c->lunk - y), c->stream));
+            }
+        }
         heom_solve_info inf;
         solve_device(c, *o, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, CoefSet{K64, K32, KDF});
         if (info) *info = inf;

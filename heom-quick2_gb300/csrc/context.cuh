@@ -132,5 +132,9 @@ struct heom_ctx {
     float2 *fx = nullptr, *fy = nullptr;
     double *dscratch = nullptr;
     std::vector<double> rt_host;                    // drandn stream (2*(lunk+1) reals)
+    // first stored entry of every tier (1-based tier k at index k-1; lunk at index ntier):
+    // the tables are tier-major, so a hierarchy truncated at tier k is the prefix up to
+    // tier_entry[k]
+    std::vector<int64_t> tier_entry;
     ~heom_ctx();
 };

@@ -53,7 +53,23 @@ struct DevCoef {
     // left diagonal preconditioner of the inner solves: every row of ADO n is scaled by
     // pre[n] (the trace slot is not); nullptr = none
     const float *pre = nullptr;
+    // truncated batches (instances of one table family at different hierarchy depths, on the
+    // deepest member's tables): per instance, x = first stored entry of its last kept tier,
+    // y = one past its last kept entry.  Rows from y on are zero, and the rows of the last
+    // kept tier skip their couplings to the next tier (whose entries the caller keeps zero).
+    // nullptr = every instance uses the whole hierarchy.
+    const int2 *tier_lim = nullptr;
 };
+
+// Index of the shadow-vector component that instance b pairs with its entry i (N = lunk + 1
+// elements per vector).  A truncated instance (tier_lim) pairs its trace slot with the
+// component at its own hierarchy's trace index, tier_lim[b].y: its shadow vector is then the
+// one a solve on its own tables uses (the prefix of the same drandn stream), and its Krylov
+// iterates are those of that solve.
+__device__ __forceinline__ int64_t shadow_index(const int2 *tier_lim, int b, int64_t i, int64_t N)
+{
+    return (tier_lim && i == N - 1) ? (int64_t)__ldg(&tier_lim[b].y) : i;
+}
 
 // Elements of type Num<T>::V that fill_gdiag needs for nbatch instances (the ADO diagonals).
 template <typename T>

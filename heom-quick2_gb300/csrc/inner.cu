@@ -123,11 +123,25 @@ __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b
         }
 }
 
-#define FUSED_SETUP                                            \
+// Truncated batches: true (after writing the block's K partials as zero) when every entry
+// of this block lies at or beyond instance b's last kept entry and the block does not hold
+// the trace slot; such a block has nothing to do (the decision is uniform over the block).
+template <typename T, int K>
+__device__ __forceinline__ bool masked_block(const InnerWork<T> &W, int b)
+{
+    if (!W.tier_lim) return false;
+    const int64_t first = (int64_t)blockIdx.x * NT * kEPT, last = first + NT * kEPT - 1;
+    if (first < (int64_t)__ldg(&W.tier_lim[b].y) || last >= W.N - 1) return false;
+    if (threadIdx.x < K) W.part[(3 * (size_t)b + threadIdx.x) * W.nblk + blockIdx.x] = 0.0;
+    return true;
+}
+
+#define FUSED_SETUP(K)                                         \
     using N = Num<T>;                                          \
     using A = typename N::A;                                   \
     const int b = blockIdx.y;                                  \
     if (W.st[b].done) return;                                  \
+    if (masked_block<T, K>(W, b)) return;                      \
     const int64_t o = (int64_t)b * W.vstride;                  \
     const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
 
@@ -150,7 +164,7 @@ __global__ void k_in_init(InnerWork<T> W)
         W.w[o + t] = N::store(bv);
         W.x[o + t] = z; W.xs[o + t] = z; W.xs2[o + t] = z; W.y[o + t] = z; W.d[o + t] = z; W.v[o + t] = z; W.u2[o + t] = z;
         bb.add(bv, bv);
-        rb.add(N::load(W.rt[t]), bv);
+        rb.add(N::load(W.rt[shadow_index(W.tier_lim, b, t, W.N)]), bv);
     }
     const typename WarpAcc<T>::R ws[2] = {bb.warp_sum(), rb.warp_sum()};
     block_partials<T, 2>(ws, W.part, W.nblk, b);
@@ -182,7 +196,7 @@ __global__ void __launch_bounds__(NTF) k_in_init_fin(InnerWork<T> W, double crit
 template <typename T, bool REG, bool CF = false>
 __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
-    FUSED_SETUP
+    FUSED_SETUP(1)
     WarpAcc<T> sg;
 #pragma unroll 1
     for (int e = 0; e < kEPT; e++) {
@@ -201,7 +215,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
         W.y[o + t] = N::store(N::add(N::load(W.w[o + t]), N::scale(y2, k.beta)));
         const A vn = N::add(u1, N::scale(N::add(u2, N::scale(vo, k.beta)), k.beta));
         W.v[o + t] = N::store(vn);
-        sg.add(N::load(W.rt[t]), vn);
+        sg.add(N::load(W.rt[shadow_index(W.tier_lim, b, t, W.N)]), vn);
     }
     const typename WarpAcc<T>::R ws[1] = {sg.warp_sum()};
     block_partials<T, 1>(ws, W.part, W.nblk, b);
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(NTF) k_in_b_fin(InnerWork<T> W)
 template <typename T, bool REG, bool CF = false>
 __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
-    FUSED_SETUP
+    FUSED_SETUP(3)
     WarpAcc<T> a1, a2, a3;
 #pragma unroll 1
     for (int e = 0; e < kEPT; e++) {
@@ -246,7 +260,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
         W.w[o + t] = N::pack(w2);
         a1.add(w1, w1);
         a2.add(w2, w2);
-        a3.add(N::load(W.rt[t]), w2);
+        a3.add(N::load(W.rt[shadow_index(W.tier_lim, b, t, W.N)]), w2);
     }
     const typename WarpAcc<T>::R ws[3] = {a1.warp_sum(), a2.warp_sum(), a3.warp_sum()};
     block_partials<T, 3>(ws, W.part, W.nblk, b);
@@ -322,6 +336,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, Inner
     using A = typename N::A;
     const int b = blockIdx.y;
     if (W.st[b].done && !W.st[b].finishing) return;
+    if (masked_block<T, 1>(W, b)) return;
     const int64_t o = (int64_t)b * W.vstride;
     const int64_t t0 = (int64_t)blockIdx.x * NT * kEPT + threadIdx.x;
     const typename N::V *xc = W.slot(1 - W.st[b].best_slot);

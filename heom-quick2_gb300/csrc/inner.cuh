@@ -57,6 +57,9 @@ struct InnerWork {
     InnerState *st = nullptr;
     InnerCoef<T> *cf = nullptr;
     double *part = nullptr;     // per-block partials: 3 runs of nblk per instance
+    // truncated batches (DevCoef::tier_lim): the apply kernels skip blocks wholly beyond an
+    // instance's last kept entry (their entries stay zero in every vector) and leave zero partials
+    const int2 *tier_lim = nullptr;
     void *mem = nullptr;        // single allocation backing everything above
 };
 

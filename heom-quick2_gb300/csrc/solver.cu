@@ -143,7 +143,7 @@ __global__ void k_init(TfqWork<T> W, double tol, int nlim, double crit, double r
     INST_SETUP
     DotAcc<T> bb, rb;
     for (int64_t i = i0; i < W.N; i += di) {
-        const AA bv = NN::load(W.b[o + i]), r = NN::load(W.rt[i]);
+        const AA bv = NN::load(W.b[o + i]), r = NN::load(W.rt[shadow_index(W.tier_lim, b, i, W.N)]);
         const typename NN::V z = NN::store(NN::zero());
         W.x[o + i] = z; W.v[o + i] = z; W.y[o + i] = z; W.d[o + i] = z; W.u[o + i] = z;
         W.w[o + i] = NN::store(bv);
@@ -250,7 +250,7 @@ __global__ void k_p2(TfqWork<T> W)
         const AA vu = NN::add(NN::scale(NN::load(v_[i]), beta), NN::load(u_[i]));
         const AA v = NN::add(NN::scale(vu, beta), NN::load(t_[i]));
         v_[i] = NN::store(v);
-        sg.add(NN::load(rt_[i]), v);
+        sg.add(NN::load(rt_[shadow_index(W.tier_lim, b, i, W.N)]), v);
     }
     write_partial(W, b, sg.val(), 0.0);
 }
@@ -393,7 +393,7 @@ __global__ void k_p5(TfqWork<T> W)
         const AA w = NN::sub(NN::load(w_[i]), NN::scale(NN::load(u_[i]), al));
         w_[i] = NN::store(w);
         ww.add(w, w);
-        rw.add(NN::load(rt_[i]), w);
+        rw.add(NN::load(rt_[shadow_index(W.tier_lim, b, i, W.N)]), w);
     }
     write_partial(W, b, ww.val(), rw.val());
 }

@@ -23,6 +23,7 @@ struct TfqWork {
     TfqState *st = nullptr;       // device, nbatch
     double *part = nullptr;       // nbatch * nblk * 2
     int *act_main = nullptr, *act_tres = nullptr, *act_chk = nullptr;
+    const int2 *tier_lim = nullptr;   // truncated batches (DevCoef::tier_lim): shadow_index
     void *mem = nullptr;          // single allocation backing everything above
 };
 

@@ -133,6 +133,7 @@ SIGNATURES = {
     "heom_batch_stride": (C.c_int64, [C.c_void_p]),
     "heom_batch_solve_dev": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_batch_destroy": (None, [C.c_void_p]),
+    "heom_batch_set_tiers": (C.c_int, [C.c_void_p, C.c_void_p]),
     "heom_batch_current_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
     "heom_solve_jacobi": (C.c_int, [C.c_void_p, _p(SolveOpts), C.c_double, C.c_void_p, _p(SolveInfo)]),
     "heom_jacobi_shift": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -617,9 +618,12 @@ class CorrFunc:
 
 class Batch:
     """Instances of one table set (bias / level sweeps) solved together; parameters stay on
-    the device.  x_dev: device pointer (int) to nbatch FP64 complex vectors of stride `stride`."""
+    the device.  x_dev: device pointer (int) to nbatch FP64 complex vectors of stride `stride`.
 
-    def __init__(self, ctx, hs_batch=None, eshift_batch=None, nbatch=None):
+    ntier: optional tier count per instance (1 .. the context's ntier): instance b is solved
+    on the hierarchy truncated at ntier[b] tiers, in the context's layout (heom_batch_set_tiers)."""
+
+    def __init__(self, ctx, hs_batch=None, eshift_batch=None, nbatch=None, ntier=None):
         self.ctx = ctx
         if nbatch is None:
             nbatch = len(hs_batch) if hs_batch is not None else len(eshift_batch)
@@ -631,11 +635,22 @@ class Batch:
                                        None if self._es is None else self._es.ctypes.data, C.byref(h)))
         self.h = h
         self.stride = lib().heom_batch_stride(h)
+        self._tiers = None
+        if ntier is not None:
+            self._tiers = np.ascontiguousarray(ntier, dtype=np.int32)
+            if self._tiers.shape != (nbatch,):
+                self.close()
+                raise HeomError(-1, f"ntier needs one tier count per instance ({nbatch})")
+            rc = lib().heom_batch_set_tiers(h, self._tiers.ctypes.data)
+            if rc:
+                msg = lib().heom_last_error().decode()
+                self.close()
+                raise HeomError(rc, msg)
 
     def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True,
-                  stag_window=0):
+                  stag_window=0, inner_precond=0):
         o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine,
-                      stag_window=stag_window)
+                      stag_window=stag_window, inner_precond=inner_precond)
         info = SolveInfo()
         rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
         if check:

@@ -267,6 +267,17 @@ int heom_batch_create(heom_ctx *ctx, int32_t nbatch, const double _Complex *hs_b
 int64_t heom_batch_stride(const heom_batch *b);
 int heom_batch_solve_dev(heom_batch *b, const heom_solve_opts *o, void *x_dev, heom_solve_info *info);
 void heom_batch_destroy(heom_batch *b);
+/* Truncated batches: instance b is solved on the hierarchy truncated at ntier[b] tiers
+ * (1 <= ntier[b] <= the context's ntier; the reference counts the RDO as tier 1, as
+ * in ntier of the input file).  The reference's tables are tier-major (main/ball2drawer.f90,
+ * main/buildcoefindex.f90), so the tables of a shallower hierarchy of the same model family
+ * are a prefix of the context's; one batch then holds instances of several depths and is
+ * solved in one launch sequence.  In place of one heom_ctx per depth (the reference runs
+ * one depth per job).  The states keep the context's layout: the entries beyond an
+ * instance's tier are set to zero by heom_batch_solve_dev and stay zero; the trace slot
+ * stays at the context's lunk.  ntier == NULL returns every instance to the whole
+ * hierarchy. */
+int heom_batch_set_tiers(heom_batch *b, const int32_t *ntier);
 
 /* Lead currents jt[b][ialf + nalf*ispin] (b < nbatch) of nbatch device-resident states
  * x_dev (FP64 complex, instance stride vstride >= lunk + 1 elements, e.g. the vectors of
