@@ -398,10 +398,11 @@ def run_gb300(args, ws, rank, local, dist):
     x0[:, :L] = torch.from_numpy(x0h).to("cuda")
     x = torch.empty_like(x0)
 
-    def step(prec, crit=None, refine=8, check=True):
+    def step(prec, crit=None, refine=8, check=True, interleave=0):
         x.copy_(x0)
         torch.cuda.synchronize()
-        return batch.solve_dev(x.data_ptr(), crit=crit or args.crit, precision=prec, max_refine=refine, check=check)
+        return batch.solve_dev(x.data_ptr(), crit=crit or args.crit, precision=prec, max_refine=refine, check=check,
+                               interleave=interleave)
 
     if args.profile_apply:
         prec = {"fp64": heomq.PREC_FP64, "fp32x2": heomq.PREC_MIXED, "fp32": heomq.PREC_MIXED_FP32}[args.profile_apply]
@@ -419,7 +420,7 @@ def run_gb300(args, ws, rank, local, dist):
         ctx.close()
         return 0
     for _ in range(args.warmup):
-        step(heomq.PREC_MIXED)
+        step(heomq.PREC_MIXED)   # the first two also tune the interleave of the inner kernels
     if args.profile:
         info = step(heomq.PREC_MIXED)
         print(json.dumps({"profile_run": True, "batch": B, "applies": info.iters, "seconds": info.seconds,
@@ -427,6 +428,11 @@ def run_gb300(args, ws, rank, local, dist):
         batch.close()
         ctx.close()
         return 0
+    # the two interleave settings the automatic choice compares, one solve each
+    g_max = 1
+    while g_max < B and g_max < 32:
+        g_max *= 2
+    interleave_ms = {str(g): 1e3 * step(heomq.PREC_MIXED, interleave=g).seconds for g in sorted({1, g_max})}
     # FP64 GPU path beside (same batch, same criterion)
     info64 = step(heomq.PREC_FP64)
     cur64 = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
@@ -527,6 +533,7 @@ def run_gb300(args, ws, rank, local, dist):
                        "l2": f"inputs larger than L2: {B} x 9 solver vectors x {L * 16 / 1e6:.1f} MB",
                        "parallelism": f"replicas x{ws}", "wall_s": wall,
                        "applies_per_solve": infos[-1].iters, "refinements": infos[-1].refinements,
+                       "inner_interleave_ms_per_solve": interleave_ms,
                        "fp64": {"solves_per_s": ws * B / t64, "applies_per_solve": info64.iters,
                                 "apply_us": sec64 * 1e6, "apply_gbs_alg": alg64 / sec64 / 1e9},
                        "speedup_mixed_vs_fp64": (ws * B / t_step) / (ws * B / t64),

@@ -21,25 +21,33 @@
 namespace heom {
 
 template <typename T>
-__device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V *__restrict__ x, const int32_t *pair, int q)
+__device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V *__restrict__ x, const int32_t *pair, int q,
+                                                      int xs)
 {
     using N = Num<T>;
-    return N::half(N::add(N::load(x[q]), N::conj(N::load(x[__ldg(pair + q)]))));
+    return N::half(N::add(N::load(x[(int64_t)q * xs]), N::conj(N::load(x[(int64_t)__ldg(pair + q) * xs]))));
 }
 
-// y[t] of instance b (x: that instance's vector); t in [0, lunk], lunk = the trace slot
-template <typename T, bool ADJ, bool REG, bool CF = false>
+// y[t] of instance b (x: that instance's vector); t in [0, lunk], lunk = the trace slot.
+// Interleaved layout (the fused inner solves): with XS = 0 the stride xs_rt (a power of two)
+// applies: instances interleaved entry by entry in groups of xs_rt, element i of this
+// instance at x[i xs_rt], and the per-instance ADO diagonals and H values interleaved the
+// same way within each group.  XS = 1: one instance per vector (the plain applies).
+template <typename T, bool ADJ, bool REG, bool CF = false, int XS = 1>
 __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, const DevCoef<T> &C,
-                                                          const typename Num<T>::V *__restrict__ x, int64_t t, int b)
+                                                          const typename Num<T>::V *__restrict__ x, int64_t t, int b,
+                                                          int xs_rt = 1)
 {
     using N = Num<T>;
     using A = typename N::A;
+    const int xs = XS > 0 ? XS : xs_rt;
+    const int bg = XS == 1 ? b : b / xs, bl = XS == 1 ? 0 : b - bg * xs;   // group and lane of instance b
     if (t == P.lunk) {   // the trace slot
         A s = N::zero();
         if (!ADJ && C.trace_on)
             for (int k = 0; k < P.ntrace; k++)
-                s = N::add(s, REG ? herm_part<T>(x, C.rdo_pair, P.trace_idx[k]) : N::load(x[P.trace_idx[k]]));
-        if (REG) s = N::add(s, N::from_d(0.0, C.reg_scale * N::im(N::load(x[t]))));
+                s = N::add(s, REG ? herm_part<T>(x, C.rdo_pair, P.trace_idx[k], xs) : N::load(x[(int64_t)P.trace_idx[k] * xs]));
+        if (REG) s = N::add(s, N::from_d(0.0, C.reg_scale * N::im(N::load(x[(int64_t)(t) * xs]))));
         return s;
     }
     if (C.tier_lim && t >= __ldg(&C.tier_lim[b].y)) return N::zero();   // beyond the instance's tier
@@ -47,11 +55,11 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
     const int off = __ldg(P.ado_off + n);
     const int p = (int)(t - off);
     const int c = __ldg(P.ado_cls + n);
-    const typename N::V *hv = C.hval + (int64_t)b * P.nh;
+    const typename N::V *hv = C.hval + (int64_t)bg * P.nh * xs + bl;
 
     // g = sum over the drawers of (cgamma + i dipm eshift)
     A g;
-    if (C.gdiag) g = N::load(C.gdiag[(int64_t)b * P.nado + n]);
+    if (C.gdiag) g = N::load(C.gdiag[(int64_t)bg * P.nado * xs + (int64_t)n * xs + bl]);
     else {
         const unsigned cnt = (unsigned)__ldg(P.ado_cnt + n);
         double es = 0;
@@ -61,17 +69,17 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
     }
     if (ADJ) g = N::conj(g);
     const bool rdo = REG && off == 0;   // output row and same-tier sources in the RDO block
-    A acc = N::mul(g, rdo ? herm_part<T>(x, C.rdo_pair, (int)t) : N::load(x[t]));
+    A acc = N::mul(g, rdo ? herm_part<T>(x, C.rdo_pair, (int)t, xs) : N::load(x[(int64_t)(t) * xs]));
     if (rdo) {
         const int q = (int)t, qp = __ldg(C.rdo_pair + q);
-        const A xq = N::load(x[q]);
-        acc = N::add(acc, N::scale(N::sub(xq, N::conj(N::load(x[qp]))), N::sc(0.5 * C.reg_scale)));
-        if (qp == q) acc = N::add(acc, N::from_d(C.reg_scale * N::re(N::load(x[P.lunk])) / C.ndiag, 0.0));
+        const A xq = N::load(x[(int64_t)(q) * xs]);
+        acc = N::add(acc, N::scale(N::sub(xq, N::conj(N::load(x[(int64_t)(qp) * xs]))), N::sc(0.5 * C.reg_scale)));
+        if (qp == q) acc = N::add(acc, N::from_d(C.reg_scale * N::re(N::load(x[(int64_t)(P.lunk) * xs])) / C.ndiag, 0.0));
     }
     if (CF) {   // dfacta = -s, dfactb = +s (calc_ax_cf_spa_omp.f90:96-105); cf_omega[b] = s w
         const bool hrow = t < C.cf_half;
         const double w = hrow ? -C.cf_omega[b] : C.cf_omega[b];
-        acc = N::add(acc, N::scale(N::load(x[hrow ? t + C.cf_half : t - C.cf_half]), N::sc(w)));
+        acc = N::add(acc, N::scale(N::load(x[(int64_t)(hrow ? t + C.cf_half : t - C.cf_half) * xs]), N::sc(w)));
     }
 
     // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
@@ -81,10 +89,10 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
     A sd = N::zero();
     for (int k = k0; k < k1; k++) {
         const uint32_t w = __ldg(P.terms + k);
-        A h = N::load(hv[(w >> 16) & 0x7FFF]);
+        A h = N::load(hv[(int64_t)((w >> 16) & 0x7FFF) * xs]);
         if (ADJ) h = N::conj(h);
-        const A xs = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF)) : N::load(x[off + (int)(w & 0xFFFF)]);
-        const A hx = C.h_real ? N::scale(xs, N::re_s(h)) : N::mul(h, xs);
+        const A xv = rdo ? herm_part<T>(x, C.rdo_pair, (int)(w & 0xFFFF), xs) : N::load(x[(int64_t)(off + (int)(w & 0xFFFF)) * xs]);
+        const A hx = C.h_real ? N::scale(xv, N::re_s(h)) : N::mul(h, xv);
         sd = N::add(sd, N::flip(hx, (w >> 31) ^ 1u, 0u));
     }
     // forward: acc += i (sum_right - sum_left); adjoint: acc += -i (...)
@@ -102,11 +110,11 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         const bool src_rdo = REG && rec.x == 0;
         const int cid = rec.z & 0x3FFFFFFF;
         if (lo) {
-            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1, xs) : N::load(x[(int64_t)(rec.x + (int)(lo & 0x7FFF) - 1) * xs]);
             acc = N::add(acc, N::mul(N::load(C.cl[cid]), N::flip(v, lo >> 15, cj)));
         }
         if (hi) {
-            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1, xs) : N::load(x[(int64_t)(rec.x + (int)(hi & 0x7FFF) - 1) * xs]);
             acc = N::add(acc, N::mul(N::load(C.cr[cid]), N::flip(v, hi >> 15, cj)));
         }
         if ((e - e0) & 1) acc = N::norm(acc);
@@ -121,11 +129,11 @@ __device__ __forceinline__ typename Num<T>::A apply_entry(const DevPlan &P, cons
         const uint32_t cj = (uint32_t)rec.z >> 31, lo = mw & 0xFFFFu, hi = mw >> 16;
         const bool src_rdo = REG && rec.x == 0;
         if (lo) {
-            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1) : N::load(x[rec.x + (int)(lo & 0x7FFF) - 1]);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(lo & 0x7FFF) - 1, xs) : N::load(x[(int64_t)(rec.x + (int)(lo & 0x7FFF) - 1) * xs]);
             ua = N::add(ua, N::flip(v, ((lo >> 15) ^ (uint32_t)rec.z) & 1u, cj));
         }
         if (hi) {
-            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1) : N::load(x[rec.x + (int)(hi & 0x7FFF) - 1]);
+            const A v = src_rdo ? herm_part<T>(x, C.rdo_pair, (int)(hi & 0x7FFF) - 1, xs) : N::load(x[(int64_t)(rec.x + (int)(hi & 0x7FFF) - 1) * xs]);
             ua = N::add(ua, N::flip(v, ((hi >> 15) ^ ((uint32_t)rec.z >> 1)) & 1u, cj));
         }
         if (((e - e0) & 3) == 3) ua = N::norm(ua);

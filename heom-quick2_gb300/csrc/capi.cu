@@ -436,26 +436,29 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
                   const std::function<void(const double2 *, double2 *)> &residual,
                   const std::function<void(const double2 *)> &batch_norms,
-                  const DevPlan &PV, int64_t N, const double *rt)
+                  const DevPlan &PV, int64_t N)
 {
     constexpr int kInnerChunk = 25;   // 50 applies between residual checks, as in the reference driver
     const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-10);
     InnerWork<T> W;
-    inner_alloc<T>(W, nbatch, N, c->stream);
+    inner_alloc<T>(W, nbatch, N, c->stream, o.interleave);
     typename Num<T>::V *gd = nullptr;
     float *pre = nullptr;
     double pre_kappa = 1.0, pre_max = 1.0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
+    // one graph of a chunk per lane configuration W.GE (instantiated on first use)
+    std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     auto release = [&] {
-        if (gexec) cudaGraphExecDestroy(gexec);
-        if (graph) cudaGraphDestroy(graph);
+        for (auto &g : graphs) {
+            if (g.second.second) cudaGraphExecDestroy(g.second.second);
+            if (g.second.first) cudaGraphDestroy(g.second.first);
+        }
         inner_free(W);
         if (gd) cudaFree(gd);
         if (pre) cudaFree(pre);
     };
     try {
-        upload_rt_to<T>(c, W.rt, N, rt);
+        inner_shadow<T>(W, 0, c->stream);   // sign-symmetric; another one after a round without progress
+        aux++;
         // with a given right-hand side the operator is used as it is; the steady problem
         // (rhs == nullptr) is solved on the regularised operator
         DevCoef<T> KI = rhs ? KT : regularised<T>(c, KT);
@@ -484,11 +487,19 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             pre_max = hi;
         }
         W.tier_lim = KI.tier_lim;
-        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
-        CK(cudaStreamEndCapture(c->stream, &graph));
-        CK(cudaGraphInstantiate(&gexec, graph, 0));
+        KI = inner_layout_coef<T>(W, PV, KI, c->stream);   // the workspace's instance-interleaved layout
+        auto chunk_graph = [&]() -> cudaGraphExec_t {
+            auto it = graphs.find(W.GE);
+            if (it != graphs.end()) return it->second.second;
+            auto &g = graphs[W.GE];
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
+            CK(cudaStreamEndCapture(c->stream, &g.first));
+            CK(cudaGraphInstantiate(&g.second, g.first, 0));
+            return g.second;
+        };
         std::vector<InnerState> st(nbatch);
+        std::vector<int> amap;
         int round = 0;
         std::vector<double> prev;
         for (; round < std::max(1, max_rounds); round++) {
@@ -498,19 +509,19 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             bool all_ok = true;
             for (double v : norms) all_ok = all_ok && v <= o.crit;
             if (all_ok) { converged = true; break; }
-            // a round that did not halve some instance's residual: the inner arithmetic cannot
-            // resolve what is left, so the caller continues with FP64 inner solves
-            if (stall_exit && !prev.empty()) {
+            // a round that did not halve some instance's residual: with stall_exit the inner
+            // arithmetic cannot resolve what is left, and the caller continues with FP64 inner
+            // solves; otherwise the next round's inner solves change their shadow vector
+            if (!prev.empty()) {
                 bool stuck = false;
                 for (int b = 0; b < nbatch; b++) stuck = stuck || (norms[b] > o.crit && norms[b] > 0.5 * prev[b]);
-                if (stuck) { stalled = true; break; }
+                if (stuck && stall_exit) { stalled = true; break; }
+                if (stuck) { inner_shadow<T>(W, round, c->stream); aux++; }   // the next inner solve
             }
             prev = norms;
             for (int b = 0; b < nbatch; b++)   // instances already below crit get b = 0 and stop at once
-                vec_from_d<T>(N, r64 + (int64_t)b * vstride, W.b + (int64_t)b * W.vstride,
-                              norms[b] <= o.crit ? 0.0 : 1.0 / norms[b], c->stream);
+                inner_rhs<T>(W, PV, r64 + (int64_t)b * vstride, b, norms[b] <= o.crit ? 0.0 : 1.0 / norms[b], pre, c->stream);
             aux += nbatch;
-            if (pre) { scale_rows<T>(PV, pre, W.b, nbatch, W.vstride, c->stream); aux++; }
             // the scaled inner problem has ||b|| = 1: stop at max(itol, crit / ||r||) (the most
             // demanding instance sets it), or at the arithmetic's floor
             double tgt = 1.0;
@@ -519,22 +530,27 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             if (pre) tgt *= pre_max / pre_kappa;   // b = M r / ||r|| has ||b|| <= max m
             inner_start<T>(W, tgt, nlim, o.stag_window > 0 ? o.stag_window : 40, c->stream);
             aux += kInnerStartLaunches;
+            CK(cudaMemcpyAsync(st.data(), W.st, sizeof(InnerState) * nbatch, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
             for (int iters = 0;;) {
-                CK(cudaGraphLaunch(gexec, c->stream));
+                bool any = false;
+                for (const auto &sv : st) any = any || !sv.done;
+                if (!any) break;
+                // the running instances of each group on as few lanes as hold them
+                inner_lanes<T>(W, st.data(), amap, c->stream);
+                CK(cudaGraphLaunch(chunk_graph(), c->stream));
                 iters += kInnerChunk;
                 launches += (int64_t)kInnerChunk * kInnerIterationLaunches + kInnerCheckLaunches;
                 CK(cudaMemcpyAsync(st.data(), W.st, sizeof(InnerState) * nbatch, cudaMemcpyDeviceToHost, c->stream));
                 CK(cudaStreamSynchronize(c->stream));
-                bool any = false;
-                for (const auto &sv : st) any = any || !sv.done;
-                if (!any || iters > nlim + kInnerChunk) break;
+                if (iters > nlim + kInnerChunk) break;
             }
             int applies = 0;
             for (const auto &sv : st) { applies = std::max(applies, 2 * sv.n + sv.checks); last_ierr = sv.ierr; }
             total_iters += applies;
             for (int b = 0; b < nbatch; b++)
                 if (norms[b] > o.crit)
-                    vec_axpy_to_d<T>(N, x + (int64_t)b * vstride, norms[b], W.slot(st[b].best_slot) + (int64_t)b * W.vstride, c->stream), aux++;
+                    inner_add_solution<T>(W, x + (int64_t)b * vstride, b, norms[b], st[b].best_slot, c->stream), aux++;
         }
         if (!rhs) { herm_rdo_dev(c, x, nbatch, vstride); aux++; }
         rounds = round;
@@ -547,8 +563,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                                   const DevCoef<double> &, const DevCoef<T> &, double2 *, std::vector<double> &, int, \
                                   int, bool, bool &, int &, int &, bool &, int &, int64_t &, int64_t &,               \
                                   const std::function<void(const double2 *, double2 *)> &,                            \
-                                  const std::function<void(const double2 *)> &, const DevPlan &, int64_t,             \
-                                  const double *);
+                                  const std::function<void(const double2 *)> &, const DevPlan &, int64_t);
 HEOM_MIXED_ROUNDS(DF)
 HEOM_MIXED_ROUNDS(double)
 #undef HEOM_MIXED_ROUNDS
@@ -621,22 +636,22 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             if (o.precision == HEOM_PREC_MIXED)
                 mixed_rounds<DF>(c, o, x, nbatch, vstride, rhs, k64, K.kdf, r64, norms, nlim, o.max_refine, true, stalled,
                                  total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
-                                 c->dfwd.view, N, c->rt_host.data());
+                                 c->dfwd.view, N);
             else if (o.precision == HEOM_PREC_FP64_REFINED)
                 mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim, o.max_refine, false, unused,
                                      total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
-                                 c->dfwd.view, N, c->rt_host.data());
+                                 c->dfwd.view, N);
             else if (o.precision == HEOM_PREC_MIXED_FP32)
                 mixed_rounds<float>(c, o, x, nbatch, vstride, rhs, k64, K.k32, r64, norms, nlim, o.max_refine, true, stalled,
                                     total_iters, last_ierr, converged, info.refinements, info.launches, aux, residual, batch_norms,
-                                 c->dfwd.view, N, c->rt_host.data());
+                                 c->dfwd.view, N);
             else fail(HEOM_E_ARG, "unknown precision");
             if (stalled && !converged) {
-                // the remaining rounds with FP64 inner solves on the same regularised operator
+                // up to max_refine rounds with FP64 inner solves on the same regularised operator
                 int more = 0;
                 mixed_rounds<double>(c, o, x, nbatch, vstride, rhs, k64, K.k64, r64, norms, nlim,
-                                     std::max(1, o.max_refine - info.refinements), false, unused, total_iters, last_ierr,
-                                     converged, more, info.launches, aux, residual, batch_norms, c->dfwd.view, N, c->rt_host.data());
+                                     std::max(1, o.max_refine), false, unused, total_iters, last_ierr,
+                                     converged, more, info.launches, aux, residual, batch_norms, c->dfwd.view, N);
                 info.refinements += more;
             }
         }
@@ -1122,7 +1137,23 @@ int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, h
             }
         }
         heom_solve_info inf;
-        solve_device(c, *o, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, CoefSet{K64, K32, KDF});
+        // automatic interleave of the mixed solves: the context's first two mixed solves of a
+        // batch of this size run with none and with the largest useful one; later ones keep
+        // the faster
+        heom_solve_opts oo = *o;
+        heom_ctx::InterleaveTune *tu = nullptr;
+        int slot = -1;
+        if (oo.precision == HEOM_PREC_MIXED && oo.interleave == 0) {
+            const int cand[2] = {1, inner_default_interleave(B->nbatch)};
+            if (cand[1] == 1) oo.interleave = 1;
+            else {
+                tu = &c->il_tune[B->nbatch];
+                if (tu->tried < 2) oo.interleave = cand[slot = tu->tried];
+                else oo.interleave = cand[tu->seconds[1] < tu->seconds[0] ? 1 : 0];
+            }
+        }
+        solve_device(c, oo, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, CoefSet{K64, K32, KDF});
+        if (slot >= 0) { tu->seconds[slot] = inf.seconds; tu->tried++; }
         if (info) *info = inf;
         if (!inf.converged) fail(HEOM_E_NOCONV, "batched TFQMR did not reach crit");
     });
@@ -1236,7 +1267,11 @@ void time_inner(heom_ctx *c, const BenchInputs &I, int nbatch, int reps, double 
 {
     const int64_t N = c->lunk + 1;
     InnerWork<T> W;
-    inner_alloc<T>(W, nbatch, N, c->stream);
+    // the interleave the batch solves of this size use (the tuned one, once tuned)
+    int G = 0;
+    auto it = c->il_tune.find(nbatch);
+    if (it != c->il_tune.end() && it->second.tried >= 2) G = it->second.seconds[1] < it->second.seconds[0] ? 0 : 1;
+    inner_alloc<T>(W, nbatch, N, c->stream, G);
     try {
         upload_rt_to<T>(c, W.rt, N);
         float mb = 0, ma = 0;

@@ -269,10 +269,10 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
             int total = 0, ierr = 0, rounds = 0, more = 0;
             int64_t aux = 0;
             mixed_rounds<DF>(c, mo, X, nb, vs, B, K, KD, R, norms, nlim, 8, true, stalled, total, ierr, conv, rounds,
-                             res.launches, aux, residual, batch_norms, P, N, cf->rt_host.data());
+                             res.launches, aux, residual, batch_norms, P, N);
             if (stalled && !conv)
                 mixed_rounds<double>(c, mo, X, nb, vs, B, K, K, R, norms, nlim, 8, false, unused, total, ierr, conv, more,
-                                     res.launches, aux, residual, batch_norms, P, N, cf->rt_host.data());
+                                     res.launches, aux, residual, batch_norms, P, N);
             res.iters = total;
             res.ierr = ierr;
             res.launches += aux;

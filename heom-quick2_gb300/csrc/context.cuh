@@ -1,5 +1,6 @@
 // The opaque heom_ctx: device plans, coefficient sets and work buffers of one model.
 #pragma once
+#include <map>
 #include <memory>
 
 #include "solver.cuh"
@@ -79,8 +80,7 @@ void run_tfqmr64(heom_ctx *c, TfqWork<double> &W, const ApplyFn<double> &apply, 
 // Mixed-precision refinement of A x = rhs (rhs == nullptr: the steady problem on the
 // regularised operator) for nbatch instances of N elements on the plan PV: rounds of FP64
 // residual (residual(x, r64)), per-instance norms (batch_norms), and a fused inner TFQMR in
-// the number type T on rhs / ||rhs||, until every norm is <= o.crit.  rt: the shadow vector
-// (2 N reals).
+// the number type T on rhs / ||rhs||, until every norm is <= o.crit.
 template <typename T>
 void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch, int64_t vstride, const double2 *rhs,
                   const DevCoef<double> &K64, const DevCoef<T> &KT, double2 *r64, std::vector<double> &norms,
@@ -88,7 +88,7 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
                   int &total_iters, int &last_ierr, bool &converged, int &rounds, int64_t &launches, int64_t &aux,
                   const std::function<void(const double2 *, double2 *)> &residual,
                   const std::function<void(const double2 *)> &batch_norms,
-                  const DevPlan &PV, int64_t N, const double *rt);
+                  const DevPlan &PV, int64_t N);
 // ||H||_inf of the context's Hamiltonian (the scale of the inner preconditioner)
 double hs_inf_norm(heom_ctx *c);
 // The reference's shadow-vector stream (tfqmr_double/drandn.f90, SEED = 1): n reals.
@@ -136,5 +136,12 @@ struct heom_ctx {
     // the tables are tier-major, so a hierarchy truncated at tier k is the prefix up to
     // tier_entry[k]
     std::vector<int64_t> tier_entry;
+    // automatic interleave of the mixed batch solves, per batch size: the device seconds of
+    // one solve without interleave ([0]) and with inner_default_interleave ([1])
+    struct InterleaveTune {
+        int tried = 0;
+        double seconds[2] = {0, 0};
+    };
+    std::map<int, InterleaveTune> il_tune;
     ~heom_ctx();
 };

@@ -24,6 +24,8 @@
 // Launches per iteration: 4 (no guarded no-ops).  The FP64 reference solver keeps the
 // unfused form of solver.cuh, whose iterates follow the reference driver step by step.
 #pragma once
+#include <vector>
+
 #include "device.cuh"
 
 namespace heom {
@@ -44,27 +46,72 @@ struct InnerCoef {
     typename Num<T>::S beta, alpha, alpha_prev, dd1, eta1, dd2, eta2;
 };
 
+// Vector layout: instances are interleaved entry by entry in groups of G (G = 1 for FP64
+// and FP32; for FP32x2 the smallest power of two >= nbatch, at most 32).  Element t of
+// instance b sits at (b / G) gstride + t G + b % G.  A warp then holds 32 / G entries of G
+// instances: lanes of one entry share the plan's records, map words and loop trip counts
+// (one control flow per entry, plan reads broadcast to G lanes), and the gathered values of
+// the G instances are adjacent in memory.
 template <typename T>
 struct InnerWork {
     using V = typename Num<T>::V;
-    int nbatch = 0, nblk = 0;   // nblk: blocks of 256 per instance, one entry per thread
+    int nbatch = 0, nblk = 0;   // nblk: blocks of 256 threads per group in the current configuration
+    int G = 1, ngroups = 0;     // instances per group, groups
+    // current launch configuration: GE lanes per entry (0: G == 1, one instance per group);
+    // when GE < G, slot j of group g serves position amap[g G + j] (-1: none), so that the
+    // running instances of a group share fewer lanes and blocks (inner_lanes)
+    int GE = 0;
+    int *amap = nullptr;
     int64_t N = 0;              // complex elements per instance (lunk + 1)
-    int64_t vstride = 0;        // complex elements between instances
+    int64_t vstride = 0;        // N rounded up to a multiple of 64
+    int64_t gstride = 0;        // complex elements between groups (vstride G)
     V *x = nullptr, *xs = nullptr, *b = nullptr, *w = nullptr, *y = nullptr, *d = nullptr, *v = nullptr,
       *u1 = nullptr, *u2 = nullptr, *rt = nullptr;
     V *xs2 = nullptr;           // second iterate slot (xs is slot 0)
     __host__ __device__ V *slot(int s) const { return s ? xs2 : xs; }
+    __host__ __device__ int64_t at(int inst, int64_t t) const
+    {
+        return (int64_t)(inst / G) * gstride + t * G + inst % G;
+    }
     InnerState *st = nullptr;
     InnerCoef<T> *cf = nullptr;
-    double *part = nullptr;     // per-block partials: 3 runs of nblk per instance
+    double *part = nullptr;     // per-block partials: 3 runs of nblk per instance (G ngroups instances)
     // truncated batches (DevCoef::tier_lim): the apply kernels skip blocks wholly beyond an
     // instance's last kept entry (their entries stay zero in every vector) and leave zero partials
     const int2 *tier_lim = nullptr;
     void *mem = nullptr;        // single allocation backing everything above
+    void *coef_mem = nullptr;   // interleaved H values and ADO diagonals (inner_layout_coef)
 };
 
-template <typename T> void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s);
+// G: instances per entry group (a power of two <= 32; 0 = inner_default_interleave; FP64
+// and FP32 workspaces always use 1)
+template <typename T> void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s, int G = 0);
+// the smallest power of two >= nbatch, at most 32
+inline int inner_default_interleave(int nbatch)
+{
+    int g = 1;
+    while (g < nbatch && g < 32) g *= 2;
+    return g;
+}
 template <typename T> void inner_free(InnerWork<T> &W);
+// The coefficient set in the workspace's layout: C.hval (P.nh values per instance) and
+// C.gdiag (P.nado per instance), both instance-major, copied into W's interleaved layout
+// (W.coef_mem) when G > 1; C itself when G == 1.
+template <typename T>
+DevCoef<T> inner_layout_coef(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, cudaStream_t s);
+// Right-hand side of instance `inst`: W.b = scale r (FP64, N elements), rows of ADO n times
+// pre[n] when pre is given (the trace slot is not scaled).
+template <typename T>
+void inner_rhs(InnerWork<T> &W, const DevPlan &P, const double2 *r, int inst, double scale, const float *pre, cudaStream_t s);
+// The shadow vector W.rt of the inner solves: sign-symmetric pseudo-random entries, a
+// different vector for every `round`.  The reference's stream (all positive) left the inner
+// solves of the Kanamori model at T = 0.1 without progress round after round: restarted on
+// the same normalised residual with the same shadow vector, TFQMR repeats the same iterates.
+template <typename T>
+void inner_shadow(InnerWork<T> &W, int round, cudaStream_t s);
+// x += a W.slot(slot) of instance `inst` (x: FP64, N elements).
+template <typename T>
+void inner_add_solution(InnerWork<T> &W, double2 *x, int inst, double a, int slot, cudaStream_t s);
 
 // Start a solve: W.b holds the right-hand sides and W.rt the shadow vector.  An instance
 // stops at the first check with ||b - A xs|| <= crit; with stag_window > 0 also at the
@@ -72,7 +119,14 @@ template <typename T> void inner_free(InnerWork<T> &W);
 // stag_window checks that fail to halve the best residual); or once nlim iterations ran.
 template <typename T>
 void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaStream_t s);
-// Enqueue `iters` iterations and one check (capturable in a CUDA graph).
+// Configure W for the next chunk from the instances' states (host copy): GE = the smallest
+// power of two >= the most running instances of any group, and their positions in the lane
+// map (copied with cudaMemcpyAsync from amap_host, which must stay unchanged until the
+// stream has passed the copy).
+template <typename T>
+void inner_lanes(InnerWork<T> &W, const InnerState *st, std::vector<int> &amap_host, cudaStream_t s);
+// Enqueue `iters` iterations and one check in W's current configuration (capturable in a
+// CUDA graph; W is captured by value).
 template <typename T>
 void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int iters, cudaStream_t s);
 

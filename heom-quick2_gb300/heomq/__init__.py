@@ -81,7 +81,7 @@ class CtxOpts(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32), ("inner_tol", C.c_double),
                 ("max_refine", C.c_int32), ("stag_window", C.c_int32), ("inner_precond", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("interleave", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -648,9 +648,9 @@ class Batch:
                 raise HeomError(rc, msg)
 
     def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True,
-                  stag_window=0, inner_precond=0):
+                  stag_window=0, inner_precond=0, interleave=0):
         o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine,
-                      stag_window=stag_window, inner_precond=inner_precond)
+                      stag_window=stag_window, inner_precond=inner_precond, interleave=interleave)
         info = SolveInfo()
         rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
         if check:

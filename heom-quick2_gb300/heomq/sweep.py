@@ -48,7 +48,9 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8, c
     did not reach crit (their `converged` is 0) instead of raising."""
     import torch
 
-    groups = group_instances(cfgs)
+    # within a family, instances in order of their tier: the fused kernels run instances in
+    # interleaved groups, and a group of one depth skips the blocks beyond its tier together
+    groups = [sorted(g, key=lambda i: cfgs[i]["ntier"]) for g in group_instances(cfgs)]
     currents = np.zeros(len(cfgs))
     infos = [None] * len(groups)
 

@@ -179,15 +179,23 @@ typedef struct {
                                  unless the inner arithmetic's floor stops it; 1e-2 for
                                  MIXED_FP32) */
     int32_t max_refine;       /* MIXED: outer refinement rounds; a round that fails to halve an
-                                 instance's FP64 residual hands the remaining rounds to FP64
-                                 inner solves on the same regularised operator */
+                                 instance's FP64 residual hands the solve to up to max_refine
+                                 rounds of FP64 inner solves on the same regularised operator
+                                 (a round of those that fails to halve one changes the inner
+                                 solves' shadow vector) */
     int32_t stag_window;      /* MIXED: an inner solve also stops after this many every-50-applies
                                  tests without halving its residual; <= 0 selects 40 */
     int32_t inner_precond;    /* MIXED, MIXED_FP32: left diagonal preconditioning of the FP32x2 /
                                  FP32 inner solves (the rows of ADO n scaled by
                                  1 / (|sum of its damping rates| + ||H||_inf)); 0 (default) or
                                  1 = on, -1 = off.  FP64 inner solves are not scaled. */
-    int32_t reserved;
+    int32_t interleave;       /* MIXED: instances interleaved per entry group in the FP32x2 inner
+                                 kernels (lanes of one entry share the plan's control flow and
+                                 reads); 1 = none, 2..32 a power of two, 0 (default) = automatic:
+                                 a batch times its first two mixed solves with none and with the
+                                 smallest power of two >= nbatch (at most 32), and keeps the
+                                 faster; single solves use none.  An interleaved group runs
+                                 until all its instances have finished. */
 } heom_solve_opts;
 
 typedef struct {
