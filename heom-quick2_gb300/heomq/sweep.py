@@ -40,12 +40,15 @@ def _lead_shift(cfg, nalf, nspin):
     return es
 
 
-def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8, check=True):
+def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8, check=True, interleave=1):
     """Steady states of many instances; returns (lead-1 currents, per-family solve infos).
 
     The states stay on the device; only the currents (through the allocation-free batch
     current reduction) come back to the host.  check=False returns the infos of families that
-    did not reach crit (their `converged` is 0) instead of raising."""
+    did not reach crit (their `converged` is 0) instead of raising.  interleave: instances
+    per entry group of the mixed solver's inner kernels (heom_solve_opts.interleave; every
+    family is solved once, on a context of its own, so the automatic choice 0 would always
+    take its first candidate)."""
     import torch
 
     # within a family, instances in order of their tier: the fused kernels run instances in
@@ -77,7 +80,7 @@ def solve_sweep(cfgs, crit=1e-9, precision=PREC_MIXED, device=0, max_refine=8, c
             x[:, : rep.lunk] = torch.from_numpy(rep.initial_guess()).to(x.device)
             torch.cuda.synchronize(device)
             infos[gi] = batch.solve_dev(x.data_ptr(), crit=crit, precision=precision, max_refine=max_refine,
-                                        check=check)
+                                        check=check, interleave=interleave)
             jt = batch.currents_static(x.data_ptr())
         for k, i in enumerate(idx):
             currents[i] = jt[k, 0].sum()
