@@ -307,7 +307,14 @@ def gradient_record():
     dI, ainfo = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF,
                                     crit=1e-12)
     t_adj = time.perf_counter() - t0
-    steady = {"adjoint_s": t_adj, "adjoint_applies": ainfo.iters, "dI": dict(zip(("V", "gamma", "U", "eps"), map(float, dI)))}
+    t0 = time.perf_counter()
+    dmx, minfo = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF,
+                                     crit=1e-12, precision=heomq.PREC_MIXED)
+    t_mx = time.perf_counter() - t0
+    steady = {"adjoint_s": t_adj, "adjoint_applies": ainfo.iters, "dI": dict(zip(("V", "gamma", "U", "eps"), map(float, dI))),
+              "mixed_adjoint": {"adjoint_s": t_mx, "applies": minfo.iters, "refinements": minfo.refinements,
+                                "converged": bool(minfo.converged),
+                                "max_rel_diff_vs_fp64": float(np.max(np.abs(dmx - dI)) / np.max(np.abs(dI)))}}
     rel = {}
     for k, key in enumerate(("V", "gamma", "U")):
         h = 1e-4 * max(1.0, abs(p0[key]))

@@ -409,6 +409,65 @@ void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, 
     info.seconds = ms * 1e-3;
 }
 
+void solve_custom_mixed(heom_ctx *c, const ApplyFn<double> &op64, const ApplyFn<DF> &opdf, const double2 *rhs, double2 *x,
+                        double crit_abs, int maxit0, heom_solve_info &info)
+{
+    const int64_t N = c->lunk + 1;
+    const int nlim = std::max(1, maxit0 / 2);
+    info = heom_solve_info{};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    TfqWork<DF> W;
+    tfq_alloc<DF>(W, 1, N, c->stream);
+    double2 *r = nullptr;
+    double resid = 0, prev = 0;
+    bool stalled = false;
+    try {
+        CK(cudaMalloc((void **)&r, sizeof(double2) * N));
+        upload_rt_to<DF>(c, W.rt, N);
+        for (int round = 0; round < 16; round++) {
+            op64(x, r, nullptr);
+            vec_axpby<double>(N, r, 1.0, rhs, -1.0, r, c->stream);   // r = rhs - op64(x)
+            resid = device_norm2(N, r, c->dscratch, c->stream);
+            if (resid <= crit_abs) break;
+            if (round > 0 && resid > 0.5 * prev) { stalled = true; break; }
+            prev = resid;
+            vec_from_d<DF>(N, r, W.b, 1.0 / resid, c->stream);
+            const double tgt = std::max(crit_abs / resid, 1e-10);
+            tfq_start<DF>(W, tgt * 1e-3, nlim, tgt, 0.0, 40, c->stream);
+            int it = 0;
+            tfq_run<DF>(c, W, opdf, nlim, it, info.launches);
+            vec_axpy_to_d<DF>(N, x, resid, W.x, c->stream);
+            TfqState st;
+            CK(cudaMemcpyAsync(&st, W.st, sizeof(TfqState), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            info.iters += st.axb;
+            info.refinements = round + 1;
+        }
+    } catch (...) { tfq_free(W); if (r) cudaFree(r); cudaEventDestroy(e0); cudaEventDestroy(e1); throw; }
+    tfq_free(W);
+    cudaFree(r);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    info.resid = resid;
+    info.converged = resid <= crit_abs;
+    info.seconds = ms * 1e-3;
+    if (stalled && !info.converged) {   // the rest with the restarted FP64 solve
+        heom_solve_info more{};
+        solve_custom64(c, op64, rhs, x, crit_abs, maxit0, more);
+        info.iters += more.iters;
+        info.refinements += more.refinements;
+        info.launches += more.launches;
+        info.resid = more.resid;
+        info.converged = more.converged;
+        info.seconds += more.seconds;
+    }
+}
+
 // ||H||_inf of the context's Hamiltonian (the scale of the inner preconditioner)
 double hs_inf_norm(heom_ctx *c)
 {

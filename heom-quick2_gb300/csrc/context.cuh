@@ -71,6 +71,12 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
 // at ||rhs - op(x)|| <= crit_abs.
 void solve_custom64(heom_ctx *c, const ApplyFn<double> &op, const double2 *rhs, double2 *x, double crit_abs, int maxit0,
                     heom_solve_info &info);
+// Mixed-precision solve of op(x) = rhs for one instance (x: initial guess in, solution out):
+// rounds of FP64 residual r = rhs - op64(x), FP32x2 TFQMR on opdf(d) = r / ||r|| to
+// max(crit_abs / ||r||, 1e-10) or its floor, x += ||r|| d, until ||r|| <= crit_abs; a round
+// that fails to halve ||r|| hands the rest to solve_custom64.
+void solve_custom_mixed(heom_ctx *c, const ApplyFn<double> &op64, const ApplyFn<DF> &opdf, const double2 *rhs, double2 *x,
+                        double crit_abs, int maxit0, heom_solve_info &info);
 // Values of a full nrho x nrho matrix on the context's H structure (FP64).
 void hvalues64(heom_ctx *c, const cd *hs, std::vector<double2> &h64);
 double device_rdot(heom_ctx *c, int64_t n, const double2 *a, const double2 *b);

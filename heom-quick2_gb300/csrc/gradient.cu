@@ -23,30 +23,35 @@ namespace {
 constexpr int NT = 256;
 
 // z = P_H z + s P_A y on the RDO block; z[lunk] = (s / ndiag) sum_diag Re y + i s Im y[lunk].
-// P_H / P_A: Hermitian / anti-Hermitian part of the RDO block.  One block per instance.
-__global__ void k_reg_adjoint(const double2 *y, double2 *z, int64_t vstride, int64_t lunk, int nz0, int ndiag,
-                              const int32_t *pair, double s, const int *active)
+// P_H / P_A: Hermitian / anti-Hermitian part of the RDO block.  One block per instance; the
+// few RDO entries are combined in FP64 whatever the vectors' number type.
+template <typename T>
+__global__ void k_reg_adjoint(const typename Num<T>::V *y, typename Num<T>::V *z, int64_t vstride, int64_t lunk, int nz0,
+                              int ndiag, const int32_t *pair, double s, const int *active)
 {
+    using N = Num<T>;
     const int b = blockIdx.x;
     if (active && !active[b]) return;
     y += (int64_t)b * vstride;
     z += (int64_t)b * vstride;
+    auto ld = [](const typename N::V &v) { const typename N::A a = N::load(v); return make_double2(N::re(a), N::im(a)); };
+    auto st = [](typename N::V &v, double re, double im) { v = N::store(N::from_d(re, im)); };
     __shared__ double red[NT];
     double dsum = 0;
     for (int q = threadIdx.x; q < nz0; q += NT) {
         const int p = pair[q];
         if (p < q) continue;
-        const double2 zq = z[q], zp = z[p], yq = y[q], yp = y[p];
+        const double2 zq = ld(z[q]), zp = ld(z[p]), yq = ld(y[q]), yp = ld(y[p]);
         if (p == q) {
-            z[q] = make_double2(zq.x, s * yq.y);   // Hermitian part keeps Re, anti-Hermitian part is i Im
+            st(z[q], zq.x, s * yq.y);   // Hermitian part keeps Re, anti-Hermitian part is i Im
             dsum += yq.x;
             continue;
         }
         // Hermitian part of (zq, zp) plus s times the anti-Hermitian part of (yq, yp)
         const double hx = 0.5 * (zq.x + zp.x), hy = 0.5 * (zq.y - zp.y);
         const double ax = 0.5 * (yq.x - yp.x), ay = 0.5 * (yq.y + yp.y);
-        z[q] = make_double2(hx + s * ax, hy + s * ay);
-        z[p] = make_double2(hx - s * ax, -hy + s * ay);
+        st(z[q], hx + s * ax, hy + s * ay);
+        st(z[p], hx - s * ax, -hy + s * ay);
     }
     red[threadIdx.x] = dsum;
     __syncthreads();
@@ -54,7 +59,7 @@ __global__ void k_reg_adjoint(const double2 *y, double2 *z, int64_t vstride, int
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) z[lunk] = make_double2(s * red[0] / ndiag, s * y[lunk].y);
+    if (threadIdx.x == 0) st(z[lunk], s * red[0] / ndiag, s * ld(y[lunk]).y);
 }
 
 __global__ void k_fill(double2 *x, int64_t n, double2 v)
@@ -65,8 +70,9 @@ __global__ void k_fill(double2 *x, int64_t n, double2 v)
 int grid_for(int64_t n) { int64_t g = (n + NT - 1) / NT; return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g)); }
 }  // namespace
 
-// y = A~^H x for one instance (device, FP64).
-ApplyFn<double> regularised_adjoint(heom_ctx *c, const DevCoef<double> &Kadj)
+// y = A~^H x for one instance (device, in the number type T).
+template <typename T>
+ApplyFn<T> regularised_adjoint(heom_ctx *c, const DevCoef<T> &Kadj)
 {
     const DevPlan P = c->dadj.view;
     cudaStream_t s = c->stream;
@@ -74,10 +80,25 @@ ApplyFn<double> regularised_adjoint(heom_ctx *c, const DevCoef<double> &Kadj)
     const int nz0 = c->nz0, ndiag = c->ndiag;
     const int32_t *pair = c->d_rdo_pair;
     const double sc = c->reg_scale;
-    return [=](const double2 *x, double2 *y, const int *act) {
-        launch_apply<double, true>(P, Kadj, x, y, 1, N, act, s);
-        k_reg_adjoint<<<1, NT, 0, s>>>(x, y, N, lunk, nz0, ndiag, pair, sc, act);
+    return [=](const typename Num<T>::V *x, typename Num<T>::V *y, const int *act) {
+        launch_apply<T, true>(P, Kadj, x, y, 1, N, act, s);
+        k_reg_adjoint<T><<<1, NT, 0, s>>>(x, y, N, lunk, nz0, ndiag, pair, sc, act);
     };
+}
+
+// Mixed-precision solve of A~^H x = rhs for one instance (solve_custom_mixed) with the
+// adjoint plan's ADO diagonals precomputed, so that the FP32x2 applies do no FP64 arithmetic.
+void solve_adjoint_mixed(heom_ctx *c, const DevCoef<double> &K64, const DevCoef<DF> &KDF, const double2 *rhs, double2 *x,
+                         double crit_abs, int maxit0, heom_solve_info &info)
+{
+    float4 *gd = nullptr;
+    CK(cudaMalloc((void **)&gd, sizeof(float4) * gdiag_elems<DF>(c->dadj.view, 1)));
+    try {
+        DevCoef<DF> KD = KDF;
+        fill_gdiag<DF>(c->dadj.view, KD, gd, 1, c->stream);
+        solve_custom_mixed(c, regularised_adjoint<double>(c, K64), regularised_adjoint<DF>(c, KD), rhs, x, crit_abs, maxit0, info);
+    } catch (...) { cudaFree(gd); throw; }
+    cudaFree(gd);
 }
 
 // Re<a, b> over n complex entries (device vectors, result on the host).
@@ -117,7 +138,12 @@ extern "C" int heom_steady_gradient(heom_ctx *c, const heom_grad_opts *o, const 
             cn = std::sqrt(cn);
             const double crit = (o->crit > 0 ? o->crit : 1e-10) * cn;
             heom_solve_info inf{};
-            solve_custom64(c, regularised_adjoint(c, ctx_coefs(c, true).k64), cvec, lam, crit, o->maxit0 > 0 ? o->maxit0 : 20000, inf);
+            const CoefSet KA = ctx_coefs(c, true);
+            if (o->precision == HEOM_PREC_MIXED)
+                solve_adjoint_mixed(c, KA.k64, KA.kdf, cvec, lam, crit, o->maxit0 > 0 ? o->maxit0 : 20000, inf);
+            else if (o->precision == HEOM_PREC_FP64)
+                solve_custom64(c, regularised_adjoint<double>(c, KA.k64), cvec, lam, crit, o->maxit0 > 0 ? o->maxit0 : 20000, inf);
+            else fail(HEOM_E_ARG, "adjoint solve precision must be HEOM_PREC_FP64 or HEOM_PREC_MIXED");
             if (info) *info = inf;
             if (!inf.converged) fail(HEOM_E_NOCONV, "adjoint solve did not converge");
             // (dA/dtheta) x for the parameters asked for

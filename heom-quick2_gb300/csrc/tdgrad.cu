@@ -63,6 +63,20 @@ __global__ void k_lambda(int64_t n, const double2 *c, double dt, const double2 *
 
 __global__ void k_set_step(PropClock *clk, int64_t n) { clk->n = n; }
 
+// One term of a Chebyshev step with its Q kept: Q_k = (first ? 0 : Q_{k-2}) + s lq and
+// out = (first ? c0 Q_0 : out) + c Q_k (the arithmetic of the propagation step)
+__global__ void k_qcheb(int64_t n, const double2 *q0, const double2 *qm2, const double2 *lq, double2 *q, double2 *out,
+                        double s, double c, int first, double c0)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 l = lq[i];
+        const double2 v = first ? make_double2(s * l.x, s * l.y) : make_double2(qm2[i].x + s * l.x, qm2[i].y + s * l.y);
+        q[i] = v;
+        const double2 r = first ? make_double2(c0 * q0[i].x, c0 * q0[i].y) : out[i];
+        out[i] = make_double2(r.x + c * v.x, r.y + c * v.y);
+    }
+}
+
 __global__ void k_sum(int64_t n, const double *a, double *out)
 {
     __shared__ double red[NT];
@@ -159,11 +173,32 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
             KF.gdiag = B.gd; KA.gdiag = B.gda;   // refreshed by stage_prepare
             cudaStream_t s = c->stream;
             const int gL = grid_for(L);
+            // when a segment's Q_k (K ck vectors) fit in half the free device memory, the
+            // recomputation of the segment keeps them, and the backward walk reuses them
+            // instead of rebuilding them (K - 1 fewer applies per step)
+            size_t mem_free = 0, mem_total = 0;
+            CK(cudaMemGetInfo(&mem_free, &mem_total));
+            char *qseg = nullptr;
+            if ((double)vb * K * ck <= 0.5 * (double)mem_free) qseg = (char *)dalloc(vb * (size_t)K * ck);
+            auto QS = [&](int i, int k) { return (double2 *)(qseg + vb * ((size_t)i * K + k)); };
             for (int sg = ncp - 1; sg >= 0; sg--) {
                 const int n0 = sg * ck, n1 = std::min(nstep, n0 + ck);
                 // recompute rho_{n0} .. rho_{n1-1}
                 CK(cudaMemcpyAsync(st(0), cp(sg), vb, cudaMemcpyDeviceToDevice, s));
-                for (int n = n0; n < n1 - 1; n++) {
+                for (int n = n0; n < n1 - 1 || (qseg && n < n1); n++) {
+                    if (qseg) {
+                        // the step from its Q_k, kept; rho_{n+1} = J0 Q_0 + 2 sum_k J_k Q_k
+                        k_set_step<<<1, 1, 0, s>>>(B.clk, n);
+                        stage_prepare(c, B, 0.0, false, s);
+                        CK(cudaMemcpyAsync(QS(n - n0, 0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                        for (int k = 1; k < K; k++) {
+                            launch_apply<double, false>(P, KF, QS(n - n0, k - 1), lh, 1, N, nullptr, s);
+                            k_qcheb<<<gL, NT, 0, s>>>(L, QS(n - n0, 0), k >= 2 ? QS(n - n0, k - 2) : nullptr, lh, QS(n - n0, k), x,
+                                                      k == 1 ? 1.0 / delta : 2.0 / delta, 2.0 * bes[k], k == 1, bes[0]);
+                        }
+                        if (n < n1 - 1) CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
+                        continue;
+                    }
                     CK(cudaMemcpyAsync(x, st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
                     k_set_step<<<1, 1, 0, s>>>(B.clk, n);
                     enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, false);
@@ -172,11 +207,14 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
                 for (int n = n1 - 1; n >= n0; n--) {
                     k_set_step<<<1, 1, 0, s>>>(B.clk, n);
                     stage_prepare(c, B, 0.0, true, s);
-                    // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1}
-                    CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
-                    for (int k = 1; k < K; k++) {
-                        launch_apply<double, false>(P, KF, Q(k - 1), lh, 1, N, nullptr, s);
-                        k_qstep<<<gL, NT, 0, s>>>(L, k >= 2 ? Q(k - 2) : nullptr, lh, Q(k), k == 1 ? 1.0 / delta : 2.0 / delta, k == 1);
+                    // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1} (kept, or rebuilt)
+                    auto Qn = [&](int k) { return qseg ? QS(n - n0, k) : Q(k); };
+                    if (!qseg) {
+                        CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                        for (int k = 1; k < K; k++) {
+                            launch_apply<double, false>(P, KF, Q(k - 1), lh, 1, N, nullptr, s);
+                            k_qstep<<<gL, NT, 0, s>>>(L, k >= 2 ? Q(k - 2) : nullptr, lh, Q(k), k == 1 ? 1.0 / delta : 2.0 / delta, k == 1);
+                        }
                     }
                     // mu recurrence, lambda = dJ/d rho_{n+1} (zero at n = nstep - 1)
                     const double2 *m2 = nullptr, *m1 = nullptr;
@@ -188,7 +226,7 @@ extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t c
                         const double s_next = (j + 1 == 1) ? 1.0 / delta : 2.0 / delta;
                         if (m1) launch_apply<double, true>(PA, KA, m1, lh, 1, N, nullptr, s);
                         k_mu<<<gL, NT, 0, s>>>(L, P, B.es, lam, a, m1 ? lh : nullptr, s_next, m2, mj,
-                                               j >= 1 ? Q(j - 1) : nullptr, j == 1 ? 1.0 / delta : 2.0 / delta, acc);
+                                               j >= 1 ? Qn(j - 1) : nullptr, j == 1 ? 1.0 / delta : 2.0 / delta, acc);
                         m2 = m1;
                         m1 = mj;
                     }

@@ -96,7 +96,7 @@ class CfTables(C.Structure):
 
 class GradOpts(C.Structure):
     _fields_ = [("deshift", C.c_void_p), ("gamma", C.c_double), ("dhs_du", C.c_void_p), ("dhs_deps", C.c_void_p),
-                ("crit", C.c_double), ("maxit0", C.c_int32)]
+                ("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32)]
 
 
 # symbol -> (restype, argtypes); also the list of entry points of include/heom_gb300.h
@@ -476,9 +476,10 @@ class Context:
         _check(lib().heom_propagate(self.h, method, t0, dt, nstep, rho.ctypes.data, None if jt is None else jt.ctypes.data))
         return (rho, jt) if currents else rho
 
-    def steady_gradient(self, rho, deshift=None, gamma=None, dhs_du=None, dhs_deps=None, which=0xF, crit=1e-10, maxit0=20000):
+    def steady_gradient(self, rho, deshift=None, gamma=None, dhs_du=None, dhs_deps=None, which=0xF, crit=1e-10, maxit0=20000,
+                        precision=PREC_FP64):
         rho = _c128(rho, self.lunk)
-        o = GradOpts(crit=crit, maxit0=maxit0, gamma=gamma or 0.0)
+        o = GradOpts(crit=crit, maxit0=maxit0, gamma=gamma or 0.0, precision=precision)
         keep = []
         if deshift is not None:
             d = np.ascontiguousarray(deshift, dtype=np.float64); keep.append(d); o.deshift = d.ctypes.data

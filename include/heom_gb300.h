@@ -247,6 +247,9 @@ typedef struct {
     const double _Complex *dhs_deps;  /* d hs / d eps (nrho^2) */
     double crit;                      /* adjoint solve tolerance */
     int32_t maxit0;
+    int32_t precision;                /* adjoint solve: HEOM_PREC_FP64 (0, restarted FP64 TFQMR) or
+                                         HEOM_PREC_MIXED (FP32x2 TFQMR rounds on the regularised
+                                         adjoint, FP64 residual refinement to the same tolerance) */
 } heom_grad_opts;
 int heom_steady_gradient(heom_ctx *ctx, const heom_grad_opts *o, const double _Complex *rho,
                          int32_t which, double *dI, heom_solve_info *info);

@@ -58,6 +58,25 @@ def test_adjoint_gradient_matches_central_differences(name):
         assert abs(dI[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * abs(ip)), (key, dI[k], fd)
 
 
+@pytest.mark.parametrize("name", sorted(BASE))
+def test_mixed_adjoint_solve_gives_the_fp64_gradients(name):
+    """The adjoint solve in mixed precision (FP32x2 TFQMR rounds on the regularised adjoint,
+    FP64 refinement to the same tolerance) against the FP64 adjoint solve: dI/d{V, Gamma, U,
+    eps} within 1e-8 relative (of the largest)."""
+    p0 = PARAMS[BASE[name]["kind"]]
+    m = heomq.Model(make_cfg(name))
+    du, de = m.get("dhs_du", m.nrho ** 2, np.complex128), m.get("dhs_deps", m.nrho ** 2, np.complex128)
+    ctx = heomq.Context(m, dhs=(du, de))
+    rho, info = ctx.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    assert info.converged
+    deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / HB
+    kw = dict(deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF, crit=1e-12)
+    d64, i64 = ctx.steady_gradient(rho, precision=heomq.PREC_FP64, **kw)
+    dmx, imx = ctx.steady_gradient(rho, precision=heomq.PREC_MIXED, **kw)
+    assert imx.converged and imx.resid <= i64.resid * 10 + 1e-300 or imx.converged
+    assert np.max(np.abs(dmx - d64)) <= 1e-8 * np.max(np.abs(d64)), (dmx, d64)
+
+
 def test_adjoint_identity_of_the_regularised_solve():
     """<c, x_theta> from a forward tangent solve equals the adjoint value."""
     cfg = make_cfg("siam_L2")
@@ -152,6 +171,10 @@ def test_full_size_gradients_match_central_differences():
     assert info.converged
     deshift = np.array([[0.5, 0.5], [-0.5, -0.5]]).T.reshape(-1) / HB
     dI, _ = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF, crit=1e-12)
+    dmx, imx = ctx.steady_gradient(rho, deshift=deshift, gamma=p0["gamma"], dhs_du=du, dhs_deps=de, which=0xF, crit=1e-12,
+                                   precision=heomq.PREC_MIXED)
+    assert imx.converged
+    assert np.max(np.abs(dmx - dI)) <= 1e-8 * np.max(np.abs(dI)), (dmx, dI)
     for k, key in enumerate(("V", "gamma", "U")):
         h = 1e-4 * max(1.0, abs(p0[key]))
         fd = (current(cfg(**{key: p0[key] + h})) - current(cfg(**{key: p0[key] - h}))) / (2 * h)
