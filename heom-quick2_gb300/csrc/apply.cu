@@ -74,25 +74,6 @@ void fill_pre(const DevPlan &P, const double2 *g0, double hnorm, float *pre, cud
     k_fill_pre<<<std::max(1, std::min(1024, (P.nado + 255) / 256)), 256, 0, s>>>(P, g0, hnorm, pre);
 }
 
-template <typename T>
-__global__ void k_scale_rows(DevPlan P, const float *__restrict__ pre, typename Num<T>::V *v, int64_t vstride)
-{
-    using N = Num<T>;
-    v += (int64_t)blockIdx.y * vstride;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < P.lunk; t += (int64_t)gridDim.x * blockDim.x)
-        v[t] = N::store(N::scale(N::load(v[t]), N::sc((double)pre[__ldg(P.ent_ado + t)])));
-}
-
-template <typename T>
-void scale_rows(const DevPlan &P, const float *pre, typename Num<T>::V *v, int nbatch, int64_t vstride, cudaStream_t s)
-{
-    dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>(2048, (P.lunk + 255) / 256)), (unsigned)nbatch);
-    k_scale_rows<T><<<grid, 256, 0, s>>>(P, pre, v, vstride);
-}
-
-template void scale_rows<double>(const DevPlan &, const float *, double2 *, int, int64_t, cudaStream_t);
-template void scale_rows<float>(const DevPlan &, const float *, float2 *, int, int64_t, cudaStream_t);
-template void scale_rows<DF>(const DevPlan &, const float *, float4 *, int, int64_t, cudaStream_t);
 template void fill_gdiag<double>(const DevPlan &, DevCoef<double> &, double2 *, int, cudaStream_t);
 template void fill_gdiag<float>(const DevPlan &, DevCoef<float> &, float2 *, int, cudaStream_t);
 template void fill_gdiag<DF>(const DevPlan &, DevCoef<DF> &, float4 *, int, cudaStream_t);

@@ -77,9 +77,6 @@ inline int64_t gdiag_elems(const DevPlan &P, int nbatch) { return std::max<int64
 
 // pre[n] = 1 / (|g0[n]| + hnorm): the inverse size of ADO n's diagonal block
 void fill_pre(const DevPlan &P, const double2 *g0, double hnorm, float *pre, cudaStream_t s);
-// v[t] *= pre[ent_ado[t]] for the stored entries t < lunk of nbatch vectors of stride vstride
-template <typename T>
-void scale_rows(const DevPlan &P, const float *pre, typename Num<T>::V *v, int nbatch, int64_t vstride, cudaStream_t s);
 
 // y = A x (ADJ = false) or y = A^H x (ADJ = true) for nbatch instances (gridDim.y);
 // vstride = complex elements between instance vectors; active[b] == 0 skips instance b.
