@@ -198,6 +198,16 @@ __device__ __forceinline__ bool block_work(const InnerWork<T> &W, const Lane &L,
     return first < (int64_t)__ldg(&W.tier_lim[L.b].y) || last >= W.N - 1;
 }
 
+// Programmatic dependent launch: `k_in_b` and `k_in_a` are launched while the preceding
+// finaliser still runs (it calls allow_dependents first).  Their applies read only vectors
+// that the fused kernel before the finaliser wrote; they wait for the finaliser
+// (wait_prior_grid, griddepcontrol.wait: the whole preceding grid has finished and its
+// writes are visible) before they read the instances' states and coefficients it writes, or
+// write partial sums it may still be reading.  Without the launch attribute the wait returns
+// at once.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Entry of the fused kernels with K partials: false (after writing the K partials of this
 // block as zero for the instances its slots serve) when no lane of the block has work; the
 // decision is uniform over the block.  `work`: this lane's block_work.
@@ -209,6 +219,7 @@ __device__ __forceinline__ bool block_enter(const InnerWork<T> &W, bool work)
     if constexpr (GE == 0) any = work;   // one instance per block
     else any = __syncthreads_or(work) != 0;
     if (any) return true;
+    wait_prior_grid();
     if (threadIdx.x < K * NL) {
         const int p = slot_pos<T, GE, CMP>(W, (int)(threadIdx.x % NL)), k = (int)(threadIdx.x / NL);
         const int b = (int)blockIdx.y * W.G + p;
@@ -269,12 +280,15 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
     using A = typename N::A;
     constexpr int NL = lanes_of<GE>();
     const Lane L = lane_of<T, GE, CMP>(W);
+    // an instance finished before the preceding finaliser stays finished within the round
     const bool work = block_work<T, GE, CMP>(W, L, L.on && !W.st[L.b].done);
     if (!block_enter<T, 1, GE, CMP>(W, work)) return;
     WarpAcc<T> sg;
-    if (work && L.t < W.N) {
+    A aw = N::zero();
+    if (work && L.t < W.N) aw = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.w, L);
+    wait_prior_grid();
+    if (work && L.t < W.N && !W.st[L.b].done) {
         const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-        const A aw = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.w, L);
         const InnerCoef<T> &k = W.cf[L.b];
         const A u2 = N::load(W.u2[e]), vo = N::load(W.v[e]), yo = N::load(W.y[e]);
         const A u1 = N::add(aw, N::scale(u2, k.beta));
@@ -296,6 +310,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWo
 template <typename T>
 __global__ void __launch_bounds__(NTF) k_in_b_fin(InnerWork<T> W)
 {
+    allow_dependents();
     const int b = blockIdx.x;
     if (W.st[b].done) return;
     double tot[1];
@@ -322,9 +337,11 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
     const bool work = block_work<T, GE, CMP>(W, L, L.on && !W.st[L.b].done);
     if (!block_enter<T, 3, GE, CMP>(W, work)) return;
     WarpAcc<T> a1, a2, a3;
-    if (work && L.t < W.N) {
+    A av = N::zero();
+    if (work && L.t < W.N) av = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.v, L);
+    wait_prior_grid();
+    if (work && L.t < W.N && !W.st[L.b].done) {
         const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-        const A av = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.v, L);
         const typename N::S al = W.cf[L.b].alpha;
         const A u1 = N::load(W.u1[e]);
         const A u2 = N::sub(u1, N::scale(av, al));
@@ -344,6 +361,7 @@ __global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWo
 template <typename T>
 __global__ void __launch_bounds__(NTF) k_in_a_fin(InnerWork<T> W)
 {
+    allow_dependents();
     const int b = blockIdx.x;
     if (W.st[b].done) return;
     double tot[3];
@@ -485,14 +503,28 @@ void chunk_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int iters,
 {
     dim3 g((unsigned)W.nblk, (unsigned)W.ngroups);
     const unsigned nb = (unsigned)W.nbatch;
+    // the fused kernels as programmatic dependents of the finaliser before them
+    auto dependent = [&](auto kernel) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = g;
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, kernel, Q, C, W) != cudaSuccess) fail(HEOM_E_CUDA, "launch of a fused inner kernel failed");
+    };
     for (int i = 0; i < iters; i++) {
-        if (C.cf_half) k_in_b<T, false, true, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else if (C.reg) k_in_b<T, true, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else k_in_b<T, false, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) dependent(k_in_b<T, false, true, GE, CMP>);
+        else if (C.reg) dependent(k_in_b<T, true, false, GE, CMP>);
+        else dependent(k_in_b<T, false, false, GE, CMP>);
         k_in_b_fin<T><<<nb, NTF, 0, s>>>(W);
-        if (C.cf_half) k_in_a<T, false, true, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else if (C.reg) k_in_a<T, true, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else k_in_a<T, false, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
+        if (C.cf_half) dependent(k_in_a<T, false, true, GE, CMP>);
+        else if (C.reg) dependent(k_in_a<T, true, false, GE, CMP>);
+        else dependent(k_in_a<T, false, false, GE, CMP>);
         k_in_a_fin<T><<<nb, NTF, 0, s>>>(W);
     }
     k_in_x<T, GE, CMP><<<g, NT, 0, s>>>(W);
