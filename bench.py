@@ -333,10 +333,10 @@ def gradient_record():
     J, dJ = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32)
     t_grad = time.perf_counter() - t0
 
-    def integral(scale):
+    def integral(scale, method=heomq.PROP_CHEBYSHEV):
         c = heomq.Context(m, adjoint=False, amps=scale * amps, tchar=tchar)
         t = time.perf_counter()
-        _, jt = c.propagate(rho_eq, 0.0, 0.05, 1000, method=heomq.PROP_CHEBYSHEV, currents=True)
+        _, jt = c.propagate(rho_eq, 0.0, 0.05, 1000, method=method, currents=True)
         dt = time.perf_counter() - t
         c.close()
         return 0.05 * jt[:, 0::m.nalf].sum(), dt
@@ -344,9 +344,12 @@ def gradient_record():
     jp, t_fwd = integral(1 + 1e-5)
     jm, _ = integral(1 - 1e-5)
     fd = (jp - jm) / 2e-5
+    j1, _ = integral(1.0)
+    jmx, t_mx = integral(1.0, heomq.PROP_CHEBYSHEV_MIXED)
     ctx.close()
     td = {"steps": 1000, "dt": 0.05, "checkpoint_every": 32, "forward_s": t_fwd, "gradient_s": t_grad,
-          "dJ_dA": dJ, "central_difference": fd, "rel_err": abs(dJ - fd) / abs(fd)}
+          "dJ_dA": dJ, "central_difference": fd, "rel_err": abs(dJ - fd) / abs(fd),
+          "forward_mixed_s": t_mx, "integral_rel_diff_mixed_vs_fp64": abs(jmx / j1 - 1)}
     return {"model": "serial double dot nd=16, tier 4, M=3", "steady": steady, "chebyshev": td}
 
 

@@ -53,6 +53,56 @@ __global__ void k_current(const double2 *x, const CurrentTerm *terms, int nterms
     if (threadIdx.x < nslot) jt[(int64_t)clk->n * nslot + threadIdx.x] = -2.0 * part[0][threadIdx.x] * kJconst;
 }
 
+// The current of an FP32x2 state (k_current on the FP64 value of every summed entry)
+__global__ void k_current_df(const float4 *x, const CurrentTerm *terms, int nterms, int nslot, const PropClock *clk,
+                             double *jt)
+{
+    __shared__ double part[NT][4];
+    double acc[4] = {0, 0, 0, 0};
+    for (int k = threadIdx.x; k < nterms; k += NT) {
+        const CurrentTerm tm = terms[k];
+        const double v = (double)tm.sign * Num<DF>::im(Num<DF>::load(x[tm.entry]));
+#pragma unroll
+        for (int s = 0; s < 4; s++) acc[s] += (tm.slot == s) ? v : 0.0;
+    }
+    for (int s = 0; s < 4; s++) part[threadIdx.x][s] = acc[s];
+    __syncthreads();
+    for (int w = NT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int s = 0; s < 4; s++) part[threadIdx.x][s] += part[threadIdx.x + w][s];
+        __syncthreads();
+    }
+    if (threadIdx.x < nslot) jt[(int64_t)clk->n * nslot + threadIdx.x] = -2.0 * part[0][threadIdx.x] * kJconst;
+}
+
+// Chebyshev term in FP32x2: pn = pm2 + s lp; rho += c pn (first term: pn = s lp, rho = c0 pm2 + c pn)
+__global__ void k_cheb_df(int64_t n, const float4 *pm2, const float4 *lp, float4 *pn, float4 *rho, f2r s, f2r c, int first,
+                          f2r c0)
+{
+    using N = Num<DF>;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const N::A l = N::load(lp[i]), p2 = N::load(pm2[i]);
+        const N::A v = first ? N::scale(l, s) : N::add(p2, N::scale(l, s));
+        pn[i] = N::store(v);
+        const N::A r = first ? N::scale(p2, c0) : N::load(rho[i]);
+        rho[i] = N::store(N::add(r, N::scale(N::norm(v), c)));
+    }
+}
+
+__global__ void k_to_df(int64_t n, const double2 *a, float4 *o)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        o[i] = Num<DF>::store(Num<DF>::from_d(a[i].x, a[i].y));
+}
+
+__global__ void k_from_df(int64_t n, const float4 *a, double2 *o)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const Num<DF>::A v = Num<DF>::load(a[i]);
+        o[i] = make_double2(Num<DF>::re(v), Num<DF>::im(v));
+    }
+}
+
 // RK4 stage update: rt = r0 + a k; acc = (first ? r0 : acc) + b k
 __global__ void k_rk4(int64_t n, const double2 *r0, const double2 *k, double2 *rt, double2 *acc, double a, double b,
                       int first, int write_rt)
@@ -204,6 +254,35 @@ void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &Kin, PropBuffe
     k_advance<<<1, 1, 0, s>>>(B.clk);
 }
 
+// One Chebyshev step in FP32x2 (HEOM_PROP_CHEBYSHEV_MIXED): the state rho, the recurrence
+// vectors v[0..3] and the applies in FP32x2; gdf receives the step's ADO diagonals.
+void enqueue_step_df(heom_ctx *c, const DevCoef<DF> &Kin, PropBuffers &B, float4 *rho, float4 *const v[4], float4 *gdf,
+                     double delta, const std::vector<double> &bes, bool record_current)
+{
+    const DevPlan &P = c->dfwd.view;
+    DevCoef<DF> K = Kin;
+    K.trace_on = 0;
+    K.eshift = B.es;
+    const int64_t N = B.N, L = c->lunk;
+    const int ns = c->nalf * c->nspin;
+    cudaStream_t s = c->stream;
+    if (record_current) k_current_df<<<1, NT, 0, s>>>(rho, c->d_cur_terms, c->n_cur_terms, ns, B.clk, B.jt);
+    stage_prepare(c, B, 0.0, false, s);   // the step's lead shifts in B.es
+    fill_gdiag<DF>(P, K, gdf, 1, s);      // and its ADO diagonals in FP32x2 (K.gdiag = gdf)
+    float4 *pm2 = v[0], *pm1 = v[1], *pn = v[2], *lp = v[3];
+    CK(cudaMemcpyAsync(pm2, rho, sizeof(float4) * L, cudaMemcpyDeviceToDevice, s));
+    launch_apply<DF, false>(P, K, pm2, lp, 1, N, nullptr, s);
+    k_cheb_df<<<grid_for(L), NT, 0, s>>>(L, pm2, lp, pm1, rho, f2r_from_d(1.0 / delta), f2r_from_d(2.0 * bes[1]), 1,
+                                         f2r_from_d(bes[0]));
+    for (size_t n = 2; n < bes.size(); n++) {
+        launch_apply<DF, false>(P, K, pm1, lp, 1, N, nullptr, s);
+        k_cheb_df<<<grid_for(L), NT, 0, s>>>(L, pm2, lp, pn, rho, f2r_from_d(2.0 / delta), f2r_from_d(2.0 * bes[n]), 0,
+                                             f2r_from_d(0.0));
+        float4 *t = pm2; pm2 = pm1; pm1 = pn; pn = t;
+    }
+    k_advance<<<1, 1, 0, s>>>(B.clk);
+}
+
 }  // namespace heom
 
 using namespace heom;
@@ -216,7 +295,8 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
     return guarded([&] {
         require_ctx(c);
         if (!rho || nstep < 0 || !(dt > 0)) fail(HEOM_E_ARG, "bad propagation arguments");
-        if (method != HEOM_PROP_RK4 && method != HEOM_PROP_CHEBYSHEV) fail(HEOM_E_ARG, "unknown propagation method");
+        if (method != HEOM_PROP_RK4 && method != HEOM_PROP_CHEBYSHEV && method != HEOM_PROP_CHEBYSHEV_MIXED)
+            fail(HEOM_E_ARG, "unknown propagation method");
         DeviceScope dsc(c->device);
         const int ns = c->nalf * c->nspin;
         PropBuffers B(c, 5, (int64_t)nstep * ns);
@@ -228,18 +308,32 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
         CK(cudaMemcpyAsync(B.clk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
         double delta = 0.0;
         std::vector<double> bes;
-        if (method == HEOM_PROP_CHEBYSHEV) {
+        if (method != HEOM_PROP_RK4) {
             delta = cheby_width(c);
             if (!(delta > 0)) fail(HEOM_E_ARG, "Chebyshev propagation needs a nonzero spectral width");
             const int nt = std::max(2, cheby_terms(delta, dt, 1e-21));
             for (int n = 0; n < nt; n++) bes.push_back(bessel_j(n, delta * dt));
         }
         const CoefSet K = ctx_coefs(c);
+        // FP32x2 state and recurrence for HEOM_PROP_CHEBYSHEV_MIXED
+        float4 *dfmem = nullptr;
+        float4 *xdf = nullptr, *vdf[4] = {nullptr, nullptr, nullptr, nullptr}, *gdf = nullptr;
+        struct DfFree { float4 *&p; ~DfFree() { if (p) cudaFree(p); } } df_free{dfmem};
+        if (method == HEOM_PROP_CHEBYSHEV_MIXED) {
+            const int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64, nd = std::max<int64_t>(1, c->dfwd.view.nado);
+            CK(cudaMalloc((void **)&dfmem, sizeof(float4) * (size_t)(5 * vs + nd)));
+            CK(cudaMemsetAsync(dfmem, 0, sizeof(float4) * (size_t)(5 * vs + nd), c->stream));
+            xdf = dfmem;
+            for (int k = 0; k < 4; k++) vdf[k] = dfmem + (k + 1) * vs;
+            gdf = dfmem + 5 * vs;
+            k_to_df<<<grid_for(c->lunk), NT, 0, c->stream>>>(c->lunk, x, xdf);
+        }
         if (nstep > 0) {
             cudaGraph_t g = nullptr;
             cudaGraphExec_t ge = nullptr;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_step(c, method, K.k64, B, x, delta, bes, true);
+            if (method == HEOM_PROP_CHEBYSHEV_MIXED) enqueue_step_df(c, K.kdf, B, xdf, vdf, gdf, delta, bes, true);
+            else enqueue_step(c, method, K.k64, B, x, delta, bes, true);
             CK(cudaStreamEndCapture(c->stream, &g));
             CK(cudaGraphInstantiate(&ge, g, 0));
             cudaError_t err = cudaSuccess;
@@ -248,6 +342,7 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
             cudaGraphDestroy(g);
             CK(err);
         }
+        if (method == HEOM_PROP_CHEBYSHEV_MIXED) k_from_df<<<grid_for(c->lunk), NT, 0, c->stream>>>(c->lunk, xdf, x);
         CK(cudaMemcpyAsync(rho, x, sizeof(double2) * c->lunk, cudaMemcpyDeviceToHost, c->stream));
         if (jt_out && nstep > 0)
             CK(cudaMemcpyAsync(jt_out, B.jt, sizeof(double) * (size_t)nstep * ns, cudaMemcpyDeviceToHost, c->stream));

@@ -28,7 +28,7 @@ STATIC_CURRENT_MAX = 4096
 def static_current_chunks(n, limit=STATIC_CURRENT_MAX):
     """(first instance, count) of the consecutive calls that cover n instances."""
     return [(b0, min(limit, n - b0)) for b0 in range(0, n, limit)]
-PROP_RK4, PROP_CHEBYSHEV = 0, 1
+PROP_RK4, PROP_CHEBYSHEV, PROP_CHEBYSHEV_MIXED = 0, 1, 2
 ERRORS = {-1: "invalid argument", -2: "CUDA failure", -3: "out of memory", -4: "unsupported",
           -5: "TFQMR breakdown", -6: "not converged", -7: "device wait timed out"}
 

@@ -25,7 +25,9 @@
 extern "C" {
 #endif
 
-#define HEOM_ABI_VERSION 3
+/* 4: heom_grad_opts.precision, heom_solve_opts.interleave (in place of a reserved field),
+ *    heom_batch_set_tiers */
+#define HEOM_ABI_VERSION 4
 
 enum {
     HEOM_OK = 0,
@@ -230,8 +232,10 @@ int heom_occupation(heom_ctx *ctx, const double _Complex *rho, double *occ);
 /* Time propagation (td/intstp.f90 RK4; td/chebyshev.f90 Chebyshev, on the sparse
  * layout).  rho (host, lunk) advanced from t0 by nstep steps of dt.  If jt_out is
  * non-NULL it receives the current jt (nalf*nspin) at the start of every step
- * (nstep rows), like curr.data. */
-enum { HEOM_PROP_RK4 = 0, HEOM_PROP_CHEBYSHEV = 1 };
+ * (nstep rows), like curr.data.  HEOM_PROP_CHEBYSHEV_MIXED: the Chebyshev steps with the
+ * state, the recurrence and the applies in FP32x2 (about 48 bits; the coefficients, the
+ * lead shifts and the currents in FP64); no counterpart in the reference. */
+enum { HEOM_PROP_RK4 = 0, HEOM_PROP_CHEBYSHEV = 1, HEOM_PROP_CHEBYSHEV_MIXED = 2 };
 int heom_propagate(heom_ctx *ctx, int32_t method, double t0, double dt, int32_t nstep,
                    double _Complex *rho, double *jt_out);
 

@@ -73,3 +73,36 @@ def test_full_size_propagation_buffers(method):
     rho, jt = ctx.propagate(rho0, 0.0, 0.05, 3, method=method, currents=True)
     np.testing.assert_allclose(jt[0], ctx.current(rho0).T.reshape(-1), rtol=1e-12, atol=1e-9)
     assert np.isfinite(rho).all() and np.isfinite(jt).all()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_mixed_chebyshev_follows_the_fp64_one(name):
+    """HEOM_PROP_CHEBYSHEV_MIXED (state, recurrence and applies in FP32x2) against the FP64
+    Chebyshev run over 400 steps of 0.05: states within 1e-11 relative, currents within 1e-10
+    of the largest."""
+    m = heomq.Model(CASES[name])
+    ctx = heomq.Context(m)
+    rho0 = m.initial_guess()
+    r64, j64 = ctx.propagate(rho0, 0.0, 0.05, 400, method=heomq.PROP_CHEBYSHEV, currents=True)
+    rmx, jmx = ctx.propagate(rho0, 0.0, 0.05, 400, method=heomq.PROP_CHEBYSHEV_MIXED, currents=True)
+    assert _rel(rmx, r64) <= 1e-11, _rel(rmx, r64)
+    assert _rel(jmx, j64) <= 1e-10, _rel(jmx, j64)
+
+
+def test_mixed_chebyshev_at_full_size():
+    """The gradient configuration's model (double dot, tier 4, M = 3) from the V = 0 steady
+    state under the step bias: 1 000 mixed Chebyshev steps of 0.05 against the FP64 ones,
+    currents within 1e-9 of the largest and the time integral within 1e-10."""
+    cfg = cf.dqd(ntier=5, nmats=3, V=0.8)
+    m0 = heomq.Model(cf.dqd(ntier=5, nmats=3, V=0.0))
+    c0 = heomq.Context(m0, adjoint=False)
+    rho_eq, info = c0.solve_tfqmr(crit=1e-12, precision=heomq.PREC_FP64_REFINED, max_refine=16)
+    assert info.converged
+    m = heomq.Model(cfg)
+    ctx = heomq.Context(m, adjoint=False)
+    _, j64 = ctx.propagate(rho_eq, 0.0, 0.05, 1000, method=heomq.PROP_CHEBYSHEV, currents=True)
+    _, jmx = ctx.propagate(rho_eq, 0.0, 0.05, 1000, method=heomq.PROP_CHEBYSHEV_MIXED, currents=True)
+    assert _rel(jmx, j64) <= 1e-9, _rel(jmx, j64)
+    i64, imx = j64[:, 0::m.nalf].sum(), jmx[:, 0::m.nalf].sum()
+    assert abs(imx / i64 - 1) <= 1e-10
+
