@@ -332,6 +332,9 @@ def gradient_record():
     t0 = time.perf_counter()
     J, dJ = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32)
     t_grad = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Jm, dJm = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32, method=heomq.PROP_CHEBYSHEV_MIXED)
+    t_grad_mx = time.perf_counter() - t0
 
     def integral(scale, method=heomq.PROP_CHEBYSHEV):
         c = heomq.Context(m, adjoint=False, amps=scale * amps, tchar=tchar)
@@ -349,7 +352,8 @@ def gradient_record():
     ctx.close()
     td = {"steps": 1000, "dt": 0.05, "checkpoint_every": 32, "forward_s": t_fwd, "gradient_s": t_grad,
           "dJ_dA": dJ, "central_difference": fd, "rel_err": abs(dJ - fd) / abs(fd),
-          "forward_mixed_s": t_mx, "integral_rel_diff_mixed_vs_fp64": abs(jmx / j1 - 1)}
+          "forward_mixed_s": t_mx, "integral_rel_diff_mixed_vs_fp64": abs(jmx / j1 - 1),
+          "gradient_mixed_s": t_grad_mx, "dJ_dA_mixed_rel_diff_vs_fp64": abs(dJm / dJ - 1)}
     return {"model": "serial double dot nd=16, tier 4, M=3", "steady": steady, "chebyshev": td}
 
 

@@ -9,7 +9,10 @@
 //     dJ/d rho = mu_0,   dJ/dA += sum_{j>=1} s_j Re<mu_j, (dL/dA) Q_{j-1}>,
 // s_1 = 1/delta, s_j = 2/delta.  dL/dA is diagonal: i sum_k cnt_k(ado) amps_k onset_k(t).
 // The forward pass stores rho every `checkpoint_every` steps; the reverse pass recomputes
-// the states of one segment from its checkpoint, then walks it backwards.
+// the states of one segment from its checkpoint, then walks it backwards.  The vectors and
+// the applies are FP64 (HEOM_PROP_CHEBYSHEV) or FP32x2 (HEOM_PROP_CHEBYSHEV_MIXED, the
+// streaming updates computed in FP64 from the stored values); the coefficients, the lead
+// shifts and the accumulated parameter term are FP64 in both.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -22,32 +25,51 @@ namespace {
 constexpr int NT = 256;
 int grid_for(int64_t n) { int64_t g = (n + NT - 1) / NT; return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g)); }
 
+// a stored complex value as FP64, and back (identity for FP64)
+template <typename T> struct Io;
+template <> struct Io<double> {
+    static __device__ __forceinline__ double2 ld(const double2 &v) { return v; }
+    static __device__ __forceinline__ void st(double2 &v, double2 a) { v = a; }
+};
+template <> struct Io<DF> {
+    static __device__ __forceinline__ double2 ld(const float4 &v)
+    {
+        const Num<DF>::A a = Num<DF>::load(v);
+        return make_double2(Num<DF>::re(a), Num<DF>::im(a));
+    }
+    static __device__ __forceinline__ void st(float4 &v, double2 a) { v = Num<DF>::store(Num<DF>::from_d(a.x, a.y)); }
+};
+
 // Q_k = (first ? 0 : Q_{k-2}) + s lq
-__global__ void k_qstep(int64_t n, const double2 *qm2, const double2 *lq, double2 *q, double s, int first)
+template <typename T>
+__global__ void k_qstep(int64_t n, const typename Num<T>::V *qm2, const typename Num<T>::V *lq, typename Num<T>::V *q,
+                        double s, int first)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 l = lq[i];
-        const double2 b = first ? make_double2(0, 0) : qm2[i];
-        q[i] = make_double2(b.x + s * l.x, b.y + s * l.y);
+        const double2 l = Io<T>::ld(lq[i]);
+        const double2 b = first ? make_double2(0, 0) : Io<T>::ld(qm2[i]);
+        Io<T>::st(q[i], make_double2(b.x + s * l.x, b.y + s * l.y));
     }
 }
 
 // mu_j = a lam + s_next lh + mu_{j+2} (terms present when the pointers are non-null), then
 // acc[e] += s_j d_e Re(conj(mu_j) i Q_{j-1}) with d_e = sum_k cnt_k es_k (when qprev != null)
-__global__ void k_mu(int64_t n, const DevPlan P, const double *es, const double2 *lam, double a, const double2 *lh,
-                     double s_next, const double2 *mu2, double2 *mu, const double2 *qprev, double s_j, double *acc)
+template <typename T>
+__global__ void k_mu(int64_t n, const DevPlan P, const double *es, const typename Num<T>::V *lam, double a,
+                     const typename Num<T>::V *lh, double s_next, const typename Num<T>::V *mu2, typename Num<T>::V *mu,
+                     const typename Num<T>::V *qprev, double s_j, double *acc)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 l = lam[i];
+        const double2 l = Io<T>::ld(lam[i]);
         double2 m = make_double2(a * l.x, a * l.y);
-        if (lh) { m.x += s_next * lh[i].x; m.y += s_next * lh[i].y; }
-        if (mu2) { m.x += mu2[i].x; m.y += mu2[i].y; }
-        mu[i] = m;
+        if (lh) { const double2 h = Io<T>::ld(lh[i]); m.x += s_next * h.x; m.y += s_next * h.y; }
+        if (mu2) { const double2 u = Io<T>::ld(mu2[i]); m.x += u.x; m.y += u.y; }
+        Io<T>::st(mu[i], m);
         if (qprev) {
             const unsigned cnt = (unsigned)P.ado_cnt[P.ent_ado[i]];
             double d = 0;
             for (int k = 0; k < 4; k++) d += (double)(int8_t)(cnt >> (8 * k)) * es[k];
-            const double2 q = qprev[i];
+            const double2 q = Io<T>::ld(qprev[i]);
             // Re(conj(m) * i q) = m.x * (-q.y) + m.y * q.x
             acc[i] += s_j * d * (m.y * q.x - m.x * q.y);
         }
@@ -55,26 +77,42 @@ __global__ void k_mu(int64_t n, const DevPlan P, const double *es, const double2
 }
 
 // lam = dt c + mu0
-__global__ void k_lambda(int64_t n, const double2 *c, double dt, const double2 *mu0, double2 *lam)
+template <typename T>
+__global__ void k_lambda(int64_t n, const typename Num<T>::V *c, double dt, const typename Num<T>::V *mu0,
+                         typename Num<T>::V *lam)
 {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        lam[i] = make_double2(dt * c[i].x + mu0[i].x, dt * c[i].y + mu0[i].y);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 cc = Io<T>::ld(c[i]), m = Io<T>::ld(mu0[i]);
+        Io<T>::st(lam[i], make_double2(dt * cc.x + m.x, dt * cc.y + m.y));
+    }
 }
 
 __global__ void k_set_step(PropClock *clk, int64_t n) { clk->n = n; }
 
 // One term of a Chebyshev step with its Q kept: Q_k = (first ? 0 : Q_{k-2}) + s lq and
 // out = (first ? c0 Q_0 : out) + c Q_k (the arithmetic of the propagation step)
-__global__ void k_qcheb(int64_t n, const double2 *q0, const double2 *qm2, const double2 *lq, double2 *q, double2 *out,
-                        double s, double c, int first, double c0)
+template <typename T>
+__global__ void k_qcheb(int64_t n, const typename Num<T>::V *q0, const typename Num<T>::V *qm2, const typename Num<T>::V *lq,
+                        typename Num<T>::V *q, typename Num<T>::V *out, double s, double c, int first, double c0)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 l = lq[i];
-        const double2 v = first ? make_double2(s * l.x, s * l.y) : make_double2(qm2[i].x + s * l.x, qm2[i].y + s * l.y);
-        q[i] = v;
-        const double2 r = first ? make_double2(c0 * q0[i].x, c0 * q0[i].y) : out[i];
-        out[i] = make_double2(r.x + c * v.x, r.y + c * v.y);
+        const double2 l = Io<T>::ld(lq[i]);
+        double2 v;
+        if (first) v = make_double2(s * l.x, s * l.y);
+        else { const double2 p = Io<T>::ld(qm2[i]); v = make_double2(p.x + s * l.x, p.y + s * l.y); }
+        Io<T>::st(q[i], v);
+        double2 r;
+        if (first) { const double2 z = Io<T>::ld(q0[i]); r = make_double2(c0 * z.x, c0 * z.y); }
+        else r = Io<T>::ld(out[i]);
+        Io<T>::st(out[i], make_double2(r.x + c * v.x, r.y + c * v.y));
     }
+}
+
+template <typename T>
+__global__ void k_from_host_d(int64_t n, const double2 *a, typename Num<T>::V *o)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        Io<T>::st(o[i], a[i]);
 }
 
 __global__ void k_sum(int64_t n, const double *a, double *out)
@@ -90,156 +128,184 @@ __global__ void k_sum(int64_t n, const double *a, double *out)
     }
     if (threadIdx.x == 0) *out = red[0];
 }
+
+template <typename T> DevCoef<T> pick(const CoefSet &K);
+template <> DevCoef<double> pick<double>(const CoefSet &K) { return K.k64; }
+template <> DevCoef<DF> pick<DF>(const CoefSet &K) { return K.kdf; }
+
+// J and dJ/dA with vectors and applies in the number type T
+template <typename T>
+void td_gradient_run(heom_ctx *c, double dt, int nstep, int ck, const double _Complex *rho0, double *integral,
+                     double *dintegral)
+{
+    using V = typename Num<T>::V;
+    const int64_t N = c->lunk + 1, L = c->lunk;
+    const int ns = c->nalf * c->nspin;
+    const double delta = cheby_width(c);
+    if (!(delta > 0)) fail(HEOM_E_ARG, "Chebyshev propagation needs a nonzero spectral width");
+    const int K = std::max(2, cheby_terms(delta, dt, 1e-21));
+    std::vector<double> bes(K);
+    for (int k = 0; k < K; k++) bes[k] = bessel_j(k, delta * dt);
+    const int ncp = (nstep + ck - 1) / ck;
+    // buffers: 5 FP64 propagation vectors (FP64 forward steps) and the stage data; in T:
+    // checkpoints, one segment of states, Q_0..Q_{K-1}, 3 mu, lambda, L^H output, the current
+    // functional, the forward state and recurrence (FP32x2 forward steps); the per-entry
+    // accumulator in FP64
+    PropBuffers B(c, 5, (int64_t)nstep * ns);
+    B.dt = dt;
+    std::vector<void *> blocks;
+    auto dalloc = [&](size_t bytes) { void *p = nullptr; CK(cudaMalloc(&p, bytes)); blocks.push_back(p); CK(cudaMemsetAsync(p, 0, bytes, c->stream)); return p; };
+    try {
+        const size_t vb = sizeof(V) * (size_t)N;
+        const size_t nd = (size_t)std::max<int32_t>(1, std::max(c->dfwd.view.nado, c->dadj.view.nado));
+        char *cps = (char *)dalloc(vb * ncp);
+        char *seg = (char *)dalloc(vb * (ck + 1));
+        char *qs = (char *)dalloc(vb * K);
+        V *mu[3] = {(V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb)};
+        V *lam = (V *)dalloc(vb), *lh = (V *)dalloc(vb), *cv = (V *)dalloc(vb);
+        V *x = (V *)dalloc(vb), *xv[4] = {(V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb)};
+        V *gdT = (V *)dalloc(sizeof(V) * nd), *gdaT = (V *)dalloc(sizeof(V) * nd);
+        double *acc = (double *)dalloc(sizeof(double) * N);
+        double *dsum = (double *)dalloc(sizeof(double));
+        double2 *stage = (double2 *)dalloc(sizeof(double2) * N);
+        auto cp = [&](int i) { return (V *)(cps + vb * i); };
+        auto st = [&](int i) { return (V *)(seg + vb * i); };
+        auto Q = [&](int k) { return (V *)(qs + vb * k); };
+        cudaStream_t s = c->stream;
+        const int gL = grid_for(L);
+        std::vector<cd> ch(N, 0.0);
+        for (const CurrentTerm &tm : c->cur_terms)
+            if (tm.slot % c->nalf == 0) ch[tm.entry] += cd(0.0, -2.0 * kJconst * tm.sign);
+        CK(cudaMemcpyAsync(stage, ch.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+        k_from_host_d<T><<<gL, NT, 0, s>>>(N, stage, cv);
+        CK(cudaMemcpyAsync(stage, rho0, sizeof(double2) * L, cudaMemcpyHostToDevice, s));
+        k_from_host_d<T><<<gL, NT, 0, s>>>(L, stage, x);
+        PropClock h;
+        prop_clock_init(c, h, 0.0, dt, 1.0);
+        CK(cudaMemcpyAsync(B.clk, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+        const CoefSet Kf = ctx_coefs(c, false), Ka = ctx_coefs(c, true);
+        // forward pass: checkpoints and currents
+        {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            if constexpr (std::is_same<T, double>::value) enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, true);
+            else enqueue_step_df(c, Kf.kdf, B, x, xv, gdT, delta, bes, true);
+            CK(cudaStreamEndCapture(s, &g));
+            CK(cudaGraphInstantiate(&ge, g, 0));
+            cudaError_t err = cudaSuccess;
+            for (int n = 0; n < nstep && err == cudaSuccess; n++) {
+                if (n % ck == 0) err = cudaMemcpyAsync(cp(n / ck), x, vb, cudaMemcpyDeviceToDevice, s);
+                if (err == cudaSuccess) err = cudaGraphLaunch(ge, s);
+            }
+            cudaGraphExecDestroy(ge);
+            cudaGraphDestroy(g);
+            CK(err);
+        }
+        std::vector<double> jt((size_t)nstep * ns);
+        CK(cudaMemcpyAsync(jt.data(), B.jt, sizeof(double) * jt.size(), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        double J = 0;
+        for (int n = 0; n < nstep; n++)
+            for (int k = 0; k < ns; k++)
+                if (k % c->nalf == 0) J += dt * jt[(size_t)n * ns + k];
+        *integral = J;
+        // reverse pass
+        const DevPlan &P = c->dfwd.view, &PA = c->dadj.view;
+        DevCoef<T> KF = pick<T>(Kf), KA = pick<T>(Ka);
+        KF.trace_on = 0; KA.trace_on = 0;
+        KF.eshift = B.es; KA.eshift = B.es;
+        // the step's lead shifts (stage_prepare) and ADO diagonals of both plans in T
+        auto prepare = [&](bool adj) {
+            stage_prepare(c, B, 0.0, false, s);
+            fill_gdiag<T>(P, KF, gdT, 1, s);
+            if (adj) fill_gdiag<T>(PA, KA, gdaT, 1, s);
+        };
+        // when a segment's Q_k (K ck vectors) fit in half the free device memory, the
+        // recomputation of the segment keeps them, and the backward walk reuses them
+        // instead of rebuilding them (K - 1 fewer applies per step)
+        size_t mem_free = 0, mem_total = 0;
+        CK(cudaMemGetInfo(&mem_free, &mem_total));
+        char *qseg = nullptr;
+        if ((double)vb * K * ck <= 0.5 * (double)mem_free) qseg = (char *)dalloc(vb * (size_t)K * ck);
+        auto QS = [&](int i, int k) { return (V *)(qseg + vb * ((size_t)i * K + k)); };
+        for (int sg = ncp - 1; sg >= 0; sg--) {
+            const int n0 = sg * ck, n1 = std::min(nstep, n0 + ck);
+            // recompute rho_{n0} .. rho_{n1-1} (and keep every step's Q_k when qseg is there)
+            CK(cudaMemcpyAsync(st(0), cp(sg), vb, cudaMemcpyDeviceToDevice, s));
+            for (int n = n0; n < (qseg ? n1 : n1 - 1); n++) {
+                k_set_step<<<1, 1, 0, s>>>(B.clk, n);
+                prepare(false);
+                auto Qk = [&](int k) { return qseg ? QS(n - n0, k) : Q(k); };
+                CK(cudaMemcpyAsync(Qk(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                for (int k = 1; k < K; k++) {
+                    launch_apply<T, false>(P, KF, Qk(k - 1), lh, 1, N, nullptr, s);
+                    k_qcheb<T><<<gL, NT, 0, s>>>(L, Qk(0), k >= 2 ? Qk(k - 2) : nullptr, lh, Qk(k), x,
+                                                 k == 1 ? 1.0 / delta : 2.0 / delta, 2.0 * bes[k], k == 1, bes[0]);
+                }
+                if (n < n1 - 1) CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
+            }
+            for (int n = n1 - 1; n >= n0; n--) {
+                k_set_step<<<1, 1, 0, s>>>(B.clk, n);
+                prepare(true);
+                // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1} (kept, or rebuilt)
+                auto Qn = [&](int k) { return qseg ? QS(n - n0, k) : Q(k); };
+                if (!qseg) {
+                    CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
+                    for (int k = 1; k < K; k++) {
+                        launch_apply<T, false>(P, KF, Q(k - 1), lh, 1, N, nullptr, s);
+                        k_qstep<T><<<gL, NT, 0, s>>>(L, k >= 2 ? Q(k - 2) : nullptr, lh, Q(k), k == 1 ? 1.0 / delta : 2.0 / delta, k == 1);
+                    }
+                }
+                // mu recurrence, lambda = dJ/d rho_{n+1} (zero at n = nstep - 1)
+                const V *m2 = nullptr, *m1 = nullptr;
+                int slot = 0;
+                for (int j = K - 1; j >= 0; j--) {
+                    V *mj = mu[slot];
+                    slot = (slot + 1) % 3;
+                    const double a = j == 0 ? bes[0] : 2.0 * bes[j];
+                    const double s_next = (j + 1 == 1) ? 1.0 / delta : 2.0 / delta;
+                    if (m1) launch_apply<T, true>(PA, KA, m1, lh, 1, N, nullptr, s);
+                    k_mu<T><<<gL, NT, 0, s>>>(L, P, B.es, lam, a, m1 ? lh : nullptr, s_next, m2, mj,
+                                              j >= 1 ? Qn(j - 1) : nullptr, j == 1 ? 1.0 / delta : 2.0 / delta, acc);
+                    m2 = m1;
+                    m1 = mj;
+                }
+                k_lambda<T><<<gL, NT, 0, s>>>(L, cv, dt, m1, lam);
+            }
+            CK(cudaGetLastError());
+        }
+        k_sum<<<1, NT, 0, s>>>(L, acc, dsum);
+        double dJ = 0;
+        CK(cudaMemcpyAsync(&dJ, dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        *dintegral = dJ;
+        for (void *p : blocks) cudaFree(p);
+    } catch (...) { for (void *p : blocks) cudaFree(p); throw; }
+}
 }  // namespace
 }  // namespace heom
 
 using namespace heom;
 
-extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t checkpoint_every,
-                                const double _Complex *rho0, double *integral, double *dintegral)
+extern "C" int heom_td_gradient_ex(heom_ctx *c, int32_t method, double dt, int32_t nstep, int32_t checkpoint_every,
+                                   const double _Complex *rho0, double *integral, double *dintegral)
 {
     return guarded([&] {
         require_ctx(c);
         if (!rho0 || !integral || !dintegral || nstep < 1 || !(dt > 0)) fail(HEOM_E_ARG, "bad arguments");
         if (!c->has_adj) fail(HEOM_E_ARG, "the context was created without the adjoint plan");
+        if (method != HEOM_PROP_CHEBYSHEV && method != HEOM_PROP_CHEBYSHEV_MIXED)
+            fail(HEOM_E_ARG, "the gradient runs through HEOM_PROP_CHEBYSHEV or HEOM_PROP_CHEBYSHEV_MIXED steps");
         DeviceScope dsc(c->device);
         const int ck = checkpoint_every > 0 ? checkpoint_every : 32;
-        const int64_t N = c->lunk + 1, L = c->lunk;
-        const int ns = c->nalf * c->nspin;
-        const double delta = cheby_width(c);
-        if (!(delta > 0)) fail(HEOM_E_ARG, "Chebyshev propagation needs a nonzero spectral width");
-        const int K = std::max(2, cheby_terms(delta, dt, 1e-21));
-        std::vector<double> bes(K);
-        for (int k = 0; k < K; k++) bes[k] = bessel_j(k, delta * dt);
-        const int ncp = (nstep + ck - 1) / ck;
-        // buffers: 5 propagation vectors; checkpoints; one segment of states; Q_0..Q_{K-1};
-        // 3 mu; lambda; L^H output; the current functional; the per-entry accumulator
-        PropBuffers B(c, 5, (int64_t)nstep * ns);
-        B.dt = dt;
-        std::vector<void *> blocks;
-        auto dalloc = [&](size_t bytes) { void *p = nullptr; CK(cudaMalloc(&p, bytes)); blocks.push_back(p); CK(cudaMemsetAsync(p, 0, bytes, c->stream)); return p; };
-        try {
-            const size_t vb = sizeof(double2) * (size_t)N;
-            char *cps = (char *)dalloc(vb * ncp);
-            char *seg = (char *)dalloc(vb * (ck + 1));
-            char *qs = (char *)dalloc(vb * K);
-            double2 *mu[3] = {(double2 *)dalloc(vb), (double2 *)dalloc(vb), (double2 *)dalloc(vb)};
-            double2 *lam = (double2 *)dalloc(vb), *lh = (double2 *)dalloc(vb), *cv = (double2 *)dalloc(vb);
-            double *acc = (double *)dalloc(sizeof(double) * N);
-            double *dsum = (double *)dalloc(sizeof(double));
-            auto cp = [&](int i) { return (double2 *)(cps + vb * i); };
-            auto st = [&](int i) { return (double2 *)(seg + vb * i); };
-            auto Q = [&](int k) { return (double2 *)(qs + vb * k); };
-            std::vector<cd> ch(N, 0.0);
-            for (const CurrentTerm &tm : c->cur_terms)
-                if (tm.slot % c->nalf == 0) ch[tm.entry] += cd(0.0, -2.0 * kJconst * tm.sign);
-            CK(cudaMemcpyAsync(cv, ch.data(), vb, cudaMemcpyHostToDevice, c->stream));
-            double2 *x = B.vec[4];
-            CK(cudaMemcpyAsync(x, rho0, sizeof(double2) * L, cudaMemcpyHostToDevice, c->stream));
-            PropClock h;
-            prop_clock_init(c, h, 0.0, dt, 1.0);
-            CK(cudaMemcpyAsync(B.clk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
-            const CoefSet Kf = ctx_coefs(c, false), Ka = ctx_coefs(c, true);
-            // forward pass: checkpoints and currents
-            {
-                cudaGraph_t g = nullptr;
-                cudaGraphExec_t ge = nullptr;
-                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-                enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, true);
-                CK(cudaStreamEndCapture(c->stream, &g));
-                CK(cudaGraphInstantiate(&ge, g, 0));
-                cudaError_t err = cudaSuccess;
-                for (int n = 0; n < nstep && err == cudaSuccess; n++) {
-                    if (n % ck == 0) err = cudaMemcpyAsync(cp(n / ck), x, vb, cudaMemcpyDeviceToDevice, c->stream);
-                    if (err == cudaSuccess) err = cudaGraphLaunch(ge, c->stream);
-                }
-                cudaGraphExecDestroy(ge);
-                cudaGraphDestroy(g);
-                CK(err);
-            }
-            std::vector<double> jt((size_t)nstep * ns);
-            CK(cudaMemcpyAsync(jt.data(), B.jt, sizeof(double) * jt.size(), cudaMemcpyDeviceToHost, c->stream));
-            CK(cudaStreamSynchronize(c->stream));
-            double J = 0;
-            for (int n = 0; n < nstep; n++)
-                for (int s = 0; s < ns; s++)
-                    if (s % c->nalf == 0) J += dt * jt[(size_t)n * ns + s];
-            *integral = J;
-            // reverse pass
-            const DevPlan &P = c->dfwd.view, &PA = c->dadj.view;
-            DevCoef<double> KF = Kf.k64, KA = Ka.k64;
-            KF.trace_on = 0; KA.trace_on = 0;
-            KF.eshift = B.es; KA.eshift = B.es;
-            KF.gdiag = B.gd; KA.gdiag = B.gda;   // refreshed by stage_prepare
-            cudaStream_t s = c->stream;
-            const int gL = grid_for(L);
-            // when a segment's Q_k (K ck vectors) fit in half the free device memory, the
-            // recomputation of the segment keeps them, and the backward walk reuses them
-            // instead of rebuilding them (K - 1 fewer applies per step)
-            size_t mem_free = 0, mem_total = 0;
-            CK(cudaMemGetInfo(&mem_free, &mem_total));
-            char *qseg = nullptr;
-            if ((double)vb * K * ck <= 0.5 * (double)mem_free) qseg = (char *)dalloc(vb * (size_t)K * ck);
-            auto QS = [&](int i, int k) { return (double2 *)(qseg + vb * ((size_t)i * K + k)); };
-            for (int sg = ncp - 1; sg >= 0; sg--) {
-                const int n0 = sg * ck, n1 = std::min(nstep, n0 + ck);
-                // recompute rho_{n0} .. rho_{n1-1}
-                CK(cudaMemcpyAsync(st(0), cp(sg), vb, cudaMemcpyDeviceToDevice, s));
-                for (int n = n0; n < n1 - 1 || (qseg && n < n1); n++) {
-                    if (qseg) {
-                        // the step from its Q_k, kept; rho_{n+1} = J0 Q_0 + 2 sum_k J_k Q_k
-                        k_set_step<<<1, 1, 0, s>>>(B.clk, n);
-                        stage_prepare(c, B, 0.0, false, s);
-                        CK(cudaMemcpyAsync(QS(n - n0, 0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
-                        for (int k = 1; k < K; k++) {
-                            launch_apply<double, false>(P, KF, QS(n - n0, k - 1), lh, 1, N, nullptr, s);
-                            k_qcheb<<<gL, NT, 0, s>>>(L, QS(n - n0, 0), k >= 2 ? QS(n - n0, k - 2) : nullptr, lh, QS(n - n0, k), x,
-                                                      k == 1 ? 1.0 / delta : 2.0 / delta, 2.0 * bes[k], k == 1, bes[0]);
-                        }
-                        if (n < n1 - 1) CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
-                        continue;
-                    }
-                    CK(cudaMemcpyAsync(x, st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
-                    k_set_step<<<1, 1, 0, s>>>(B.clk, n);
-                    enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, false);
-                    CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
-                }
-                for (int n = n1 - 1; n >= n0; n--) {
-                    k_set_step<<<1, 1, 0, s>>>(B.clk, n);
-                    stage_prepare(c, B, 0.0, true, s);
-                    // Q_0 = rho_n, Q_1 = L Q_0 / delta, Q_k = Q_{k-2} + (2/delta) L Q_{k-1} (kept, or rebuilt)
-                    auto Qn = [&](int k) { return qseg ? QS(n - n0, k) : Q(k); };
-                    if (!qseg) {
-                        CK(cudaMemcpyAsync(Q(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
-                        for (int k = 1; k < K; k++) {
-                            launch_apply<double, false>(P, KF, Q(k - 1), lh, 1, N, nullptr, s);
-                            k_qstep<<<gL, NT, 0, s>>>(L, k >= 2 ? Q(k - 2) : nullptr, lh, Q(k), k == 1 ? 1.0 / delta : 2.0 / delta, k == 1);
-                        }
-                    }
-                    // mu recurrence, lambda = dJ/d rho_{n+1} (zero at n = nstep - 1)
-                    const double2 *m2 = nullptr, *m1 = nullptr;
-                    int slot = 0;
-                    for (int j = K - 1; j >= 0; j--) {
-                        double2 *mj = mu[slot];
-                        slot = (slot + 1) % 3;
-                        const double a = j == 0 ? bes[0] : 2.0 * bes[j];
-                        const double s_next = (j + 1 == 1) ? 1.0 / delta : 2.0 / delta;
-                        if (m1) launch_apply<double, true>(PA, KA, m1, lh, 1, N, nullptr, s);
-                        k_mu<<<gL, NT, 0, s>>>(L, P, B.es, lam, a, m1 ? lh : nullptr, s_next, m2, mj,
-                                               j >= 1 ? Qn(j - 1) : nullptr, j == 1 ? 1.0 / delta : 2.0 / delta, acc);
-                        m2 = m1;
-                        m1 = mj;
-                    }
-                    k_lambda<<<gL, NT, 0, s>>>(L, cv, dt, m1, lam);
-                }
-                CK(cudaGetLastError());
-            }
-            k_sum<<<1, NT, 0, s>>>(L, acc, dsum);
-            double dJ = 0;
-            CK(cudaMemcpyAsync(&dJ, dsum, sizeof(double), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            *dintegral = dJ;
-            for (void *p : blocks) cudaFree(p);
-        } catch (...) { for (void *p : blocks) cudaFree(p); throw; }
+        if (method == HEOM_PROP_CHEBYSHEV) td_gradient_run<double>(c, dt, nstep, ck, rho0, integral, dintegral);
+        else td_gradient_run<DF>(c, dt, nstep, ck, rho0, integral, dintegral);
     });
+}
+
+extern "C" int heom_td_gradient(heom_ctx *c, double dt, int32_t nstep, int32_t checkpoint_every,
+                                const double _Complex *rho0, double *integral, double *dintegral)
+{
+    return heom_td_gradient_ex(c, HEOM_PROP_CHEBYSHEV, dt, nstep, checkpoint_every, rho0, integral, dintegral);
 }

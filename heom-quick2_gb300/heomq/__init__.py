@@ -125,6 +125,8 @@ SIGNATURES = {
     "heom_propagate": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_steady_gradient": (C.c_int, [C.c_void_p, _p(GradOpts), C.c_void_p, C.c_int32, C.c_void_p, _p(SolveInfo)]),
     "heom_td_gradient": (C.c_int, [C.c_void_p, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "heom_td_gradient_ex": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]),
     "heom_solve_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_bench_inner": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
@@ -492,11 +494,14 @@ class Context:
         _check(lib().heom_steady_gradient(self.h, C.byref(o), rho.ctypes.data, which, dI.ctypes.data, C.byref(info)))
         return dI, info
 
-    def td_gradient(self, rho0, dt, nstep, checkpoint_every=32):
+    def td_gradient(self, rho0, dt, nstep, checkpoint_every=32, method=PROP_CHEBYSHEV):
+        """(J, dJ/dA) of J = dt sum_n I_1(rho_n) through the Chebyshev steps of `method`
+        (PROP_CHEBYSHEV or PROP_CHEBYSHEV_MIXED)."""
         rho0 = _c128(rho0, self.lunk)
         val = C.c_double()
         grad = C.c_double()
-        _check(lib().heom_td_gradient(self.h, dt, nstep, checkpoint_every, rho0.ctypes.data, C.byref(val), C.byref(grad)))
+        _check(lib().heom_td_gradient_ex(self.h, method, dt, nstep, checkpoint_every, rho0.ctypes.data, C.byref(val),
+                                         C.byref(grad)))
         return val.value, grad.value
 
     def bench_apply(self, precision=PREC_FP64, reps=20, nbatch=1):

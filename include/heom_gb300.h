@@ -26,7 +26,7 @@ extern "C" {
 #endif
 
 /* 4: heom_grad_opts.precision, heom_solve_opts.interleave (in place of a reserved field),
- *    heom_batch_set_tiers */
+ *    heom_batch_set_tiers, HEOM_PROP_CHEBYSHEV_MIXED, heom_td_gradient_ex */
 #define HEOM_ABI_VERSION 4
 
 enum {
@@ -263,6 +263,10 @@ int heom_steady_gradient(heom_ctx *ctx, const heom_grad_opts *o, const double _C
  * reverse pass with checkpoints every k steps. rho0: initial state (host, lunk). */
 int heom_td_gradient(heom_ctx *ctx, double dt, int32_t nstep, int32_t checkpoint_every,
                      const double _Complex *rho0, double *integral, double *dintegral);
+/* The same through the steps of `method`: HEOM_PROP_CHEBYSHEV (as heom_td_gradient) or
+ * HEOM_PROP_CHEBYSHEV_MIXED (forward and reverse passes with FP32x2 vectors and applies). */
+int heom_td_gradient_ex(heom_ctx *ctx, int32_t method, double dt, int32_t nstep, int32_t checkpoint_every,
+                        const double _Complex *rho0, double *integral, double *dintegral);
 
 /* Batched steady states: many instances that share one table set and differ in
  * hs and eleadinfty are solved together (one vector per instance, one launch per

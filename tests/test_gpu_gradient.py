@@ -114,6 +114,9 @@ def test_td_gradient_matches_central_differences(name, nstep, ck):
     h = 1e-5
     fd = (integral(1 + h) - integral(1 - h)) / (2 * h)
     assert abs(dJ - fd) <= 1e-6 * abs(fd), (dJ, fd)
+    # through FP32x2 steps: the same integral and gradient to about 48-bit accumulation
+    Jm, dJm = ctx.td_gradient(rho_eq, dt, nstep, checkpoint_every=ck, method=heomq.PROP_CHEBYSHEV_MIXED)
+    assert abs(Jm / J - 1) < 1e-11 and abs(dJm / dJ - 1) < 1e-10, (Jm, J, dJm, dJ)
 
 
 def test_autograd_wrappers_match_the_entry_points():
@@ -195,3 +198,6 @@ def test_full_size_gradients_match_central_differences():
     assert abs(J / integral(1.0) - 1) < 1e-12
     fd = (integral(1 + 1e-5) - integral(1 - 1e-5)) / 2e-5
     assert abs(dJ - fd) <= 1e-6 * abs(fd), (dJ, fd)
+    # the same gradient through FP32x2 Chebyshev steps (forward and reverse)
+    Jm, dJm = ctx.td_gradient(rho_eq, 0.05, 1000, checkpoint_every=32, method=heomq.PROP_CHEBYSHEV_MIXED)
+    assert abs(Jm / J - 1) < 1e-10 and abs(dJm / dJ - 1) < 1e-9, (Jm, J, dJm, dJ)
