@@ -194,10 +194,11 @@ typedef struct {
     int32_t interleave;       /* MIXED: instances interleaved per entry group in the FP32x2 inner
                                  kernels (lanes of one entry share the plan's control flow and
                                  reads); 1 = none, 2..32 a power of two, 0 (default) = automatic:
-                                 a batch times its first two mixed solves with none and with the
-                                 smallest power of two >= nbatch (at most 32), and keeps the
-                                 faster; single solves use none.  An interleaved group runs
-                                 until all its instances have finished. */
+                                 the context times its first two mixed batch solves of each
+                                 batch size with none and with the smallest power of two >=
+                                 nbatch (at most 32), and keeps the faster for that size; single
+                                 solves use none.  An interleaved group runs until all its
+                                 instances have finished. */
 } heom_solve_opts;
 
 typedef struct {
