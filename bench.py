@@ -40,6 +40,9 @@ def parse():
                     help="profiler run: warm-up solves, then one timed mixed solve; prints one short line")
     ap.add_argument("--profile-inner", action="store_true",
                     help="profiler run of the two fused FP32x2 inner-iteration kernels: 3 warm-up + 2 timed launches each")
+    ap.add_argument("--inner-layout", default=None,
+                    help="--profile-inner: the instance layout GxL (interleave G, L instances per lane, e.g. 2x2) "
+                         "instead of the one the batch solves use")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
     ap.add_argument("--workload", default="steady", choices=["steady", "dos", "jacobi"],
@@ -412,11 +415,11 @@ def run_gb300(args, ws, rank, local, dist):
     x0[:, :L] = torch.from_numpy(x0h).to("cuda")
     x = torch.empty_like(x0)
 
-    def step(prec, crit=None, refine=8, check=True, interleave=0):
+    def step(prec, crit=None, refine=8, check=True, interleave=0, lane_instances=0):
         x.copy_(x0)
         torch.cuda.synchronize()
         return batch.solve_dev(x.data_ptr(), crit=crit or args.crit, precision=prec, max_refine=refine, check=check,
-                               interleave=interleave)
+                               interleave=interleave, lane_instances=lane_instances)
 
     if args.profile_apply:
         prec = {"fp64": heomq.PREC_FP64, "fp32x2": heomq.PREC_MIXED, "fp32": heomq.PREC_MIXED_FP32}[args.profile_apply]
@@ -427,14 +430,22 @@ def run_gb300(args, ws, rank, local, dist):
         ctx.close()
         return 0
     if args.profile_inner:
-        (sb, sa), (bb, ba) = ctx.bench_inner(heomq.PREC_MIXED, reps=2, nbatch=B)
-        print(json.dumps({"profile_inner": True, "batch": B, "k_in_b_us": sb * 1e6, "k_in_a_us": sa * 1e6,
-                          "alg_bytes": [bb, ba]}), flush=True)
+        if args.inner_layout:
+            g, lanes = (int(v) for v in args.inner_layout.split("x"))
+            (sb, sa), (bb, ba) = ctx.bench_inner_layout(g, lanes, reps=2, nbatch=B)
+        else:
+            (sb, sa), (bb, ba) = ctx.bench_inner(heomq.PREC_MIXED, reps=2, nbatch=B)
+        print(json.dumps({"profile_inner": True, "batch": B, "layout": args.inner_layout or "of the solves",
+                          "k_in_b_us": sb * 1e6, "k_in_a_us": sa * 1e6, "alg_bytes": [bb, ba]}), flush=True)
         batch.close()
         ctx.close()
         return 0
     for _ in range(args.warmup):
-        step(heomq.PREC_MIXED)   # the first two also tune the interleave of the inner kernels
+        step(heomq.PREC_MIXED)
+    # the automatic layout choice of the inner kernels times one solve with each candidate first
+    while ctx.tuned_layout(B) == (0, 0):
+        step(heomq.PREC_MIXED)
+    layout = ctx.tuned_layout(B)
     if args.profile:
         info = step(heomq.PREC_MIXED)
         print(json.dumps({"profile_run": True, "batch": B, "applies": info.iters, "seconds": info.seconds,
@@ -442,11 +453,12 @@ def run_gb300(args, ws, rank, local, dist):
         batch.close()
         ctx.close()
         return 0
-    # the two interleave settings the automatic choice compares, one solve each
-    g_max = 1
-    while g_max < B and g_max < 32:
-        g_max *= 2
-    interleave_ms = {str(g): 1e3 * step(heomq.PREC_MIXED, interleave=g).seconds for g in sorted({1, g_max})}
+    # the instance layouts the automatic choice compares: one solve and the two fused kernels each
+    layouts = {}
+    for g, lanes in heomq.layout_candidates(B):
+        (kb, ka), _ = ctx.bench_inner_layout(g, lanes, reps=10, nbatch=B)
+        layouts[f"{g}x{lanes}"] = {"solve_ms": 1e3 * step(heomq.PREC_MIXED, interleave=g, lane_instances=lanes).seconds,
+                                   "k_in_b_us": kb * 1e6, "k_in_a_us": ka * 1e6}
     # FP64 GPU path beside (same batch, same criterion)
     info64 = step(heomq.PREC_FP64)
     cur64 = [ctx.current(x[b, :L].cpu().numpy())[0].sum() for b in range(B)]
@@ -499,7 +511,9 @@ def run_gb300(args, ws, rank, local, dist):
     sec64, alg64 = ctx.bench_apply(heomq.PREC_FP64, reps=10, nbatch=B)
     peak, peak_kind = measured_peak_hbm()
     achieved = bb / sb / 1e9
-    prof = "inner_fp32x2_dqd_L4_batch8.md"
+    # ncu summary of the fused kernels in the chosen layout
+    prof = {(8, 1): "inner_fp32x2_interleaved_dqd_L4_batch8.md",
+            (2, 2): "inner_fp32x2_pairs_dqd_L4_batch8.md"}.get(layout, "inner_fp32x2_dqd_L4_batch8.md")
     traffic = profile_traffic(prof, "dram_bytes_per_launch_k_in_b")
     traffic_a = profile_traffic(prof, "dram_bytes_per_launch_k_in_a")
     # accuracy: both paths against a reference steady state refined in FP64 to ||b - A x|| <= 1e-12
@@ -547,7 +561,8 @@ def run_gb300(args, ws, rank, local, dist):
                        "l2": f"inputs larger than L2: {B} x 9 solver vectors x {L * 16 / 1e6:.1f} MB",
                        "parallelism": f"replicas x{ws}", "wall_s": wall,
                        "applies_per_solve": infos[-1].iters, "refinements": infos[-1].refinements,
-                       "inner_interleave_ms_per_solve": interleave_ms,
+                       "inner_layout": {"chosen": f"{layout[0]}x{layout[1]}", "candidates": layouts,
+                                        "key": "GxL: G instances interleaved per entry group, L per thread"},
                        "fp64": {"solves_per_s": ws * B / t64, "applies_per_solve": info64.iters,
                                 "apply_us": sec64 * 1e6, "apply_gbs_alg": alg64 / sec64 / 1e9},
                        "speedup_mixed_vs_fp64": (ws * B / t_step) / (ws * B / t64),
@@ -556,7 +571,8 @@ def run_gb300(args, ws, rank, local, dist):
                        "current_reference_resid": info_ref.resid, "other_configurations": configs},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_in_b<FP32x2, regularised>: apply of w plus the fused vector updates, over the batch",
+                         "kernel": f"k_in_b<FP32x2, regularised>, layout {layout[0]}x{layout[1]}: apply of w plus "
+                                   "the fused vector updates, over the batch",
                          "kernel_us": sb * 1e6, "alg_bytes_per_launch": bb,
                          "k_in_a": {"kernel_us": sa * 1e6, "alg_bytes_per_launch": ba, "achieved": ba / sa / 1e9,
                                     "traffic": traffic_a},

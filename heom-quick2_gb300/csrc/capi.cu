@@ -500,11 +500,11 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     constexpr int kInnerChunk = 25;   // 50 applies between residual checks, as in the reference driver
     const double itol = o.inner_tol > 0 ? o.inner_tol : (std::is_same<T, float>::value ? 1e-2 : 1e-10);
     InnerWork<T> W;
-    inner_alloc<T>(W, nbatch, N, c->stream, o.interleave);
+    inner_alloc<T>(W, nbatch, N, c->stream, o.interleave, o.lane_instances > 0 ? o.lane_instances : 1);
     typename Num<T>::V *gd = nullptr;
     float *pre = nullptr;
     double pre_kappa = 1.0, pre_max = 1.0;
-    // one graph of a chunk per lane configuration W.GE (instantiated on first use)
+    // one graph of a chunk per lane configuration (W.GE, W.ipl), instantiated on first use
     std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
     auto release = [&] {
         for (auto &g : graphs) {
@@ -546,11 +546,14 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             pre_max = hi;
         }
         W.tier_lim = KI.tier_lim;
+        if (W.ipl_max > 1 && (KI.tier_lim || KI.cf_half))
+            fail(HEOM_E_ARG, "two instances per lane: steady solves of whole hierarchies only");
         KI = inner_layout_coef<T>(W, PV, KI, c->stream);   // the workspace's instance-interleaved layout
         auto chunk_graph = [&]() -> cudaGraphExec_t {
-            auto it = graphs.find(W.GE);
+            const int key = 4 * W.GE + W.ipl;
+            auto it = graphs.find(key);
             if (it != graphs.end()) return it->second.second;
-            auto &g = graphs[W.GE];
+            auto &g = graphs[key];
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
             CK(cudaStreamEndCapture(c->stream, &g.first));
@@ -627,6 +630,21 @@ HEOM_MIXED_ROUNDS(DF)
 HEOM_MIXED_ROUNDS(double)
 #undef HEOM_MIXED_ROUNDS
 
+// The layouts (interleave, instances per lane) the automatic choice of the mixed batch
+// solves compares: one instance per group; two instances per lane in groups of two (the
+// iterates of the first, with the plan decoded once for two instances; not for truncated
+// batches); the largest interleave with one and with two instances per lane.
+std::vector<std::pair<int, int>> layout_candidates(int nbatch, bool truncated)
+{
+    const int g = inner_default_interleave(nbatch);
+    std::vector<std::pair<int, int>> c = {{1, 1}};
+    if (g == 1) return c;
+    if (!truncated) c.push_back({2, 2});
+    if (g > 2 || truncated) c.push_back({g, 1});
+    if (g > 2 && !truncated) c.push_back({g, 2});
+    return c;
+}
+
 // Solve A x = rhs (rhs = e_trace when rhs == nullptr) for nbatch instances, in FP64 or
 // mixed precision.  x: device FP64, nbatch vectors with stride vstride (vstride >= lunk+1),
 // holding the initial guess on entry.
@@ -636,6 +654,9 @@ void solve_device(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
     const int64_t N = c->lunk + 1;
     int nlim = o.maxit0 / 2;
     if (nlim < 1) nlim = 1;
+    if (o.lane_instances < 0 || o.lane_instances > 2) fail(HEOM_E_ARG, "lane_instances must be 0, 1 or 2");
+    if (o.precision == HEOM_PREC_MIXED && o.lane_instances == 2 && o.interleave == 1)
+        fail(HEOM_E_ARG, "two instances per lane need an interleave of at least 2");
     info = heom_solve_info{};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
@@ -1196,23 +1217,21 @@ int heom_batch_solve_dev(heom_batch *B, const heom_solve_opts *o, void *x_dev, h
             }
         }
         heom_solve_info inf;
-        // automatic interleave of the mixed solves: the context's first two mixed solves of a
-        // batch of this size run with none and with the largest useful one; later ones keep
-        // the faster
+        // automatic layout of the mixed solves' inner kernels: the context's first mixed
+        // solves of a batch of this size and kind run with each candidate layout; later ones
+        // keep the fastest
         heom_solve_opts oo = *o;
-        heom_ctx::InterleaveTune *tu = nullptr;
-        int slot = -1;
+        heom_ctx::LayoutTune *tu = nullptr;
         if (oo.precision == HEOM_PREC_MIXED && oo.interleave == 0) {
-            const int cand[2] = {1, inner_default_interleave(B->nbatch)};
-            if (cand[1] == 1) oo.interleave = 1;
-            else {
-                tu = &c->il_tune[B->nbatch];
-                if (tu->tried < 2) oo.interleave = cand[slot = tu->tried];
-                else oo.interleave = cand[tu->seconds[1] < tu->seconds[0] ? 1 : 0];
-            }
+            tu = &c->il_tune[{B->nbatch, B->tier_lim ? 1 : 0}];
+            if (tu->cand.empty()) tu->cand = layout_candidates(B->nbatch, B->tier_lim != nullptr);
+            const std::pair<int, int> l = tu->done() ? tu->best() : tu->cand[tu->seconds.size()];
+            oo.interleave = l.first;
+            oo.lane_instances = l.second;
+            if (tu->done()) tu = nullptr;
         }
         solve_device(c, oo, (double2 *)x_dev, B->nbatch, B->vs, false, nullptr, inf, CoefSet{K64, K32, KDF});
-        if (slot >= 0) { tu->seconds[slot] = inf.seconds; tu->tried++; }
+        if (tu) tu->seconds.push_back(inf.seconds);
         if (info) *info = inf;
         if (!inf.converged) fail(HEOM_E_NOCONV, "batched TFQMR did not reach crit");
     });
@@ -1321,16 +1340,20 @@ double plan_bytes(heom_ctx *c)
     return st[8];
 }
 
+// layout (interleave G, instances per lane) of the inner kernels: G = 0 selects the one the
+// batch solves of this size use (the tuned one once tuned, else the largest interleave)
 template <typename T>
-void time_inner(heom_ctx *c, const BenchInputs &I, int nbatch, int reps, double *seconds, double *bytes)
+void time_inner(heom_ctx *c, const BenchInputs &I, int nbatch, int reps, double *seconds, double *bytes, int G = 0,
+                int ipl = 1)
 {
     const int64_t N = c->lunk + 1;
     InnerWork<T> W;
-    // the interleave the batch solves of this size use (the tuned one, once tuned)
-    int G = 0;
-    auto it = c->il_tune.find(nbatch);
-    if (it != c->il_tune.end() && it->second.tried >= 2) G = it->second.seconds[1] < it->second.seconds[0] ? 0 : 1;
-    inner_alloc<T>(W, nbatch, N, c->stream, G);
+    if (G == 0) {
+        ipl = 1;
+        auto it = c->il_tune.find({nbatch, 0});
+        if (it != c->il_tune.end() && it->second.done()) std::tie(G, ipl) = it->second.best();
+    }
+    inner_alloc<T>(W, nbatch, N, c->stream, G, ipl);
     try {
         upload_rt_to<T>(c, W.rt, N);
         float mb = 0, ma = 0;
@@ -1407,6 +1430,36 @@ int heom_bench_inner(heom_ctx *c, int32_t precision, int32_t nbatch, int32_t rep
         else if (precision == HEOM_PREC_MIXED_FP32) time_inner<float>(c, I, nbatch, reps, seconds, bytes);
         else if (precision == HEOM_PREC_FP64_REFINED) time_inner<double>(c, I, nbatch, reps, seconds, bytes);
         else fail(HEOM_E_ARG, "heom_bench_inner: precision must be one of the refined (inner-solve) precisions");
+    });
+}
+
+int heom_bench_inner_layout(heom_ctx *c, int32_t nbatch, int32_t reps, int32_t interleave, int32_t lane_instances,
+                            double *seconds, double *bytes)
+{
+    return guarded([&] {
+        require_ctx(c);
+        DeviceScope dsc(c->device);
+        if (reps < 1) reps = 1;
+        if (nbatch < 1) nbatch = 1;
+        if (interleave < 1) fail(HEOM_E_ARG, "heom_bench_inner_layout: interleave must be 1 or a power of two up to 32");
+        if (lane_instances == 2 && interleave < 2) fail(HEOM_E_ARG, "two instances per lane need interleave >= 2");
+        BenchInputs I;
+        bench_inputs(c, HEOM_PREC_MIXED, nbatch, I);
+        time_inner<DF>(c, I, nbatch, reps, seconds, bytes, interleave, lane_instances);
+    });
+}
+
+int heom_tuned_layout(heom_ctx *c, int32_t nbatch, int32_t truncated, int32_t *interleave, int32_t *lane_instances)
+{
+    return guarded([&] {
+        require_ctx(c);
+        if (!interleave || !lane_instances) fail(HEOM_E_ARG, "null argument");
+        *interleave = 0;
+        *lane_instances = 0;
+        const auto cand = layout_candidates(nbatch, truncated != 0);
+        if (cand.size() == 1) { *interleave = cand[0].first; *lane_instances = cand[0].second; return; }
+        auto it = c->il_tune.find({nbatch, truncated ? 1 : 0});
+        if (it != c->il_tune.end() && it->second.done()) std::tie(*interleave, *lane_instances) = it->second.best();
     });
 }
 

@@ -142,12 +142,22 @@ struct heom_ctx {
     // the tables are tier-major, so a hierarchy truncated at tier k is the prefix up to
     // tier_entry[k]
     std::vector<int64_t> tier_entry;
-    // automatic interleave of the mixed batch solves, per batch size: the device seconds of
-    // one solve without interleave ([0]) and with inner_default_interleave ([1])
-    struct InterleaveTune {
-        int tried = 0;
-        double seconds[2] = {0, 0};
+    // automatic layout of the FP32x2 inner kernels of the mixed batch solves, per batch size
+    // and kind (whole hierarchies 0, truncated 1): the candidate layouts (interleave,
+    // instances per lane) and the device seconds of one solve with each, timed on the
+    // context's first solves of that size and kind; then the fastest is kept
+    struct LayoutTune {
+        std::vector<std::pair<int, int>> cand;
+        std::vector<double> seconds;   // of the candidates timed so far, in order
+        bool done() const { return seconds.size() >= cand.size(); }
+        std::pair<int, int> best() const
+        {
+            size_t k = 0;
+            for (size_t i = 1; i < seconds.size(); i++)
+                if (seconds[i] < seconds[k]) k = i;
+            return cand[k];
+        }
     };
-    std::map<int, InterleaveTune> il_tune;
+    std::map<std::pair<int, int>, LayoutTune> il_tune;
     ~heom_ctx();
 };

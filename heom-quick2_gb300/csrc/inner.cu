@@ -70,12 +70,13 @@ __global__ void k_in_add_solution(double2 *__restrict__ x, InnerWork<T> W, int i
 // G > 1 only for FP32x2 (the mixed solves); FP64 and FP32 keep one instance per group
 template <typename T> constexpr bool kInterleaves = std::is_same<T, DF>::value;
 
-// W configured for every position of every group (GE = G; 0 for the plain layout)
+// W configured for every position of every group (GE = G / ipl_max; 0 for the plain layout)
 template <typename T>
 InnerWork<T> full_lanes(const InnerWork<T> &W)
 {
     InnerWork<T> F = W;
-    F.GE = W.G == 1 ? 0 : W.G;
+    F.ipl = W.ipl_max;
+    F.GE = W.G == 1 ? 0 : W.G / W.ipl_max;
     F.nblk = blocks_per_group(W.N, F.GE);
     return F;
 }
@@ -89,21 +90,27 @@ void inner_time(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int reps
     Q.order = nullptr;
     const DevCoef<T> K = inner_layout_coef<T>(W, P, C, s);
     InnerWork<T> F = full_lanes(W);
-    if (F.GE == 0) time_ge<T, 0, false>(F, Q, K, reps, s, ms_b, ms_a);
-    else if constexpr (kInterleaves<T>) df_time_full(F, Q, K, reps, s, ms_b, ms_a);
+    if (F.GE == 0) time_ge<T, 0, false, 1>(F, Q, K, reps, s, ms_b, ms_a);
+    else if constexpr (kInterleaves<T>) {
+        if (F.ipl == 2) df_time_pair(F, Q, K, reps, s, ms_b, ms_a);
+        else df_time_full(F, Q, K, reps, s, ms_b, ms_a);
+    }
     else fail(HEOM_E_ARG, "inner workspace: interleave of a non-FP32x2 type");
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) fail(HEOM_E_CUDA, std::string("fused inner kernels: ") + cudaGetErrorString(e));
 }
 
 template <typename T>
-void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s, int G)
+void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s, int G, int ipl)
 {
     using V = typename Num<T>::V;
     if (G < 0 || G > 32 || (G & (G - 1))) fail(HEOM_E_ARG, "interleave must be 0 or a power of two up to 32");
+    if (ipl != 1 && ipl != 2) fail(HEOM_E_ARG, "instances per lane must be 1 or 2");
     W.nbatch = nbatch;
     W.N = N;
     W.G = !kInterleaves<T> ? 1 : G > 0 ? G : inner_default_interleave(nbatch);
+    W.ipl_max = W.G > 1 ? ipl : 1;
+    W.ipl = 1;
     W.ngroups = (nbatch + W.G - 1) / W.G;
     W.vstride = (N + 63) / 64 * 64;
     W.gstride = W.vstride * W.G;
@@ -186,8 +193,11 @@ void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaSt
 {
     const InnerWork<T> F = full_lanes(W);
     dim3 g((unsigned)F.nblk, (unsigned)F.ngroups);
-    if (F.GE == 0) k_in_init<T, 0, false><<<g, NT, 0, s>>>(F);
-    else if constexpr (kInterleaves<T>) df_init_full(F, s);
+    if (F.GE == 0) k_in_init<T, 0, false, 1><<<g, NT, 0, s>>>(F);
+    else if constexpr (kInterleaves<T>) {
+        if (F.ipl == 2) df_init_pair(F, s);
+        else df_init_full(F, s);
+    }
     else fail(HEOM_E_ARG, "inner workspace: interleave of a non-FP32x2 type");
     k_in_init_fin<T><<<F.nbatch, NTF, 0, s>>>(F, crit, nlim, stag_window);
 }
@@ -195,7 +205,7 @@ void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaSt
 template <typename T>
 void inner_lanes(InnerWork<T> &W, const InnerState *st, std::vector<int> &amap_host, cudaStream_t s)
 {
-    if (W.G == 1) { W.GE = 0; W.nblk = blocks_per_group(W.N, 0); return; }
+    if (W.G == 1) { W.GE = 0; W.ipl = 1; W.nblk = blocks_per_group(W.N, 0); return; }
     int most = 0;
     amap_host.assign((size_t)W.ngroups * W.G, -1);
     for (int g = 0; g < W.ngroups; g++) {
@@ -206,8 +216,15 @@ void inner_lanes(InnerWork<T> &W, const InnerState *st, std::vector<int> &amap_h
         }
         most = std::max(most, n);
     }
+    if (W.ipl_max == 2 && 2 * most > W.G) {   // every position, two per lane
+        W.ipl = 2;
+        W.GE = W.G / 2;
+        W.nblk = blocks_per_group(W.N, W.GE);
+        return;
+    }
     int ge = 1;
     while (ge < most) ge *= 2;
+    W.ipl = 1;
     W.GE = ge;
     W.nblk = blocks_per_group(W.N, ge);
     if (ge < W.G && cudaMemcpyAsync(W.amap, amap_host.data(), sizeof(int) * amap_host.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
@@ -219,15 +236,16 @@ void inner_chunk(InnerWork<T> &W, const DevPlan &P, const DevCoef<T> &C, int ite
 {
     DevPlan Q = P;
     Q.order = nullptr;   // entry order: coalesced epilogue access
-    if (W.GE == 0) chunk_ge<T, 0, false>(W, Q, C, iters, s);
+    if (W.GE == 0) chunk_ge<T, 0, false, 1>(W, Q, C, iters, s);
     else if constexpr (kInterleaves<T>) {
-        if (W.GE == W.G) df_chunk_full(W, Q, C, iters, s);
+        if (W.ipl == 2) df_chunk_pair(W, Q, C, iters, s);
+        else if (W.GE == W.G) df_chunk_full(W, Q, C, iters, s);
         else df_chunk_compact(W, Q, C, iters, s);
     } else fail(HEOM_E_ARG, "inner workspace: interleave of a non-FP32x2 type");
 }
 
 #define INST(T)                                                                              \
-    template void inner_alloc<T>(InnerWork<T> &, int, int64_t, cudaStream_t, int);           \
+    template void inner_alloc<T>(InnerWork<T> &, int, int64_t, cudaStream_t, int, int);      \
     template void inner_free<T>(InnerWork<T> &);                                              \
     template DevCoef<T> inner_layout_coef<T>(InnerWork<T> &, const DevPlan &, const DevCoef<T> &, cudaStream_t); \
     template void inner_rhs<T>(InnerWork<T> &, const DevPlan &, const double2 *, int, double, const float *, cudaStream_t); \

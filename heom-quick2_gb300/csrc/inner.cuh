@@ -62,6 +62,10 @@ struct InnerWork {
     // running instances of a group share fewer lanes and blocks (inner_lanes)
     int GE = 0;
     int *amap = nullptr;
+    // instances per lane: ipl_max = 2 lets a lane serve two adjacent positions of its group
+    // (GE = G / 2 lanes per entry; the plan is decoded once for both) while more than half of
+    // a group's instances run; ipl is the current configuration's
+    int ipl_max = 1, ipl = 1;
     int64_t N = 0;              // complex elements per instance (lunk + 1)
     int64_t vstride = 0;        // N rounded up to a multiple of 64
     int64_t gstride = 0;        // complex elements between groups (vstride G)
@@ -84,8 +88,8 @@ struct InnerWork {
 };
 
 // G: instances per entry group (a power of two <= 32; 0 = inner_default_interleave; FP64
-// and FP32 workspaces always use 1)
-template <typename T> void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s, int G = 0);
+// and FP32 workspaces always use 1); ipl: instances per lane (1, or 2 for FP32x2 with G > 1)
+template <typename T> void inner_alloc(InnerWork<T> &W, int nbatch, int64_t N, cudaStream_t s, int G = 0, int ipl = 1);
 // the smallest power of two >= nbatch, at most 32
 inline int inner_default_interleave(int nbatch)
 {
@@ -119,10 +123,11 @@ void inner_add_solution(InnerWork<T> &W, double2 *x, int inst, double a, int slo
 // stag_window checks that fail to halve the best residual); or once nlim iterations ran.
 template <typename T>
 void inner_start(InnerWork<T> &W, double crit, int nlim, int stag_window, cudaStream_t s);
-// Configure W for the next chunk from the instances' states (host copy): GE = the smallest
-// power of two >= the most running instances of any group, and their positions in the lane
-// map (copied with cudaMemcpyAsync from amap_host, which must stay unchanged until the
-// stream has passed the copy).
+// Configure W for the next chunk from the instances' states (host copy): with two instances
+// per lane allowed and more than half of some group's instances running, every position on
+// G / 2 lanes of two instances; else GE = the smallest power of two >= the most running
+// instances of any group, and their positions in the lane map (copied with cudaMemcpyAsync
+// from amap_host, which must stay unchanged until the stream has passed the copy).
 template <typename T>
 void inner_lanes(InnerWork<T> &W, const InnerState *st, std::vector<int> &amap_host, cudaStream_t s);
 // Enqueue `iters` iterations and one check in W's current configuration (capturable in a

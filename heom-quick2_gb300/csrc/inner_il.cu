@@ -18,17 +18,17 @@ namespace inner_detail {
 void df_init_full(const InnerWork<DF> &F, cudaStream_t s)
 {
     dim3 g((unsigned)F.nblk, (unsigned)F.ngroups);
-    HEOM_FULL_G((k_in_init<DF, G, false><<<g, NT, 0, s>>>(F)))
+    HEOM_FULL_G((k_in_init<DF, G, false, 1><<<g, NT, 0, s>>>(F)))
 }
 
 void df_chunk_full(InnerWork<DF> &F, const DevPlan &Q, const DevCoef<DF> &C, int iters, cudaStream_t s)
 {
-    HEOM_FULL_G((chunk_ge<DF, G, false>(F, Q, C, iters, s)))
+    HEOM_FULL_G((chunk_ge<DF, G, false, 1>(F, Q, C, iters, s)))
 }
 
 void df_time_full(InnerWork<DF> &F, const DevPlan &Q, const DevCoef<DF> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a)
 {
-    HEOM_FULL_G((time_ge<DF, G, false>(F, Q, C, reps, s, ms_b, ms_a)))
+    HEOM_FULL_G((time_ge<DF, G, false, 1>(F, Q, C, reps, s, ms_b, ms_a)))
 }
 
 #undef HEOM_FULL_G

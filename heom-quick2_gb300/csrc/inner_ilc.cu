@@ -8,11 +8,11 @@ namespace inner_detail {
 void df_chunk_compact(InnerWork<DF> &W, const DevPlan &Q, const DevCoef<DF> &C, int iters, cudaStream_t s)
 {
     switch (W.GE) {
-    case 1: chunk_ge<DF, 1, true>(W, Q, C, iters, s); break;
-    case 2: chunk_ge<DF, 2, true>(W, Q, C, iters, s); break;
-    case 4: chunk_ge<DF, 4, true>(W, Q, C, iters, s); break;
-    case 8: chunk_ge<DF, 8, true>(W, Q, C, iters, s); break;
-    case 16: chunk_ge<DF, 16, true>(W, Q, C, iters, s); break;
+    case 1: chunk_ge<DF, 1, true, 1>(W, Q, C, iters, s); break;
+    case 2: chunk_ge<DF, 2, true, 1>(W, Q, C, iters, s); break;
+    case 4: chunk_ge<DF, 4, true, 1>(W, Q, C, iters, s); break;
+    case 8: chunk_ge<DF, 8, true, 1>(W, Q, C, iters, s); break;
+    case 16: chunk_ge<DF, 16, true, 1>(W, Q, C, iters, s); break;
     default: fail(HEOM_E_ARG, "inner workspace: unsupported lanes per entry");
     }
 }

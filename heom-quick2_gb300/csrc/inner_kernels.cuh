@@ -3,7 +3,8 @@
 // (FP32x2, every position of a group served, stride known at compile time) and
 // inner_ilc.cu (FP32x2, a group's running instances compacted onto fewer lanes, stride read
 // at run time).  Template parameters of the kernels: GE lanes per entry (0: one instance
-// per group) and CMP (lanes map to positions through the lane map).
+// per group), CMP (lanes map to positions through the lane map) and IPL instances per lane
+// (2: a lane serves two adjacent positions of its group and decodes the plan once for both).
 #pragma once
 #include <cmath>
 #include <functional>
@@ -110,10 +111,11 @@ __device__ __forceinline__ void grand_totals(const double *part, int nblk, int b
 }
 
 // Lane geometry of the fused kernels.  GE lanes serve one entry (GE = 0: the plain layout,
-// one instance per group, stride 1 known at compile time).  Slot j < GE of group blockIdx.y
-// serves the instance at position p of the group: p = j when every position is served
-// (GE == G), else p = amap[G blockIdx.y + j] (-1: no instance), so that a group whose
-// instances have partly finished runs on fewer lanes and fewer blocks.  The instance is
+// one instance per group, stride 1 known at compile time), each lane IPL instances.  Slot
+// j < GE IPL of group blockIdx.y serves the instance at position p of the group: p = j when
+// every position is served (GE IPL == G), else p = amap[G blockIdx.y + j] (-1: no
+// instance), so that a group whose instances have partly finished runs on fewer lanes and
+// fewer blocks.  Lane l serves slots l IPL .. l IPL + IPL - 1.  The instance is
 // b = G blockIdx.y + p, and its entry t sits at o + t stride.
 template <int GE> constexpr int lanes_of() { return GE == 0 ? 1 : GE; }
 
@@ -125,77 +127,95 @@ __device__ __forceinline__ int slot_pos(const InnerWork<T> &W, int j)
     else return __ldg(&W.amap[(int)blockIdx.y * W.G + j]);
 }
 
+template <int IPL>
 struct Lane {
-    int b;          // instance
-    bool on;        // the slot serves an instance
-    int64_t t, o;   // entry; base of the instance's vectors
+    int b[IPL];         // instances
+    bool on[IPL];       // the slot serves an instance
+    int64_t t;          // entry
+    int64_t o[IPL];     // base of the instances' vectors
 };
-template <typename T, int GE, bool CMP>
-__device__ __forceinline__ Lane lane_of(const InnerWork<T> &W)
+template <typename T, int GE, bool CMP, int IPL>
+__device__ __forceinline__ Lane<IPL> lane_of(const InnerWork<T> &W)
 {
+    static_assert(IPL == 1 || (GE > 0 && !CMP), "two instances per lane: every position of the group served");
     constexpr int NL = lanes_of<GE>();
-    Lane L;
-    const int p = slot_pos<T, GE, CMP>(W, (int)(threadIdx.x & (NL - 1)));
-    L.b = (int)blockIdx.y * W.G + p;
-    L.on = p >= 0 && L.b < W.nbatch;
+    Lane<IPL> L;
+    const int l = (int)(threadIdx.x & (NL - 1));
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        const int p = slot_pos<T, GE, CMP>(W, l * IPL + i);
+        L.b[i] = (int)blockIdx.y * W.G + p;
+        L.on[i] = p >= 0 && L.b[i] < W.nbatch;
+        L.o[i] = (int64_t)blockIdx.y * W.gstride + (p < 0 ? 0 : p);
+    }
     L.t = (int64_t)blockIdx.x * (NT / NL) + threadIdx.x / NL;
-    L.o = (int64_t)blockIdx.y * W.gstride + (p < 0 ? 0 : p);
     return L;
 }
-template <typename T, int GE, bool CMP>
-__device__ __forceinline__ int64_t stride_of(const InnerWork<T> &W) { return GE == 0 ? 1 : CMP ? W.G : GE; }
+template <typename T, int GE, bool CMP, int IPL>
+__device__ __forceinline__ int64_t stride_of(const InnerWork<T> &W) { return GE == 0 ? 1 : CMP ? W.G : GE * IPL; }
 
-// the apply of instance L.b's entry L.t on vector x (the instance's element stride)
-template <typename T, bool REG, bool CF, int GE, bool CMP>
-__device__ __forceinline__ typename Num<T>::A apply_lane(const DevPlan &P, const DevCoef<T> &C, const InnerWork<T> &W,
-                                                       const typename Num<T>::V *x, const Lane &L)
+// the applies of the lane's instances to their entry L.t, instance i on the vector at x[i]
+// (an instance's element stride); with two instances per lane, one whose slot serves no
+// instance is computed on the group's zero padding and not used
+template <typename T, bool REG, bool CF, int GE, bool CMP, int IPL>
+__device__ __forceinline__ void apply_lane(const DevPlan &P, const DevCoef<T> &C, const InnerWork<T> &W,
+                                           const typename Num<T>::V *const (&x)[IPL], const Lane<IPL> &L,
+                                           typename Num<T>::A (&y)[IPL])
 {
-    return apply_entry<T, false, REG, CF, GE == 0 ? 1 : CMP ? 0 : GE>(P, C, x + L.o, L.t, L.b, W.G);
+    const typename Num<T>::V *xv[IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++) xv[i] = x[i] + L.o[i];
+    apply_entries<T, false, REG, CF, GE == 0 ? 1 : CMP ? 0 : GE * IPL, IPL>(P, C, xv, L.t, L.b, y, W.G);
 }
 
 // K warp sums per slot -> one FP64 partial per block and instance, written to
 // part[(3 b + k) nblk + block] for the instances the slots serve.  Warps 1..7 leave their
 // sums in shared memory, arrive at named barrier 1 and retire at once; warp 0 waits there
-// (bar.sync), then its lanes 0 .. GE-1 add the eight sums of their slot in warp order
-// (deterministic).  Every thread of the block must reach this call.
+// (bar.sync), then its lanes 0 .. GE-1 add the eight sums of each of their slots in warp
+// order (deterministic).  Every thread of the block must reach this call.
 constexpr int kWarps = NT / 32;
-template <typename T, int K, int GE, bool CMP>
-__device__ __forceinline__ void block_partials(const typename WarpAcc<T>::R (&ws)[K], const InnerWork<T> &W)
+template <typename T, int K, int GE, bool CMP, int IPL>
+__device__ __forceinline__ void block_partials(const typename WarpAcc<T>::R (&ws)[K][IPL], const InnerWork<T> &W)
 {
     using R = typename WarpAcc<T>::R;
     constexpr int NL = lanes_of<GE>();
-    __shared__ R sh[K][kWarps][NL];
+    __shared__ R sh[K][IPL][kWarps][NL];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (wid != 0) {
         if (lane < NL)
 #pragma unroll
-            for (int k = 0; k < K; k++) sh[k][wid][lane] = ws[k];
+            for (int k = 0; k < K; k++)
+#pragma unroll
+                for (int i = 0; i < IPL; i++) sh[k][i][wid][lane] = ws[k][i];
         asm volatile("bar.arrive 1, %0;" ::"r"(NT) : "memory");
         return;
     }
     asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
     if (lane >= NL) return;
-    const int p = slot_pos<T, GE, CMP>(W, lane), b = (int)blockIdx.y * W.G + p;
-    if (p < 0 || b >= W.nbatch) return;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        R s = ws[k];
-        for (int w = 1; w < kWarps; w++) s = WarpAcc<T>::add(s, sh[k][w][lane]);
-        W.part[(3 * (size_t)b + k) * W.nblk + blockIdx.x] = WarpAcc<T>::to_double(s);
+    for (int i = 0; i < IPL; i++) {
+        const int p = slot_pos<T, GE, CMP>(W, lane * IPL + i), b = (int)blockIdx.y * W.G + p;
+        if (p < 0 || b >= W.nbatch) continue;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            R s = ws[k][i];
+            for (int w = 1; w < kWarps; w++) s = WarpAcc<T>::add(s, sh[k][i][w][lane]);
+            W.part[(3 * (size_t)b + k) * W.nblk + blockIdx.x] = WarpAcc<T>::to_double(s);
+        }
     }
 }
 
-// Whether the block has work for the lane's instance: the slot serves one, it runs (`run`),
-// and, in a truncated batch (tier_lim), the block's entries are not all beyond its tier (a
-// block that holds the trace slot always has work).
-template <typename T, int GE, bool CMP>
-__device__ __forceinline__ bool block_work(const InnerWork<T> &W, const Lane &L, bool run)
+// Whether the block has work for the lane's i-th instance: the slot serves one, it runs
+// (`run`), and, in a truncated batch (tier_lim), the block's entries are not all beyond its
+// tier (a block that holds the trace slot always has work).
+template <typename T, int GE, bool CMP, int IPL>
+__device__ __forceinline__ bool block_work(const InnerWork<T> &W, const Lane<IPL> &L, int i, bool run)
 {
     constexpr int NL = lanes_of<GE>();
-    if (!L.on || !run) return false;
+    if (!L.on[i] || !run) return false;
     if (!W.tier_lim) return true;
     const int64_t first = (int64_t)blockIdx.x * (NT / NL), last = first + NT / NL - 1;
-    return first < (int64_t)__ldg(&W.tier_lim[L.b].y) || last >= W.N - 1;
+    return first < (int64_t)__ldg(&W.tier_lim[L.b[i]].y) || last >= W.N - 1;
 }
 
 // Programmatic dependent launch: `k_in_b` and `k_in_a` are launched while the preceding
@@ -210,18 +230,19 @@ __device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontro
 
 // Entry of the fused kernels with K partials: false (after writing the K partials of this
 // block as zero for the instances its slots serve) when no lane of the block has work; the
-// decision is uniform over the block.  `work`: this lane's block_work.
-template <typename T, int K, int GE, bool CMP>
+// decision is uniform over the block.  `work`: whether this lane has work for any of its
+// instances.
+template <typename T, int K, int GE, bool CMP, int IPL>
 __device__ __forceinline__ bool block_enter(const InnerWork<T> &W, bool work)
 {
-    constexpr int NL = lanes_of<GE>();
+    constexpr int NS = lanes_of<GE>() * IPL;   // slots of a block
     bool any;
     if constexpr (GE == 0) any = work;   // one instance per block
     else any = __syncthreads_or(work) != 0;
     if (any) return true;
     wait_prior_grid();
-    if (threadIdx.x < K * NL) {
-        const int p = slot_pos<T, GE, CMP>(W, (int)(threadIdx.x % NL)), k = (int)(threadIdx.x / NL);
+    if (threadIdx.x < K * NS) {
+        const int p = slot_pos<T, GE, CMP>(W, (int)(threadIdx.x % NS)), k = (int)(threadIdx.x / NS);
         const int b = (int)blockIdx.y * W.G + p;
         if (p >= 0 && b < W.nbatch) W.part[(3 * (size_t)b + k) * W.nblk + blockIdx.x] = 0.0;
     }
@@ -229,25 +250,32 @@ __device__ __forceinline__ bool block_enter(const InnerWork<T> &W, bool work)
 }
 
 // w = b, other vectors 0; partials ||b||^2, <r~, b>
-template <typename T, int GE, bool CMP>
+template <typename T, int GE, bool CMP, int IPL>
 __global__ void k_in_init(InnerWork<T> W)
 {
     using N = Num<T>;
     using A = typename N::A;
     constexpr int NL = lanes_of<GE>();
-    const Lane L = lane_of<T, GE, CMP>(W);
-    WarpAcc<T> bb, rb;
-    if (L.on && L.t < W.N) {
-        const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-        const A bv = N::load(W.b[e]);
-        const typename N::V z = N::store(N::zero());
-        W.w[e] = N::store(bv);
-        W.x[e] = z; W.xs[e] = z; W.xs2[e] = z; W.y[e] = z; W.d[e] = z; W.v[e] = z; W.u2[e] = z;
-        bb.add(bv, bv);
-        rb.add(N::load(W.rt[shadow_index(W.tier_lim, L.b, L.t, W.N)]), bv);
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
+    WarpAcc<T> bb[IPL], rb[IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++)
+        if (L.on[i] && L.t < W.N) {
+            const int64_t e = L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W);
+            const A bv = N::load(W.b[e]);
+            const typename N::V z = N::store(N::zero());
+            W.w[e] = N::store(bv);
+            W.x[e] = z; W.xs[e] = z; W.xs2[e] = z; W.y[e] = z; W.d[e] = z; W.v[e] = z; W.u2[e] = z;
+            bb[i].add(bv, bv);
+            rb[i].add(N::load(W.rt[shadow_index(W.tier_lim, L.b[i], L.t, W.N)]), bv);
+        }
+    typename WarpAcc<T>::R ws[2][IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        ws[0][i] = bb[i].template warp_sum<NL>();
+        ws[1][i] = rb[i].template warp_sum<NL>();
     }
-    const typename WarpAcc<T>::R ws[2] = {bb.template warp_sum<NL>(), rb.template warp_sum<NL>()};
-    block_partials<T, 2, GE, CMP>(ws, W);
+    block_partials<T, 2, GE, CMP, IPL>(ws, W);
 }
 
 template <typename T>
@@ -272,39 +300,60 @@ __global__ void __launch_bounds__(NTF) k_in_init_fin(InnerWork<T> W, double crit
     W.cf[b] = k;
 }
 
+// Resident blocks per SM of the apply kernels: six (at most 40 registers) with one instance
+// per lane; five (48 registers, 8-24 bytes of spills) with two, whose accumulators double.
+// Measured on the double dot at tier 4, batch 8, two instances per lane in groups of two
+// (k_in_b + k_in_a): 437 us at four blocks (64 registers, no spills: the warps could not
+// hide the gathers' latency), 403 us at five.
+template <int IPL> constexpr int apply_blocks_per_sm() { return IPL == 1 ? 6 : 5; }
+
 // B: u1 = A w + beta u2, the pending x / d updates, y = w + beta y2, v = u1 + beta (u2 + beta v)
-template <typename T, bool REG, bool CF, int GE, bool CMP>
-__global__ void __launch_bounds__(NT, 6) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+template <typename T, bool REG, bool CF, int GE, bool CMP, int IPL>
+__global__ void __launch_bounds__(NT, apply_blocks_per_sm<IPL>()) k_in_b(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     using N = Num<T>;
     using A = typename N::A;
     constexpr int NL = lanes_of<GE>();
-    const Lane L = lane_of<T, GE, CMP>(W);
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
     // an instance finished before the preceding finaliser stays finished within the round
-    const bool work = block_work<T, GE, CMP>(W, L, L.on && !W.st[L.b].done);
-    if (!block_enter<T, 1, GE, CMP>(W, work)) return;
-    WarpAcc<T> sg;
-    A aw = N::zero();
-    if (work && L.t < W.N) aw = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.w, L);
-    wait_prior_grid();
-    if (work && L.t < W.N && !W.st[L.b].done) {
-        const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-        const InnerCoef<T> &k = W.cf[L.b];
-        const A u2 = N::load(W.u2[e]), vo = N::load(W.v[e]), yo = N::load(W.y[e]);
-        const A u1 = N::add(aw, N::scale(u2, k.beta));
-        W.u1[e] = N::store(u1);
-        const A d1 = N::add(yo, N::scale(N::load(W.d[e]), k.dd1));
-        const A y2 = N::sub(yo, N::scale(vo, k.alpha_prev));
-        const A d2 = N::add(y2, N::scale(d1, k.dd2));
-        W.d[e] = N::store(d2);
-        W.x[e] = N::store(N::add(N::load(W.x[e]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
-        W.y[e] = N::store(N::add(N::load(W.w[e]), N::scale(y2, k.beta)));
-        const A vn = N::add(u1, N::scale(N::add(u2, N::scale(vo, k.beta)), k.beta));
-        W.v[e] = N::store(vn);
-        sg.add(N::load(W.rt[shadow_index(W.tier_lim, L.b, L.t, W.N)]), vn);
+    bool work[IPL], any = false;
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        work[i] = block_work<T, GE, CMP, IPL>(W, L, i, L.on[i] && !W.st[L.b[i]].done);
+        any = any || work[i];
     }
-    const typename WarpAcc<T>::R ws[1] = {sg.template warp_sum<NL>()};
-    block_partials<T, 1, GE, CMP>(ws, W);
+    if (!block_enter<T, 1, GE, CMP, IPL>(W, any)) return;
+    WarpAcc<T> sg[IPL];
+    A aw[IPL];
+    if (any && L.t < W.N) {
+        const typename N::V *xv[IPL];
+#pragma unroll
+        for (int i = 0; i < IPL; i++) xv[i] = W.w;
+        apply_lane<T, REG, CF, GE, CMP, IPL>(P, C, W, xv, L, aw);
+    }
+    wait_prior_grid();
+#pragma unroll
+    for (int i = 0; i < IPL; i++)
+        if (work[i] && L.t < W.N && !W.st[L.b[i]].done) {
+            const int64_t e = L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W);
+            const InnerCoef<T> &k = W.cf[L.b[i]];
+            const A u2 = N::load(W.u2[e]), vo = N::load(W.v[e]), yo = N::load(W.y[e]);
+            const A u1 = N::add(aw[i], N::scale(u2, k.beta));
+            W.u1[e] = N::store(u1);
+            const A d1 = N::add(yo, N::scale(N::load(W.d[e]), k.dd1));
+            const A y2 = N::sub(yo, N::scale(vo, k.alpha_prev));
+            const A d2 = N::add(y2, N::scale(d1, k.dd2));
+            W.d[e] = N::store(d2);
+            W.x[e] = N::store(N::add(N::load(W.x[e]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+            W.y[e] = N::store(N::add(N::load(W.w[e]), N::scale(y2, k.beta)));
+            const A vn = N::add(u1, N::scale(N::add(u2, N::scale(vo, k.beta)), k.beta));
+            W.v[e] = N::store(vn);
+            sg[i].add(N::load(W.rt[shadow_index(W.tier_lim, L.b[i], L.t, W.N)]), vn);
+        }
+    typename WarpAcc<T>::R ws[1][IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++) ws[0][i] = sg[i].template warp_sum<NL>();
+    block_partials<T, 1, GE, CMP, IPL>(ws, W);
 }
 
 template <typename T>
@@ -327,35 +376,53 @@ __global__ void __launch_bounds__(NTF) k_in_b_fin(InnerWork<T> W)
 }
 
 // A: u2 = u1 - alpha A v, w1 = w - alpha u1, w = w1 - alpha u2
-template <typename T, bool REG, bool CF, int GE, bool CMP>
-__global__ void __launch_bounds__(NT, 6) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+template <typename T, bool REG, bool CF, int GE, bool CMP, int IPL>
+__global__ void __launch_bounds__(NT, apply_blocks_per_sm<IPL>()) k_in_a(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     using N = Num<T>;
     using A = typename N::A;
     constexpr int NL = lanes_of<GE>();
-    const Lane L = lane_of<T, GE, CMP>(W);
-    const bool work = block_work<T, GE, CMP>(W, L, L.on && !W.st[L.b].done);
-    if (!block_enter<T, 3, GE, CMP>(W, work)) return;
-    WarpAcc<T> a1, a2, a3;
-    A av = N::zero();
-    if (work && L.t < W.N) av = apply_lane<T, REG, CF, GE, CMP>(P, C, W, W.v, L);
-    wait_prior_grid();
-    if (work && L.t < W.N && !W.st[L.b].done) {
-        const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-        const typename N::S al = W.cf[L.b].alpha;
-        const A u1 = N::load(W.u1[e]);
-        const A u2 = N::sub(u1, N::scale(av, al));
-        W.u2[e] = N::store(u2);
-        // normalised before the squared norms (the lazy differences cancel near convergence)
-        const A w1 = N::norm(N::sub(N::load(W.w[e]), N::scale(u1, al)));
-        const A w2 = N::norm(N::sub(w1, N::scale(u2, al)));
-        W.w[e] = N::pack(w2);
-        a1.add(w1, w1);
-        a2.add(w2, w2);
-        a3.add(N::load(W.rt[shadow_index(W.tier_lim, L.b, L.t, W.N)]), w2);
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
+    bool work[IPL], any = false;
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        work[i] = block_work<T, GE, CMP, IPL>(W, L, i, L.on[i] && !W.st[L.b[i]].done);
+        any = any || work[i];
     }
-    const typename WarpAcc<T>::R ws[3] = {a1.template warp_sum<NL>(), a2.template warp_sum<NL>(), a3.template warp_sum<NL>()};
-    block_partials<T, 3, GE, CMP>(ws, W);
+    if (!block_enter<T, 3, GE, CMP, IPL>(W, any)) return;
+    WarpAcc<T> a1[IPL], a2[IPL], a3[IPL];
+    A av[IPL];
+    if (any && L.t < W.N) {
+        const typename N::V *xv[IPL];
+#pragma unroll
+        for (int i = 0; i < IPL; i++) xv[i] = W.v;
+        apply_lane<T, REG, CF, GE, CMP, IPL>(P, C, W, xv, L, av);
+    }
+    wait_prior_grid();
+#pragma unroll
+    for (int i = 0; i < IPL; i++)
+        if (work[i] && L.t < W.N && !W.st[L.b[i]].done) {
+            const int64_t e = L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W);
+            const typename N::S al = W.cf[L.b[i]].alpha;
+            const A u1 = N::load(W.u1[e]);
+            const A u2 = N::sub(u1, N::scale(av[i], al));
+            W.u2[e] = N::store(u2);
+            // normalised before the squared norms (the lazy differences cancel near convergence)
+            const A w1 = N::norm(N::sub(N::load(W.w[e]), N::scale(u1, al)));
+            const A w2 = N::norm(N::sub(w1, N::scale(u2, al)));
+            W.w[e] = N::pack(w2);
+            a1[i].add(w1, w1);
+            a2[i].add(w2, w2);
+            a3[i].add(N::load(W.rt[shadow_index(W.tier_lim, L.b[i], L.t, W.N)]), w2);
+        }
+    typename WarpAcc<T>::R ws[3][IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        ws[0][i] = a1[i].template warp_sum<NL>();
+        ws[1][i] = a2[i].template warp_sum<NL>();
+        ws[2][i] = a3[i].template warp_sum<NL>();
+    }
+    block_partials<T, 3, GE, CMP, IPL>(ws, W);
 }
 
 template <typename T>
@@ -402,43 +469,62 @@ __global__ void __launch_bounds__(NTF) k_in_a_fin(InnerWork<T> W)
 
 // xs = x + the pending updates of the last iteration (into the slot that does not hold the
 // best checked iterate)
-template <typename T, int GE, bool CMP>
+template <typename T, int GE, bool CMP, int IPL>
 __global__ void k_in_x(InnerWork<T> W)
 {
     using N = Num<T>;
     using A = typename N::A;
-    const Lane L = lane_of<T, GE, CMP>(W);
-    if (!L.on || L.t >= W.N) return;
-    const InnerState &st = W.st[L.b];
-    if (st.done && !st.finishing) return;
-    const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-    const InnerCoef<T> &k = W.cf[L.b];
-    typename N::V *xo = W.slot(1 - st.best_slot);
-    const A yo = N::load(W.y[e]);
-    const A d1 = N::add(yo, N::scale(N::load(W.d[e]), k.dd1));
-    const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[e]), k.alpha_prev)), N::scale(d1, k.dd2));
-    xo[e] = N::store(N::add(N::load(W.x[e]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
+    if (L.t >= W.N) return;
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        if (!L.on[i]) continue;
+        const InnerState &st = W.st[L.b[i]];
+        if (st.done && !st.finishing) continue;
+        const int64_t e = L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W);
+        const InnerCoef<T> &k = W.cf[L.b[i]];
+        typename N::V *xo = W.slot(1 - st.best_slot);
+        const A yo = N::load(W.y[e]);
+        const A d1 = N::add(yo, N::scale(N::load(W.d[e]), k.dd1));
+        const A d2 = N::add(N::sub(yo, N::scale(N::load(W.v[e]), k.alpha_prev)), N::scale(d1, k.dd2));
+        xo[e] = N::store(N::add(N::load(W.x[e]), N::add(N::scale(d1, k.eta1), N::scale(d2, k.eta2))));
+    }
 }
 
 // partial ||b - A xs||^2
-template <typename T, bool REG, bool CF, int GE, bool CMP>
-__global__ void __launch_bounds__(NT, 6) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
+template <typename T, bool REG, bool CF, int GE, bool CMP, int IPL>
+__global__ void __launch_bounds__(NT, apply_blocks_per_sm<IPL>()) k_in_chk(DevPlan P, DevCoef<T> C, InnerWork<T> W)
 {
     using N = Num<T>;
     using A = typename N::A;
     constexpr int NL = lanes_of<GE>();
-    const Lane L = lane_of<T, GE, CMP>(W);
-    const bool run = L.on && (!W.st[L.b].done || W.st[L.b].finishing);
-    const bool work = block_work<T, GE, CMP>(W, L, run);
-    if (!block_enter<T, 1, GE, CMP>(W, work)) return;
-    WarpAcc<T> ee;
-    if (work && L.t < W.N) {
-        const typename N::V *xc = W.slot(1 - W.st[L.b].best_slot);
-        const A r = N::norm(N::sub(N::load(W.b[L.o + L.t * stride_of<T, GE, CMP>(W)]), apply_lane<T, REG, CF, GE, CMP>(P, C, W, xc, L)));
-        ee.add(r, r);
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
+    bool work[IPL], any = false;
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        const bool run = L.on[i] && (!W.st[L.b[i]].done || W.st[L.b[i]].finishing);
+        work[i] = block_work<T, GE, CMP, IPL>(W, L, i, run);
+        any = any || work[i];
     }
-    const typename WarpAcc<T>::R ws[1] = {ee.template warp_sum<NL>()};
-    block_partials<T, 1, GE, CMP>(ws, W);
+    if (!block_enter<T, 1, GE, CMP, IPL>(W, any)) return;
+    WarpAcc<T> ee[IPL];
+    if (any && L.t < W.N) {
+        const typename N::V *xc[IPL];
+#pragma unroll
+        for (int i = 0; i < IPL; i++) xc[i] = W.slot(L.on[i] ? 1 - W.st[L.b[i]].best_slot : 0);
+        A ax[IPL];
+        apply_lane<T, REG, CF, GE, CMP, IPL>(P, C, W, xc, L, ax);
+#pragma unroll
+        for (int i = 0; i < IPL; i++)
+            if (work[i]) {
+                const A r = N::norm(N::sub(N::load(W.b[L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W)]), ax[i]));
+                ee[i].add(r, r);
+            }
+    }
+    typename WarpAcc<T>::R ws[1][IPL];
+#pragma unroll
+    for (int i = 0; i < IPL; i++) ws[0][i] = ee[i].template warp_sum<NL>();
+    block_partials<T, 1, GE, CMP, IPL>(ws, W);
 }
 
 template <typename T>
@@ -477,28 +563,34 @@ __global__ void __launch_bounds__(NTF) k_in_chk_fin(InnerWork<T> W)
 
 
 // measurement pattern: every vector = (1 + k/8) r~, finite scalars, no instance done
-template <typename T, int GE, bool CMP>
+template <typename T, int GE, bool CMP, int IPL>
 __global__ void k_in_fill(InnerWork<T> W)
 {
     using N = Num<T>;
-    const Lane L = lane_of<T, GE, CMP>(W);
-    if (!L.on || L.t >= W.N) return;
-    const int64_t e = L.o + L.t * stride_of<T, GE, CMP>(W);
-    const typename N::V r = W.rt[L.t];
-    typename N::V *vec[10] = {W.x, W.xs, W.b, W.w, W.y, W.d, W.v, W.u1, W.u2, W.xs2};
-    for (int k = 0; k < 10; k++) vec[k][e] = N::store(N::scale(N::load(r), N::sc(1.0 + 0.125 * k)));
-    if (L.t == 0) {
-        InnerState st = {};
-        st.r0 = 1; st.tau = 1; st.rho = 1; st.nlim = 1 << 30;
-        W.st[L.b] = st;
-        InnerCoef<T> k;
-        k.beta = k.alpha = k.alpha_prev = k.dd1 = k.eta1 = k.dd2 = k.eta2 = N::sc(0.5);
-        W.cf[L.b] = k;
+    const Lane<IPL> L = lane_of<T, GE, CMP, IPL>(W);
+    if (L.t >= W.N) return;
+#pragma unroll
+    for (int i = 0; i < IPL; i++) {
+        if (!L.on[i]) continue;
+        const int64_t e = L.o[i] + L.t * stride_of<T, GE, CMP, IPL>(W);
+        const typename N::V r = W.rt[L.t];
+        typename N::V *vec[10] = {W.x, W.xs, W.b, W.w, W.y, W.d, W.v, W.u1, W.u2, W.xs2};
+        for (int k = 0; k < 10; k++) vec[k][e] = N::store(N::scale(N::load(r), N::sc(1.0 + 0.125 * k)));
+        if (L.t == 0) {
+            InnerState st = {};
+            st.r0 = 1; st.tau = 1; st.rho = 1; st.nlim = 1 << 30;
+            W.st[L.b[i]] = st;
+            InnerCoef<T> k;
+            k.beta = k.alpha = k.alpha_prev = k.dd1 = k.eta1 = k.dd2 = k.eta2 = N::sc(0.5);
+            W.cf[L.b[i]] = k;
+        }
     }
 }
 
-// The launches of one chunk (`iters` iterations and a check) in configuration (GE, CMP).
-template <typename T, int GE, bool CMP>
+// The launches of one chunk (`iters` iterations and a check) in configuration (GE, CMP,
+// IPL).  Two instances per lane serve the steady operators only (no correlation-function
+// variant).
+template <typename T, int GE, bool CMP, int IPL>
 void chunk_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int iters, cudaStream_t s)
 {
     dim3 g((unsigned)W.nblk, (unsigned)W.ngroups);
@@ -517,37 +609,56 @@ void chunk_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int iters,
         cfg.numAttrs = 1;
         if (cudaLaunchKernelEx(&cfg, kernel, Q, C, W) != cudaSuccess) fail(HEOM_E_CUDA, "launch of a fused inner kernel failed");
     };
+    if (IPL > 1 && (C.cf_half || C.tier_lim)) fail(HEOM_E_ARG, "two instances per lane: steady operators of whole hierarchies only");
     for (int i = 0; i < iters; i++) {
-        if (C.cf_half) dependent(k_in_b<T, false, true, GE, CMP>);
-        else if (C.reg) dependent(k_in_b<T, true, false, GE, CMP>);
-        else dependent(k_in_b<T, false, false, GE, CMP>);
+        if constexpr (IPL == 1) {
+            if (C.cf_half) dependent(k_in_b<T, false, true, GE, CMP, IPL>);
+            else if (C.reg) dependent(k_in_b<T, true, false, GE, CMP, IPL>);
+            else dependent(k_in_b<T, false, false, GE, CMP, IPL>);
+        } else {
+            if (C.reg) dependent(k_in_b<T, true, false, GE, CMP, IPL>);
+            else dependent(k_in_b<T, false, false, GE, CMP, IPL>);
+        }
         k_in_b_fin<T><<<nb, NTF, 0, s>>>(W);
-        if (C.cf_half) dependent(k_in_a<T, false, true, GE, CMP>);
-        else if (C.reg) dependent(k_in_a<T, true, false, GE, CMP>);
-        else dependent(k_in_a<T, false, false, GE, CMP>);
+        if constexpr (IPL == 1) {
+            if (C.cf_half) dependent(k_in_a<T, false, true, GE, CMP, IPL>);
+            else if (C.reg) dependent(k_in_a<T, true, false, GE, CMP, IPL>);
+            else dependent(k_in_a<T, false, false, GE, CMP, IPL>);
+        } else {
+            if (C.reg) dependent(k_in_a<T, true, false, GE, CMP, IPL>);
+            else dependent(k_in_a<T, false, false, GE, CMP, IPL>);
+        }
         k_in_a_fin<T><<<nb, NTF, 0, s>>>(W);
     }
-    k_in_x<T, GE, CMP><<<g, NT, 0, s>>>(W);
-    if (C.cf_half) k_in_chk<T, false, true, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-    else if (C.reg) k_in_chk<T, true, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-    else k_in_chk<T, false, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
+    k_in_x<T, GE, CMP, IPL><<<g, NT, 0, s>>>(W);
+    if constexpr (IPL == 1) {
+        if (C.cf_half) k_in_chk<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+        else if (C.reg) k_in_chk<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_chk<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+    } else {
+        if (C.reg) k_in_chk<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_chk<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+    }
     k_in_chk_fin<T><<<nb, NTF, 0, s>>>(W);
 }
 
-template <typename T, int GE, bool CMP>
+template <typename T, int GE, bool CMP, int IPL>
 void time_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a)
 {
     dim3 g((unsigned)W.nblk, (unsigned)W.ngroups);
-    k_in_fill<T, GE, CMP><<<g, NT, 0, s>>>(W);
+    if (IPL > 1 && (C.cf_half || C.tier_lim)) fail(HEOM_E_ARG, "two instances per lane: steady operators of whole hierarchies only");
+    k_in_fill<T, GE, CMP, IPL><<<g, NT, 0, s>>>(W);
     auto run_b = [&] {
-        if (C.cf_half) k_in_b<T, false, true, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else if (C.reg) k_in_b<T, true, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else k_in_b<T, false, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
+        if constexpr (IPL == 1)
+            if (C.cf_half) { k_in_b<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W); return; }
+        if (C.reg) k_in_b<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_b<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
     };
     auto run_a = [&] {
-        if (C.cf_half) k_in_a<T, false, true, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else if (C.reg) k_in_a<T, true, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
-        else k_in_a<T, false, false, GE, CMP><<<g, NT, 0, s>>>(Q, C, W);
+        if constexpr (IPL == 1)
+            if (C.cf_half) { k_in_a<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W); return; }
+        if (C.reg) k_in_a<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
+        else k_in_a<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
     };
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) fail(HEOM_E_CUDA, "cudaEventCreate failed");
@@ -583,6 +694,10 @@ void df_init_full(const InnerWork<DF> &F, cudaStream_t s);
 void df_chunk_full(InnerWork<DF> &W, const DevPlan &Q, const DevCoef<DF> &C, int iters, cudaStream_t s);
 void df_time_full(InnerWork<DF> &F, const DevPlan &Q, const DevCoef<DF> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a);
 void df_chunk_compact(InnerWork<DF> &W, const DevPlan &Q, const DevCoef<DF> &C, int iters, cudaStream_t s);
+// two instances per lane, every position served (inner_ilp.cu: GE = W.G / 2)
+void df_init_pair(const InnerWork<DF> &F, cudaStream_t s);
+void df_chunk_pair(InnerWork<DF> &W, const DevPlan &Q, const DevCoef<DF> &C, int iters, cudaStream_t s);
+void df_time_pair(InnerWork<DF> &F, const DevPlan &Q, const DevCoef<DF> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a);
 
 }  // namespace inner_detail
 }  // namespace heom

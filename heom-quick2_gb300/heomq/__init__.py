@@ -81,7 +81,28 @@ class CtxOpts(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("crit", C.c_double), ("maxit0", C.c_int32), ("precision", C.c_int32), ("inner_tol", C.c_double),
                 ("max_refine", C.c_int32), ("stag_window", C.c_int32), ("inner_precond", C.c_int32),
-                ("interleave", C.c_int32)]
+                ("interleave", C.c_int32), ("lane_instances", C.c_int32)]
+
+
+def layout_candidates(nbatch, truncated=False):
+    """The (interleave, lane_instances) layouts of the FP32x2 inner kernels that the automatic
+    choice of the mixed batch solves times, in its order (the library's rule, restated here
+    for reports): one instance per group; interleave 2 with two instances per lane (not for
+    truncated batches); the smallest power of two g >= nbatch (at most 32) with one and with
+    two instances per lane."""
+    g = 1
+    while g < nbatch and g < 32:
+        g *= 2
+    c = [(1, 1)]
+    if g == 1:
+        return c
+    if not truncated:
+        c.append((2, 2))
+    if g > 2 or truncated:
+        c.append((g, 1))
+    if g > 2 and not truncated:
+        c.append((g, 2))
+    return c
 
 
 class SolveInfo(C.Structure):
@@ -130,6 +151,9 @@ SIGNATURES = {
     "heom_solve_batch": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(SolveOpts), C.c_void_p, _p(SolveInfo)]),
     "heom_bench_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_bench_inner": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "heom_bench_inner_layout": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                          C.c_void_p]),
+    "heom_tuned_layout": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "heom_ctx_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "heom_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, _p(C.c_void_p)]),
     "heom_batch_stride": (C.c_int64, [C.c_void_p]),
@@ -519,6 +543,22 @@ class Context:
         _check(lib().heom_bench_inner(self.h, precision, nbatch, reps, s, b))
         return (s[0], s[1]), (b[0], b[1])
 
+    def bench_inner_layout(self, interleave, lane_instances=1, reps=20, nbatch=1):
+        """bench_inner in FP32x2 with a given instance layout (SolveOpts.interleave and
+        lane_instances) instead of the one the batch solves use."""
+        s = (C.c_double * 2)()
+        b = (C.c_double * 2)()
+        _check(lib().heom_bench_inner_layout(self.h, nbatch, reps, interleave, lane_instances, s, b))
+        return (s[0], s[1]), (b[0], b[1])
+
+    def tuned_layout(self, nbatch, truncated=False):
+        """(interleave, lane_instances) the automatic choice keeps for mixed batch solves of
+        nbatch instances, or (0, 0) while it is still timing the candidates."""
+        g = C.c_int32()
+        l = C.c_int32()
+        _check(lib().heom_tuned_layout(self.h, nbatch, 1 if truncated else 0, C.byref(g), C.byref(l)))
+        return g.value, l.value
+
     def stats(self):
         """Plan statistics (see heom_ctx_stats in include/heom_gb300.h)."""
         out = np.zeros(9)
@@ -654,9 +694,10 @@ class Batch:
                 raise HeomError(rc, msg)
 
     def solve_dev(self, x_dev, crit=1e-8, maxit0=20000, precision=PREC_MIXED, inner_tol=0.0, max_refine=8, check=True,
-                  stag_window=0, inner_precond=0, interleave=0):
+                  stag_window=0, inner_precond=0, interleave=0, lane_instances=0):
         o = SolveOpts(crit=crit, maxit0=maxit0, precision=precision, inner_tol=inner_tol, max_refine=max_refine,
-                      stag_window=stag_window, inner_precond=inner_precond, interleave=interleave)
+                      stag_window=stag_window, inner_precond=inner_precond, interleave=interleave,
+                      lane_instances=lane_instances)
         info = SolveInfo()
         rc = lib().heom_batch_solve_dev(self.h, C.byref(o), C.c_void_p(x_dev), C.byref(info))
         if check:

@@ -26,8 +26,9 @@ extern "C" {
 #endif
 
 /* 4: heom_grad_opts.precision, heom_solve_opts.interleave (in place of a reserved field),
- *    heom_batch_set_tiers, HEOM_PROP_CHEBYSHEV_MIXED, heom_td_gradient_ex */
-#define HEOM_ABI_VERSION 4
+ *    heom_batch_set_tiers, HEOM_PROP_CHEBYSHEV_MIXED, heom_td_gradient_ex
+ * 5: heom_solve_opts.lane_instances, heom_bench_inner_layout, heom_tuned_layout */
+#define HEOM_ABI_VERSION 5
 
 enum {
     HEOM_OK = 0,
@@ -193,12 +194,22 @@ typedef struct {
                                  1 = on, -1 = off.  FP64 inner solves are not scaled. */
     int32_t interleave;       /* MIXED: instances interleaved per entry group in the FP32x2 inner
                                  kernels (lanes of one entry share the plan's control flow and
-                                 reads); 1 = none, 2..32 a power of two, 0 (default) = automatic:
-                                 the context times its first two mixed batch solves of each
-                                 batch size with none and with the smallest power of two >=
-                                 nbatch (at most 32), and keeps the faster for that size; single
-                                 solves use none.  An interleaved group runs until all its
-                                 instances have finished. */
+                                 reads); 1 = none, 2..32 a power of two, 0 (default) = automatic
+                                 choice of interleave and lane_instances: the context times its
+                                 first mixed batch solves of each batch size (and kind: whole or
+                                 truncated hierarchies) with each candidate layout -- none;
+                                 interleave 2 with two instances per lane (not for truncated
+                                 batches); g = the smallest power of two >= nbatch (at most 32)
+                                 with one and with two instances per lane -- and keeps the
+                                 fastest for that size (heom_tuned_layout); single solves use
+                                 none.  An interleaved group runs until all its instances have
+                                 finished. */
+    int32_t lane_instances;   /* MIXED with interleave >= 2: instances of a group served by one
+                                 thread of the inner kernels, 1 (0 selects 1) or 2: two adjacent
+                                 instances share the decode of the plan (entry, couplings, map
+                                 words, coefficients) while more than half of a group's
+                                 instances run; with interleave 2 their iterates are those of
+                                 interleave 1.  2 is refused for truncated batches. */
 } heom_solve_opts;
 
 typedef struct {
@@ -326,6 +337,16 @@ int heom_bench_apply(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t r
  * of one launch of each kernel.  No reference counterpart (the reference has no mixed
  * precision). */
 int heom_bench_inner(heom_ctx *ctx, int32_t precision, int32_t nbatch, int32_t reps, double *seconds, double *bytes);
+
+/* heom_bench_inner in FP32x2 with a given layout of the instances (heom_solve_opts.interleave
+ * >= 1 and lane_instances 1 or 2) instead of the one the batch solves use. */
+int heom_bench_inner_layout(heom_ctx *ctx, int32_t nbatch, int32_t reps, int32_t interleave, int32_t lane_instances,
+                            double *seconds, double *bytes);
+
+/* The layout the automatic choice keeps for mixed batch solves of nbatch instances (truncated
+ * != 0: batches with heom_batch_set_tiers): *interleave, *lane_instances as in heom_solve_opts,
+ * or 0, 0 while the context has not yet timed every candidate. */
+int heom_tuned_layout(heom_ctx *ctx, int32_t nbatch, int32_t truncated, int32_t *interleave, int32_t *lane_instances);
 
 /* ------------------------------------------------------------------------- */
 /* Correlation functions and spectral functions in the frequency domain (corrfunc/).
