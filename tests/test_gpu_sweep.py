@@ -26,7 +26,9 @@ def _family(tiers, Vs, Us):
     return cfgs, deep, hs, es
 
 
-@pytest.mark.parametrize("prec,crit,bar", [(heomq.PREC_FP64_REFINED, 1e-12, 1e-9), (heomq.PREC_MIXED, 1e-10, 1e-8)],
+# The states agree to about 100 crit (the residual bound times the conditioning of these
+# hierarchies: 1.3e-8 was seen at crit 1e-10), so the mixed solve runs at crit 1e-11.
+@pytest.mark.parametrize("prec,crit,bar", [(heomq.PREC_FP64_REFINED, 1e-12, 1e-9), (heomq.PREC_MIXED, 1e-11, 1e-8)],
                          ids=["fp64_refined", "mixed"])
 def test_truncated_batch_equals_separate_solves_at_each_tier(prec, crit, bar):
     tiers = [2, 3, 4, 5, 3]
