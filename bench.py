@@ -41,8 +41,8 @@ def parse():
     ap.add_argument("--profile-inner", action="store_true",
                     help="profiler run of the two fused FP32x2 inner-iteration kernels: 3 warm-up + 2 timed launches each")
     ap.add_argument("--inner-layout", default=None,
-                    help="--profile-inner: the instance layout GxL (interleave G, L instances per lane, e.g. 2x2) "
-                         "instead of the one the batch solves use")
+                    help="--profile-inner, --profile: the instance layout GxL (interleave G, L instances per lane, "
+                         "e.g. 8x2) instead of the one the batch solves use")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
     ap.add_argument("--workload", default="steady", choices=["steady", "dos", "jacobi"],
@@ -447,7 +447,9 @@ def run_gb300(args, ws, rank, local, dist):
         step(heomq.PREC_MIXED)
     layout = ctx.tuned_layout(B)
     if args.profile:
-        info = step(heomq.PREC_MIXED)
+        # under a profiler the timed choice of the layout is distorted: --inner-layout names it
+        g, lanes = (int(v) for v in args.inner_layout.split("x")) if args.inner_layout else (0, 0)
+        info = step(heomq.PREC_MIXED, interleave=g, lane_instances=lanes)
         print(json.dumps({"profile_run": True, "batch": B, "applies": info.iters, "seconds": info.seconds,
                           "launches": info.launches}), flush=True)
         batch.close()

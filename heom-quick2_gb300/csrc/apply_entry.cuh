@@ -106,27 +106,30 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
         acc[0] = N::add(acc[0], N::scale(N::load(x[0][(int64_t)(hrow ? t + C.cf_half : t - C.cf_half) * xs]), N::sc(w)));
     }
 
-    // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients).
-    // Every term goes straight into acc: right terms (x H) as +i h x, left terms (H x) as
-    // -i h x (adjoint: the opposite signs), the sign and the factor i as sign-bit flips and a
-    // swap of the parts; acc is renormalised after every fourth term.
+    // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)
     const int tb = __ldg(P.cls_tptr + c) + p;
     const int k0 = __ldg(P.term_ptr + tb), k1 = __ldg(P.term_ptr + tb + 1);
+    // one signed sum: right terms (x H) count +, left terms (H x) count - (no divergent branch)
+    A sd[NI];
+#pragma unroll
+    for (int i = 0; i < NI; i++) sd[i] = N::zero();
     for (int k = k0; k < k1; k++) {
         const uint32_t w = __ldg(P.terms + k);
         const int hq = (int)((w >> 16) & 0x7FFF), q = (int)(w & 0xFFFF);
-        const uint32_t ng = (w >> 31) ^ (ADJ ? 0u : 1u);
 #pragma unroll
         for (int i = 0; i < NI; i++) {
             A h = N::load(hv[i][(int64_t)hq * xs]);
             if (ADJ) h = N::conj(h);
             const A xv = rdo ? herm_part<T>(x[i], C.rdo_pair, q, xs) : N::load(x[i][(int64_t)(off + q) * xs]);
             const A hx = C.h_real ? N::scale(xv, N::re_s(h)) : N::mul(h, xv);
-            acc[i] = N::add(acc[i], N::mul_i(N::flip(hx, ng, 0u)));
+            sd[i] = N::add(sd[i], N::flip(hx, (w >> 31) ^ 1u, 0u));
         }
-        if (((k - k0) & 3) == 3)
+    }
+    // forward: acc += i (sum_right - sum_left); adjoint: acc += -i (...)
 #pragma unroll
-            for (int i = 0; i < NI; i++) acc[i] = N::norm(acc[i]);
+    for (int i = 0; i < NI; i++) {
+        const A dlt = N::mul_i(N::norm(sd[i]));
+        acc[i] = N::add(acc[i], ADJ ? N::neg(dlt) : dlt);
     }
 
     // couplings to the neighbouring tiers: coefficient pairs (lower tier) first, then the
@@ -161,8 +164,10 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
 #pragma unroll
             for (int i = 0; i < NI; i++) acc[i] = N::norm(acc[i]);
     }
-    // cL v + cR v' with cL = i sL, cR = i sR (sL, sR = +-1; real for the correlation-function
-    // operator): i sL v and i sR v' go straight into acc as sign-bit flips and a swap of the parts
+    // cL v + cR v' with cL = i sL, cR = i sR: accumulate sL v + sR v', times i below
+    A ua[NI];
+#pragma unroll
+    for (int i = 0; i < NI; i++) ua[i] = N::zero();
     // the last kept tier of a truncated instance has no higher-tier couplings
     const int eu = (C.unit_on && (ADJ || !C.tier_lim || off < __ldg(&C.tier_lim[b[0]].x))) ? e1 : em;
     for (int e = em; e < eu; e++) {
@@ -175,8 +180,8 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
             const uint32_t ng = ((lo >> 15) ^ (uint32_t)rec.z) & 1u;
 #pragma unroll
             for (int i = 0; i < NI; i++) {
-                const A v = N::flip(src_rdo ? herm_part<T>(x[i], C.rdo_pair, q, xs) : N::load(x[i][(int64_t)(rec.x + q) * xs]), ng, cj);
-                acc[i] = N::add(acc[i], CF ? v : N::mul_i(v));
+                const A v = src_rdo ? herm_part<T>(x[i], C.rdo_pair, q, xs) : N::load(x[i][(int64_t)(rec.x + q) * xs]);
+                ua[i] = N::add(ua[i], N::flip(v, ng, cj));
             }
         }
         if (hi) {
@@ -184,17 +189,18 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
             const uint32_t ng = ((hi >> 15) ^ ((uint32_t)rec.z >> 1)) & 1u;
 #pragma unroll
             for (int i = 0; i < NI; i++) {
-                const A v = N::flip(src_rdo ? herm_part<T>(x[i], C.rdo_pair, q, xs) : N::load(x[i][(int64_t)(rec.x + q) * xs]), ng, cj);
-                acc[i] = N::add(acc[i], CF ? v : N::mul_i(v));
+                const A v = src_rdo ? herm_part<T>(x[i], C.rdo_pair, q, xs) : N::load(x[i][(int64_t)(rec.x + q) * xs]);
+                ua[i] = N::add(ua[i], N::flip(v, ng, cj));
             }
         }
-        if (((e - em) & 1) == 1)
+        if (((e - e0) & 3) == 3)
 #pragma unroll
-            for (int i = 0; i < NI; i++) acc[i] = N::norm(acc[i]);
+            for (int i = 0; i < NI; i++) ua[i] = N::norm(ua[i]);
     }
     const float pre = C.pre ? __ldg(C.pre + n) : 1.f;
 #pragma unroll
     for (int i = 0; i < NI; i++) {
+        acc[i] = N::add(acc[i], CF ? ua[i] : N::mul_i(ua[i]));
         if (C.pre) acc[i] = N::scale(acc[i], N::sc((double)pre));
         y[i] = acc[i];
     }

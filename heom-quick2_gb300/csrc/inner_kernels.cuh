@@ -301,10 +301,11 @@ __global__ void __launch_bounds__(NTF) k_in_init_fin(InnerWork<T> W, double crit
 }
 
 // Resident blocks per SM of the apply kernels: six (at most 40 registers) with one instance
-// per lane; five (48 registers, no spills) with two, whose accumulators double.  Measured on
-// the double dot at tier 4, batch 8, two instances per lane in groups of two (k_in_b +
-// k_in_a): 394 us at five blocks, 399 us at six (40 registers, 16-40 bytes of spills); at
-// four (64 registers) too few warps hide the gathers' latency (437 us, issue slots 66 % busy).
+// per lane; five (48 registers, 8-24 bytes of spills) with two, whose accumulators double.
+// Measured on the double dot at tier 4, batch 8, two instances per lane in groups of two
+// (k_in_b + k_in_a): 403 us at five blocks; 430 us at six (40 registers, 40-110 bytes of
+// spills); at four (64 registers, no spills) too few warps hide the gathers' latency (437 us,
+// issue slots 66 % busy).
 template <int IPL> constexpr int apply_blocks_per_sm() { return IPL == 1 ? 6 : 5; }
 
 // B: u1 = A w + beta u2, the pending x / d updates, y = w + beta y2, v = u1 + beta (u2 + beta v)
