@@ -213,8 +213,8 @@ def sweep_record(crit):
     20261203: V ~ U[-1, 1], U in {1, 2, 3}, eps = -U/2, tier in {2, 3, 4}), one table family
     solved as one batch on the tier-4 tables with each instance truncated at its own tier
     (heomq.sweep); wall time includes the host set-up of the tables.  Errors against the same
-    sweep refined in FP64 to ||b - A x|| <= 1e-12.  A leg that does not reach crit (the plain
-    FP64 TFQMR stalls near 1.2e-9 on one of these instances) is recorded as it ends."""
+    sweep refined in FP64 to ||b - A x|| <= 1e-12.  A leg that does not reach crit is recorded
+    as it ends."""
     import numpy as np
 
     import heomq
@@ -238,8 +238,10 @@ def sweep_record(crit):
 
 def kanamori_record(crit):
     """The three-orbital Kanamori impurity (nd = 64, tier 2, Pade M = 6, T = 0.05), four bias
-    points in one batch, mixed precision against the plain FP64 TFQMR (which stalls near 4e-8
-    on this batch), and both against FP64 inner solves refined to 1e-12."""
+    points in one batch, mixed precision against the plain FP64 TFQMR (which sits at the edge
+    of its floor on this batch: it converges or stalls near 4e-8 depending on the rounding of
+    its apply, and is recorded as it ends), and both against FP64 inner solves refined to
+    1e-12."""
     import numpy as np
     import torch
 
@@ -515,7 +517,7 @@ def run_gb300(args, ws, rank, local, dist):
     achieved = bb / sb / 1e9
     # ncu summary of the fused kernels in the chosen layout
     prof = {(8, 1): "inner_fp32x2_interleaved_dqd_L4_batch8.md",
-            (2, 2): "inner_fp32x2_pairs_dqd_L4_batch8.md"}.get(layout, "inner_fp32x2_dqd_L4_batch8.md")
+            (8, 2): "inner_fp32x2_interleaved_pairs_dqd_L4_batch8.md"}.get(layout, "inner_fp32x2_dqd_L4_batch8.md")
     traffic = profile_traffic(prof, "dram_bytes_per_launch_k_in_b")
     traffic_a = profile_traffic(prof, "dram_bytes_per_launch_k_in_a")
     # accuracy: both paths against a reference steady state refined in FP64 to ||b - A x|| <= 1e-12
