@@ -8,6 +8,7 @@
 #include <cmath>
 #include <vector>
 
+#include "apply_entry.cuh"
 #include "context.cuh"
 #include "propagate.cuh"
 
@@ -75,18 +76,24 @@ __global__ void k_current_df(const float4 *x, const CurrentTerm *terms, int nter
     if (threadIdx.x < nslot) jt[(int64_t)clk->n * nslot + threadIdx.x] = -2.0 * part[0][threadIdx.x] * kJconst;
 }
 
-// Chebyshev term in FP32x2: pn = pm2 + s lp; rho += c pn (first term: pn = s lp, rho = c0 pm2 + c pn)
-__global__ void k_cheb_df(int64_t n, const float4 *pm2, const float4 *lp, float4 *pn, float4 *rho, f2r s, f2r c, int first,
-                          f2r c0)
+// One Chebyshev term in FP32x2 with the derivative apply fused in: l = A pm1, pn = pm2 + s l,
+// rho += c pn (first term: l = A pm2 with pm2 the copy of rho, pn = s l, rho = c0 pm2 + c pn).
+// l is renormalised as a store and reload of it would be: the terms are bit-identical to a
+// separate apply followed by the update, without l's round trip through memory and one
+// launch per term.
+__global__ void __launch_bounds__(256, 6) k_cheb_apply_df(DevPlan P, DevCoef<DF> C, const float4 *__restrict__ src,
+                                                       const float4 *__restrict__ pm2, float4 *__restrict__ pn,
+                                                       float4 *__restrict__ rho, f2r s, f2r c, int first, f2r c0)
 {
     using N = Num<DF>;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const N::A l = N::load(lp[i]), p2 = N::load(pm2[i]);
-        const N::A v = first ? N::scale(l, s) : N::add(p2, N::scale(l, s));
-        pn[i] = N::store(v);
-        const N::A r = first ? N::scale(p2, c0) : N::load(rho[i]);
-        rho[i] = N::store(N::add(r, N::scale(N::norm(v), c)));
-    }
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.lunk) return;
+    const N::A l = N::norm(apply_entry<DF, false, false>(P, C, src, i, 0));
+    const N::A p2 = N::load(pm2[i]);
+    const N::A v = first ? N::scale(l, s) : N::add(p2, N::scale(l, s));
+    pn[i] = N::store(v);
+    const N::A r = first ? N::scale(p2, c0) : N::load(rho[i]);
+    rho[i] = N::store(N::add(r, N::scale(N::norm(v), c)));
 }
 
 __global__ void k_to_df(int64_t n, const double2 *a, float4 *o)
@@ -256,28 +263,27 @@ void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &Kin, PropBuffe
 
 // One Chebyshev step in FP32x2 (HEOM_PROP_CHEBYSHEV_MIXED): the state rho, the recurrence
 // vectors v[0..3] and the applies in FP32x2; gdf receives the step's ADO diagonals.
-void enqueue_step_df(heom_ctx *c, const DevCoef<DF> &Kin, PropBuffers &B, float4 *rho, float4 *const v[4], float4 *gdf,
+void enqueue_step_df(heom_ctx *c, const DevCoef<DF> &Kin, PropBuffers &B, float4 *rho, float4 *const v[3], float4 *gdf,
                      double delta, const std::vector<double> &bes, bool record_current)
 {
     const DevPlan &P = c->dfwd.view;
     DevCoef<DF> K = Kin;
     K.trace_on = 0;
     K.eshift = B.es;
-    const int64_t N = B.N, L = c->lunk;
+    const int64_t L = c->lunk;
     const int ns = c->nalf * c->nspin;
     cudaStream_t s = c->stream;
     if (record_current) k_current_df<<<1, NT, 0, s>>>(rho, c->d_cur_terms, c->n_cur_terms, ns, B.clk, B.jt);
     stage_prepare(c, B, 0.0, false, s);   // the step's lead shifts in B.es
     fill_gdiag<DF>(P, K, gdf, 1, s);      // and its ADO diagonals in FP32x2 (K.gdiag = gdf)
-    float4 *pm2 = v[0], *pm1 = v[1], *pn = v[2], *lp = v[3];
+    float4 *pm2 = v[0], *pm1 = v[1], *pn = v[2];
+    const unsigned nb = (unsigned)((L + 255) / 256);
     CK(cudaMemcpyAsync(pm2, rho, sizeof(float4) * L, cudaMemcpyDeviceToDevice, s));
-    launch_apply<DF, false>(P, K, pm2, lp, 1, N, nullptr, s);
-    k_cheb_df<<<grid_for(L), NT, 0, s>>>(L, pm2, lp, pm1, rho, f2r_from_d(1.0 / delta), f2r_from_d(2.0 * bes[1]), 1,
-                                         f2r_from_d(bes[0]));
+    k_cheb_apply_df<<<nb, 256, 0, s>>>(P, K, pm2, pm2, pm1, rho, f2r_from_d(1.0 / delta), f2r_from_d(2.0 * bes[1]), 1,
+                                       f2r_from_d(bes[0]));
     for (size_t n = 2; n < bes.size(); n++) {
-        launch_apply<DF, false>(P, K, pm1, lp, 1, N, nullptr, s);
-        k_cheb_df<<<grid_for(L), NT, 0, s>>>(L, pm2, lp, pn, rho, f2r_from_d(2.0 / delta), f2r_from_d(2.0 * bes[n]), 0,
-                                             f2r_from_d(0.0));
+        k_cheb_apply_df<<<nb, 256, 0, s>>>(P, K, pm1, pm2, pn, rho, f2r_from_d(2.0 / delta), f2r_from_d(2.0 * bes[n]), 0,
+                                           f2r_from_d(0.0));
         float4 *t = pm2; pm2 = pm1; pm1 = pn; pn = t;
     }
     k_advance<<<1, 1, 0, s>>>(B.clk);
@@ -317,15 +323,15 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
         const CoefSet K = ctx_coefs(c);
         // FP32x2 state and recurrence for HEOM_PROP_CHEBYSHEV_MIXED
         float4 *dfmem = nullptr;
-        float4 *xdf = nullptr, *vdf[4] = {nullptr, nullptr, nullptr, nullptr}, *gdf = nullptr;
+        float4 *xdf = nullptr, *vdf[3] = {nullptr, nullptr, nullptr}, *gdf = nullptr;
         struct DfFree { float4 *&p; ~DfFree() { if (p) cudaFree(p); } } df_free{dfmem};
         if (method == HEOM_PROP_CHEBYSHEV_MIXED) {
             const int64_t N = c->lunk + 1, vs = (N + 63) / 64 * 64, nd = std::max<int64_t>(1, c->dfwd.view.nado);
-            CK(cudaMalloc((void **)&dfmem, sizeof(float4) * (size_t)(5 * vs + nd)));
-            CK(cudaMemsetAsync(dfmem, 0, sizeof(float4) * (size_t)(5 * vs + nd), c->stream));
+            CK(cudaMalloc((void **)&dfmem, sizeof(float4) * (size_t)(4 * vs + nd)));
+            CK(cudaMemsetAsync(dfmem, 0, sizeof(float4) * (size_t)(4 * vs + nd), c->stream));
             xdf = dfmem;
-            for (int k = 0; k < 4; k++) vdf[k] = dfmem + (k + 1) * vs;
-            gdf = dfmem + 5 * vs;
+            for (int k = 0; k < 3; k++) vdf[k] = dfmem + (k + 1) * vs;
+            gdf = dfmem + 4 * vs;
             k_to_df<<<grid_for(c->lunk), NT, 0, c->stream>>>(c->lunk, x, xdf);
         }
         if (nstep > 0) {

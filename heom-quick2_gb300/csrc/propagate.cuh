@@ -42,9 +42,9 @@ int cheby_terms(double delta, double dt, double dpre);
 void prop_clock_init(heom_ctx *c, PropClock &h, double t0, double dt, double amp_scale);
 void enqueue_step(heom_ctx *c, int method, const DevCoef<double> &K, PropBuffers &B, double2 *rho, double delta,
                   const std::vector<double> &bes, bool record_current);
-// One Chebyshev step in FP32x2: state rho, recurrence vectors v[0..3], the step's ADO
+// One Chebyshev step in FP32x2: state rho, recurrence vectors v[0..2], the step's ADO
 // diagonals written to gdf (HEOM_PROP_CHEBYSHEV_MIXED)
-void enqueue_step_df(heom_ctx *c, const DevCoef<DF> &K, PropBuffers &B, float4 *rho, float4 *const v[4], float4 *gdf,
+void enqueue_step_df(heom_ctx *c, const DevCoef<DF> &K, PropBuffers &B, float4 *rho, float4 *const v[3], float4 *gdf,
                      double delta, const std::vector<double> &bes, bool record_current);
 
 }  // namespace heom

@@ -163,7 +163,7 @@ void td_gradient_run(heom_ctx *c, double dt, int nstep, int ck, const double _Co
         char *qs = (char *)dalloc(vb * K);
         V *mu[3] = {(V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb)};
         V *lam = (V *)dalloc(vb), *lh = (V *)dalloc(vb), *cv = (V *)dalloc(vb);
-        V *x = (V *)dalloc(vb), *xv[4] = {(V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb)};
+        V *x = (V *)dalloc(vb), *xv[3] = {(V *)dalloc(vb), (V *)dalloc(vb), (V *)dalloc(vb)};
         V *gdT = (V *)dalloc(sizeof(V) * nd), *gdaT = (V *)dalloc(sizeof(V) * nd);
         double *acc = (double *)dalloc(sizeof(double) * N);
         double *dsum = (double *)dalloc(sizeof(double));
