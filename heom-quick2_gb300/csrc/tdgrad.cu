@@ -91,71 +91,66 @@ __global__ void k_lambda(int64_t n, const typename Num<T>::V *c, double dt, cons
 
 __global__ void k_set_step(PropClock *clk, int64_t n) { clk->n = n; }
 
-// One term of a Chebyshev step with its Q kept: Q_k = (first ? 0 : Q_{k-2}) + s lq and
-// out = (first ? c0 Q_0 : out) + c Q_k (the arithmetic of the propagation step)
-template <typename T>
-__global__ void k_qcheb(int64_t n, const typename Num<T>::V *q0, const typename Num<T>::V *qm2, const typename Num<T>::V *lq,
-                        typename Num<T>::V *q, typename Num<T>::V *out, double s, double c, int first, double c0)
-{
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 l = Io<T>::ld(lq[i]);
-        double2 v;
-        if (first) v = make_double2(s * l.x, s * l.y);
-        else { const double2 p = Io<T>::ld(qm2[i]); v = make_double2(p.x + s * l.x, p.y + s * l.y); }
-        Io<T>::st(q[i], v);
-        double2 r;
-        if (first) { const double2 z = Io<T>::ld(q0[i]); r = make_double2(c0 * z.x, c0 * z.y); }
-        else r = Io<T>::ld(out[i]);
-        Io<T>::st(out[i], make_double2(r.x + c * v.x, r.y + c * v.y));
-    }
-}
-
-// FP32x2 forms with the apply fused in (one kernel per term, no round trip of the applied
-// vector through memory): the applied value is renormalised in registers, as its store and
-// reload would be, and then read as FP64 like the stored values.
-__device__ __forceinline__ double2 df_to_d(const Num<DF>::A &a)
+// Terms with the apply fused in (one kernel per term, no round trip of the applied vector
+// through memory).  In FP32x2 the applied value is renormalised in registers, as its store
+// and reload would be, and then read as FP64 like the stored values.  In FP64 the threads
+// take the entries in the plan's work-profile order, as the FP64 apply does.
+template <typename T> __device__ __forceinline__ double2 applied(const typename Num<T>::A &a);
+template <> __device__ __forceinline__ double2 applied<double>(const double2 &a) { return a; }
+template <> __device__ __forceinline__ double2 applied<DF>(const f2c &a)
 {
     const Num<DF>::A v = Num<DF>::norm(a);
     return make_double2(Num<DF>::re(v), Num<DF>::im(v));
 }
-
-// k_qcheb with lq = L src (src = Q_{k-1})
-__global__ void __launch_bounds__(256, 6) k_qcheb_apply_df(DevPlan P, DevCoef<DF> C, const float4 *__restrict__ src,
-                                                        const float4 *q0, const float4 *qm2, float4 *q, float4 *out,
-                                                        double s, double c, int first, double c0)
+template <typename T> __device__ __forceinline__ int64_t term_entry(const DevPlan &P, int64_t tid)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.lunk) return;
-    const double2 l = df_to_d(apply_entry<DF, false, false>(P, C, src, i, 0));
+    return (std::is_same<T, double>::value && P.order) ? (int64_t)__ldg(P.order + tid) : tid;
+}
+
+// One term of a Chebyshev step with its Q kept, the apply fused in: Q_k = (first ? 0 :
+// Q_{k-2}) + s L Q_{k-1} and out = (first ? c0 Q_0 : out) + c Q_k (the arithmetic of the
+// propagation step); src = Q_{k-1}
+template <typename T>
+__global__ void __launch_bounds__(256, 6) k_qcheb_apply(DevPlan P, DevCoef<T> C, const typename Num<T>::V *__restrict__ src,
+                                                     const typename Num<T>::V *q0, const typename Num<T>::V *qm2,
+                                                     typename Num<T>::V *q, typename Num<T>::V *out, double s, double c,
+                                                     int first, double c0)
+{
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= P.lunk) return;
+    const int64_t i = term_entry<T>(P, tid);
+    const double2 l = applied<T>(apply_entry<T, false, false>(P, C, src, i, 0));
     double2 v;
     if (first) v = make_double2(s * l.x, s * l.y);
-    else { const double2 p = Io<DF>::ld(qm2[i]); v = make_double2(p.x + s * l.x, p.y + s * l.y); }
-    Io<DF>::st(q[i], v);
+    else { const double2 p = Io<T>::ld(qm2[i]); v = make_double2(p.x + s * l.x, p.y + s * l.y); }
+    Io<T>::st(q[i], v);
     double2 r;
-    if (first) { const double2 z = Io<DF>::ld(q0[i]); r = make_double2(c0 * z.x, c0 * z.y); }
-    else r = Io<DF>::ld(out[i]);
-    Io<DF>::st(out[i], make_double2(r.x + c * v.x, r.y + c * v.y));
+    if (first) { const double2 z = Io<T>::ld(q0[i]); r = make_double2(c0 * z.x, c0 * z.y); }
+    else r = Io<T>::ld(out[i]);
+    Io<T>::st(out[i], make_double2(r.x + c * v.x, r.y + c * v.y));
 }
 
 // k_mu with lh = L^H src (src = mu_{j+1}, the adjoint plan PA)
-__global__ void __launch_bounds__(256, 6) k_mu_apply_df(DevPlan PA, DevCoef<DF> CA, const float4 *__restrict__ src,
-                                                     const DevPlan P, const double *es, const float4 *lam, double a,
-                                                     double s_next, const float4 *mu2, float4 *mu, const float4 *qprev,
-                                                     double s_j, double *acc)
+template <typename T>
+__global__ void __launch_bounds__(256, 6) k_mu_apply(DevPlan PA, DevCoef<T> CA, const typename Num<T>::V *__restrict__ src,
+                                                  const DevPlan P, const double *es, const typename Num<T>::V *lam, double a,
+                                                  double s_next, const typename Num<T>::V *mu2, typename Num<T>::V *mu,
+                                                  const typename Num<T>::V *qprev, double s_j, double *acc)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.lunk) return;
-    const double2 h = df_to_d(apply_entry<DF, true, false>(PA, CA, src, i, 0));
-    const double2 l = Io<DF>::ld(lam[i]);
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= P.lunk) return;
+    const int64_t i = term_entry<T>(PA, tid);
+    const double2 h = applied<T>(apply_entry<T, true, false>(PA, CA, src, i, 0));
+    const double2 l = Io<T>::ld(lam[i]);
     double2 m = make_double2(a * l.x, a * l.y);
     m.x += s_next * h.x; m.y += s_next * h.y;
-    if (mu2) { const double2 u = Io<DF>::ld(mu2[i]); m.x += u.x; m.y += u.y; }
-    Io<DF>::st(mu[i], m);
+    if (mu2) { const double2 u = Io<T>::ld(mu2[i]); m.x += u.x; m.y += u.y; }
+    Io<T>::st(mu[i], m);
     if (qprev) {
         const unsigned cnt = (unsigned)P.ado_cnt[P.ent_ado[i]];
         double d = 0;
         for (int k = 0; k < 4; k++) d += (double)(int8_t)(cnt >> (8 * k)) * es[k];
-        const double2 q = Io<DF>::ld(qprev[i]);
+        const double2 q = Io<T>::ld(qprev[i]);
         acc[i] += s_j * d * (m.y * q.x - m.x * q.y);
     }
 }
@@ -292,15 +287,8 @@ void td_gradient_run(heom_ctx *c, double dt, int nstep, int ck, const double _Co
                 auto Qk = [&](int k) { return qseg ? QS(n - n0, k) : Q(k); };
                 CK(cudaMemcpyAsync(Qk(0), st(n - n0), vb, cudaMemcpyDeviceToDevice, s));
                 for (int k = 1; k < K; k++) {
-                    const double sk = k == 1 ? 1.0 / delta : 2.0 / delta;
-                    if constexpr (std::is_same<T, DF>::value)
-                        k_qcheb_apply_df<<<gA, NT, 0, s>>>(P, KF, Qk(k - 1), Qk(0), k >= 2 ? Qk(k - 2) : nullptr, Qk(k), x, sk,
-                                                           2.0 * bes[k], k == 1, bes[0]);
-                    else {
-                        launch_apply<T, false>(P, KF, Qk(k - 1), lh, 1, N, nullptr, s);
-                        k_qcheb<T><<<gL, NT, 0, s>>>(L, Qk(0), k >= 2 ? Qk(k - 2) : nullptr, lh, Qk(k), x, sk, 2.0 * bes[k],
-                                                     k == 1, bes[0]);
-                    }
+                    k_qcheb_apply<T><<<gA, NT, 0, s>>>(P, KF, Qk(k - 1), Qk(0), k >= 2 ? Qk(k - 2) : nullptr, Qk(k), x,
+                                                       k == 1 ? 1.0 / delta : 2.0 / delta, 2.0 * bes[k], k == 1, bes[0]);
                 }
                 if (n < n1 - 1) CK(cudaMemcpyAsync(st(n - n0 + 1), x, vb, cudaMemcpyDeviceToDevice, s));
             }
@@ -326,13 +314,8 @@ void td_gradient_run(heom_ctx *c, double dt, int nstep, int ck, const double _Co
                     const double s_next = (j + 1 == 1) ? 1.0 / delta : 2.0 / delta;
                     const V *qp = j >= 1 ? Qn(j - 1) : nullptr;
                     const double sj = j == 1 ? 1.0 / delta : 2.0 / delta;
-                    if constexpr (std::is_same<T, DF>::value) {
-                        if (m1) k_mu_apply_df<<<gA, NT, 0, s>>>(PA, KA, m1, P, B.es, lam, a, s_next, m2, mj, qp, sj, acc);
-                        else k_mu<T><<<gL, NT, 0, s>>>(L, P, B.es, lam, a, nullptr, s_next, m2, mj, qp, sj, acc);
-                    } else {
-                        if (m1) launch_apply<T, true>(PA, KA, m1, lh, 1, N, nullptr, s);
-                        k_mu<T><<<gL, NT, 0, s>>>(L, P, B.es, lam, a, m1 ? lh : nullptr, s_next, m2, mj, qp, sj, acc);
-                    }
+                    if (m1) k_mu_apply<T><<<gA, NT, 0, s>>>(PA, KA, m1, P, B.es, lam, a, s_next, m2, mj, qp, sj, acc);
+                    else k_mu<T><<<gL, NT, 0, s>>>(L, P, B.es, lam, a, nullptr, s_next, m2, mj, qp, sj, acc);
                     m2 = m1;
                     m1 = mj;
                 }
