@@ -134,6 +134,22 @@ def test_two_instances_per_lane_in_wide_groups():
         ctx.close()
 
 
+def test_two_instances_per_lane_in_groups_of_32():
+    """Interleave 32 with two instances per lane (16 lanes per entry) on 20 bias points of the
+    single-orbital model, instances finishing apart: currents of interleave 1 within 1e-8."""
+    m = heomq.Model(models.siam(ntier=4, nmats=3))
+    Vs = [-1.5 + 0.16 * b for b in range(20)]
+    ctx, batch = _bias_batch(m, Vs)
+    cur = {}
+    for g, lanes in ((1, 1), (32, 2)):
+        x, info = _solve(m, batch, 1e-10, g, lanes)
+        assert info.converged and info.resid <= 1e-10, (g, lanes)
+        cur[g] = np.array([ctx.current(x[b, : m.lunk].cpu().numpy()) for b in range(len(Vs))])
+    assert np.abs(cur[32] - cur[1]).max() <= 1e-8 * np.abs(cur[1]).max()
+    batch.close()
+    ctx.close()
+
+
 def test_automatic_layout_times_every_candidate_then_keeps_one():
     m = heomq.Model(models.siam(ntier=4, nmats=3))
     ctx, batch = _bias_batch(m, [0.1 * b for b in range(1, 7)])
