@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--inner-layout", default=None,
                     help="--profile-inner, --profile: the instance layout GxL (interleave G, L instances per lane, "
                          "e.g. 8x2) instead of the one the batch solves use")
+    ap.add_argument("--profile-cheb", action="store_true",
+                    help="profiler run of the FP32x2 Chebyshev propagation of the headline model (V = 0.8): 2 "
+                         "warm-up and 3 timed steps of 0.05 (one kernel per Chebyshev term)")
     ap.add_argument("--profile-apply", default=None, choices=["fp64", "fp32x2", "fp32"],
                     help="profiler run of the apply alone over the batch: 3 warm-up + 2 timed launches")
     ap.add_argument("--workload", default="steady", choices=["steady", "dos", "jacobi"],
@@ -423,6 +426,19 @@ def run_gb300(args, ws, rank, local, dist):
         return batch.solve_dev(x.data_ptr(), crit=crit or args.crit, precision=prec, max_refine=refine, check=check,
                                interleave=interleave, lane_instances=lane_instances)
 
+    if args.profile_cheb:
+        pm = heomq.Model(heomq.models.dqd(ntier=5, nmats=3, V=0.8))
+        pc = heomq.Context(pm, device=dev, adjoint=False)
+        r0 = pm.initial_guess()
+        pc.propagate(r0, 0.0, 0.05, 2, method=heomq.PROP_CHEBYSHEV_MIXED)
+        t0 = time.perf_counter()
+        pc.propagate(r0, 0.0, 0.05, 3, method=heomq.PROP_CHEBYSHEV_MIXED)
+        print(json.dumps({"profile_cheb": True, "entries": pm.lunk, "steps": 3,
+                          "ms_per_step": 1e3 * (time.perf_counter() - t0) / 3}), flush=True)
+        pc.close()
+        batch.close()
+        ctx.close()
+        return 0
     if args.profile_apply:
         prec = {"fp64": heomq.PREC_FP64, "fp32x2": heomq.PREC_MIXED, "fp32": heomq.PREC_MIXED_FP32}[args.profile_apply]
         sec, alg = ctx.bench_apply(prec, reps=2, nbatch=B)
