@@ -756,7 +756,8 @@ def run_dos(args, ws, rank, local, dist):
                        "spectrum_min": float(out[:, 1:3].min()), "steady_resid": sinfo.resid},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": f"k_in_b<FP32x2, cf>: apply of w plus the fused vector updates, over {2 * nf} instances",
+                         "kernel": f"k_in_b<FP32x2, cf>, two instances per lane: apply of w plus the fused vector updates, "
+                                   f"over {2 * nf} instances",
                          "kernel_us": sb * 1e6, "alg_bytes_per_launch": bb,
                          "k_in_a": {"kernel_us": sa * 1e6, "alg_bytes_per_launch": ba, "achieved": ba / sa / 1e9},
                          "fp64_apply": {"kernel_us": sec * 1e6, "alg_bytes_per_launch": alg, "achieved": alg / sec / 1e9,

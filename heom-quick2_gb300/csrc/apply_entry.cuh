@@ -36,7 +36,7 @@ __device__ __forceinline__ typename Num<T>::A herm_part(const typename Num<T>::V
 // applies).  NI > 1: the instances sit in one interleaved group (XS != 1) and share the
 // decode of the plan (entry, pattern class, coupling records, map words, coefficients);
 // only the loads of their values and their arithmetic are per instance.  Truncated batches
-// (C.tier_lim) and the correlation-function operator use NI = 1.
+// (C.tier_lim) use NI = 1.
 template <typename T, bool ADJ, bool REG, bool CF = false, int XS = 1, int NI = 1>
 __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T> &C,
                                               const typename Num<T>::V *const (&x)[NI], int64_t t, const int (&b)[NI],
@@ -44,7 +44,7 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
 {
     using N = Num<T>;
     using A = typename N::A;
-    static_assert(NI == 1 || (XS != 1 && !CF), "instances sharing a thread sit in one interleaved group");
+    static_assert(NI == 1 || XS != 1, "instances sharing a thread sit in one interleaved group");
     const int xs = XS > 0 ? XS : xs_rt;
     const int bg = XS == 1 ? b[0] : b[0] / xs;   // the group of the instances
     int bl[NI];                                  // their lanes in the group
@@ -102,8 +102,12 @@ __device__ __forceinline__ void apply_entries(const DevPlan &P, const DevCoef<T>
     }
     if (CF) {   // dfacta = -s, dfactb = +s (calc_ax_cf_spa_omp.f90:96-105); cf_omega[b] = s w
         const bool hrow = t < C.cf_half;
-        const double w = hrow ? -C.cf_omega[b[0]] : C.cf_omega[b[0]];
-        acc[0] = N::add(acc[0], N::scale(N::load(x[0][(int64_t)(hrow ? t + C.cf_half : t - C.cf_half) * xs]), N::sc(w)));
+        const int64_t u = hrow ? t + C.cf_half : t - C.cf_half;
+#pragma unroll
+        for (int i = 0; i < NI; i++) {
+            const double w = hrow ? -C.cf_omega[b[i]] : C.cf_omega[b[i]];
+            acc[i] = N::add(acc[i], N::scale(N::load(x[i][u * xs]), N::sc(w)));
+        }
     }
 
     // same tier: -i H X + i X H restricted to the class pattern (adjoint: conj'ed coefficients)

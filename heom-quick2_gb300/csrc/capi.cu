@@ -546,8 +546,8 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             pre_max = hi;
         }
         W.tier_lim = KI.tier_lim;
-        if (W.ipl_max > 1 && (KI.tier_lim || KI.cf_half))
-            fail(HEOM_E_ARG, "two instances per lane: steady solves of whole hierarchies only");
+        if (W.ipl_max > 1 && (KI.tier_lim || (KI.cf_half && W.G != 2)))
+            fail(HEOM_E_ARG, "two instances per lane: whole hierarchies only, and correlation functions in groups of two");
         KI = inner_layout_coef<T>(W, PV, KI, c->stream);   // the workspace's instance-interleaved layout
         auto chunk_graph = [&]() -> cudaGraphExec_t {
             const int key = 4 * W.GE + W.ipl;

@@ -227,7 +227,7 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
                 // measurement: the two fused inner kernels (B: apply of w with the first half of
                 // the vector updates; A: apply of v with the second half) over the batch
                 InnerWork<DF> IW;
-                inner_alloc<DF>(IW, nb, N, c->stream, 1);   // the layout of the solves
+                inner_alloc<DF>(IW, nb, N, c->stream, 2, 2);   // the layout of the solves
                 float4 *gdd = nullptr;
                 try {
                     std::vector<float4> rt(N);
@@ -257,7 +257,11 @@ void cf_solve_batch(heom_cf *cf, const std::vector<double> &omega, const std::ve
             heom_solve_opts mo{};
             mo.crit = crit;
             mo.maxit0 = maxit0;
-            mo.interleave = 1;   // frequencies converge at different rates: one instance per group
+            // frequencies converge at different rates: pairs of instances sharing a lane (the
+            // iterates of one instance per group, the plan decoded once per pair; a pair with one
+            // instance left runs it alone)
+            mo.interleave = 2;
+            mo.lane_instances = 2;
             std::vector<double> norms(nb, 0.0);
             std::function<void(const double2 *, double2 *)> residual = [&](const double2 *xx, double2 *r) {
                 op(xx, r, nullptr);

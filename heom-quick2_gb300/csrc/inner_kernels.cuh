@@ -589,8 +589,18 @@ __global__ void k_in_fill(InnerWork<T> W)
 }
 
 // The launches of one chunk (`iters` iterations and a check) in configuration (GE, CMP,
-// IPL).  Two instances per lane serve the steady operators only (no correlation-function
-// variant).
+// IPL).  With two instances per lane the correlation-function operator is instantiated for
+// groups of two only (the layout of its solves), and truncated batches are refused.
+template <int GE, int IPL> constexpr bool cf_variant() { return IPL == 1 || GE == 1; }
+
+template <typename T, int GE, bool CMP, int IPL>
+void check_layout(const DevCoef<T> &C)
+{
+    if (IPL > 1 && C.tier_lim) fail(HEOM_E_ARG, "two instances per lane: whole hierarchies only");
+    if (!cf_variant<GE, IPL>() && C.cf_half)
+        fail(HEOM_E_ARG, "two instances per lane: the correlation-function operator in groups of two only");
+}
+
 template <typename T, int GE, bool CMP, int IPL>
 void chunk_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int iters, cudaStream_t s)
 {
@@ -610,33 +620,27 @@ void chunk_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int iters,
         cfg.numAttrs = 1;
         if (cudaLaunchKernelEx(&cfg, kernel, Q, C, W) != cudaSuccess) fail(HEOM_E_CUDA, "launch of a fused inner kernel failed");
     };
-    if (IPL > 1 && (C.cf_half || C.tier_lim)) fail(HEOM_E_ARG, "two instances per lane: steady operators of whole hierarchies only");
+    check_layout<T, GE, CMP, IPL>(C);
     for (int i = 0; i < iters; i++) {
-        if constexpr (IPL == 1) {
+        if constexpr (cf_variant<GE, IPL>())
             if (C.cf_half) dependent(k_in_b<T, false, true, GE, CMP, IPL>);
-            else if (C.reg) dependent(k_in_b<T, true, false, GE, CMP, IPL>);
-            else dependent(k_in_b<T, false, false, GE, CMP, IPL>);
-        } else {
+        if (!C.cf_half) {
             if (C.reg) dependent(k_in_b<T, true, false, GE, CMP, IPL>);
             else dependent(k_in_b<T, false, false, GE, CMP, IPL>);
         }
         k_in_b_fin<T><<<nb, NTF, 0, s>>>(W);
-        if constexpr (IPL == 1) {
+        if constexpr (cf_variant<GE, IPL>())
             if (C.cf_half) dependent(k_in_a<T, false, true, GE, CMP, IPL>);
-            else if (C.reg) dependent(k_in_a<T, true, false, GE, CMP, IPL>);
-            else dependent(k_in_a<T, false, false, GE, CMP, IPL>);
-        } else {
+        if (!C.cf_half) {
             if (C.reg) dependent(k_in_a<T, true, false, GE, CMP, IPL>);
             else dependent(k_in_a<T, false, false, GE, CMP, IPL>);
         }
         k_in_a_fin<T><<<nb, NTF, 0, s>>>(W);
     }
     k_in_x<T, GE, CMP, IPL><<<g, NT, 0, s>>>(W);
-    if constexpr (IPL == 1) {
+    if constexpr (cf_variant<GE, IPL>())
         if (C.cf_half) k_in_chk<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
-        else if (C.reg) k_in_chk<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
-        else k_in_chk<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
-    } else {
+    if (!C.cf_half) {
         if (C.reg) k_in_chk<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_chk<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
     }
@@ -647,16 +651,16 @@ template <typename T, int GE, bool CMP, int IPL>
 void time_ge(InnerWork<T> &W, const DevPlan &Q, const DevCoef<T> &C, int reps, cudaStream_t s, float &ms_b, float &ms_a)
 {
     dim3 g((unsigned)W.nblk, (unsigned)W.ngroups);
-    if (IPL > 1 && (C.cf_half || C.tier_lim)) fail(HEOM_E_ARG, "two instances per lane: steady operators of whole hierarchies only");
+    check_layout<T, GE, CMP, IPL>(C);
     k_in_fill<T, GE, CMP, IPL><<<g, NT, 0, s>>>(W);
     auto run_b = [&] {
-        if constexpr (IPL == 1)
+        if constexpr (cf_variant<GE, IPL>())
             if (C.cf_half) { k_in_b<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W); return; }
         if (C.reg) k_in_b<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_b<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
     };
     auto run_a = [&] {
-        if constexpr (IPL == 1)
+        if constexpr (cf_variant<GE, IPL>())
             if (C.cf_half) { k_in_a<T, false, true, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W); return; }
         if (C.reg) k_in_a<T, true, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
         else k_in_a<T, false, false, GE, CMP, IPL><<<g, NT, 0, s>>>(Q, C, W);
