@@ -727,7 +727,7 @@ def run_dos(args, ws, rank, local, dist):
     (sb, sa), (bb, ba) = cf.bench_inner(nbatch=2 * nf, reps=10)
     peak, peak_kind = measured_peak_hbm()
     achieved = bb / sb / 1e9
-    prof = "inner_cf_fp32x2_dqd_L4_16inst.md"
+    prof = "inner_cf_fp32x2_pairs_dqd_L4_16inst.md"
     traffic = profile_traffic(prof, "dram_bytes_per_launch_k_in_b")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
