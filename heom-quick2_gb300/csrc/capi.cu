@@ -294,10 +294,11 @@ void tfq_run(heom_ctx *c, TfqWork<T> &W, const ApplyFn<T> &apply, int nlim, int 
     const int chunk = 25;
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < chunk; k++) tfq_iteration<T>(W, apply, c->stream);
-    CK(cudaStreamEndCapture(c->stream, &g));
-    CK(cudaGraphInstantiate(&ge, g, 0));
+    {
+        const CapturedGraph cg = capture_graph(c->stream, [&] { for (int k = 0; k < chunk; k++) tfq_iteration<T>(W, apply, c->stream); });
+        g = cg.graph;
+        ge = cg.exec;
+    }
     std::vector<int> act(W.nbatch);
     int launched = 0;
     while (true) {
@@ -553,12 +554,9 @@ void mixed_rounds(heom_ctx *c, const heom_solve_opts &o, double2 *x, int nbatch,
             const int key = 4 * W.GE + W.ipl;
             auto it = graphs.find(key);
             if (it != graphs.end()) return it->second.second;
-            auto &g = graphs[key];
-            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream);
-            CK(cudaStreamEndCapture(c->stream, &g.first));
-            CK(cudaGraphInstantiate(&g.second, g.first, 0));
-            return g.second;
+            const CapturedGraph cg = capture_graph(c->stream, [&] { inner_chunk<T>(W, PV, KI, kInnerChunk, c->stream); });
+            graphs[key] = {cg.graph, cg.exec};
+            return cg.exec;
         };
         std::vector<InnerState> st(nbatch);
         std::vector<int> amap;

@@ -28,6 +28,41 @@ struct DeviceScope {
     DeviceScope &operator=(const DeviceScope &) = delete;
 };
 
+// The launches that `enqueue` makes on stream s, captured into a graph and instantiated.
+// When enqueue or the capture fails, the capture is ended and the partial graph released
+// before the exception propagates, so that the context's stream stays usable.
+struct CapturedGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void release()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+};
+template <typename F>
+CapturedGraph capture_graph(cudaStream_t s, F &&enqueue)
+{
+    CapturedGraph cg;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue();
+    } catch (...) {
+        cudaStreamEndCapture(s, &cg.graph);
+        cg.release();
+        throw;
+    }
+    CK(cudaStreamEndCapture(s, &cg.graph));
+    const cudaError_t e = cudaGraphInstantiate(&cg.exec, cg.graph, 0);
+    if (e != cudaSuccess) {
+        cg.release();
+        CK(e);
+    }
+    return cg;
+}
+
 // Device copy of one HostPlan plus its coefficient tables in both precisions.
 struct PlanDev {
     DevPlan view;

@@ -341,10 +341,11 @@ void jacobi_run(heom_ctx *c, const heom_solve_opts *o, double ejac, double _Comp
             constexpr int kChunk = 50;
             cudaGraph_t g = nullptr;
             cudaGraphExec_t ge = nullptr;
-            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < kChunk; k += 2) { sweep(x, xn); sweep(xn, x); }
-            CK(cudaStreamEndCapture(c->stream, &g));
-            CK(cudaGraphInstantiate(&ge, g, 0));
+            {
+                const CapturedGraph cg = capture_graph(c->stream, [&] { for (int k = 0; k < kChunk; k += 2) { sweep(x, xn); sweep(xn, x); } });
+                g = cg.graph;
+                ge = cg.exec;
+            }
             CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
             CK(cudaEventRecord(e0, c->stream));
             // iteration 0, then chunks of 50; the residual test follows iterations 0, 50, 100, ...

@@ -337,11 +337,14 @@ int heom_propagate(heom_ctx *c, int32_t method, double t0, double dt, int32_t ns
         if (nstep > 0) {
             cudaGraph_t g = nullptr;
             cudaGraphExec_t ge = nullptr;
-            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            if (method == HEOM_PROP_CHEBYSHEV_MIXED) enqueue_step_df(c, K.kdf, B, xdf, vdf, gdf, delta, bes, true);
-            else enqueue_step(c, method, K.k64, B, x, delta, bes, true);
-            CK(cudaStreamEndCapture(c->stream, &g));
-            CK(cudaGraphInstantiate(&ge, g, 0));
+            {
+                const CapturedGraph cg = capture_graph(c->stream, [&] {
+                    if (method == HEOM_PROP_CHEBYSHEV_MIXED) enqueue_step_df(c, K.kdf, B, xdf, vdf, gdf, delta, bes, true);
+                    else enqueue_step(c, method, K.k64, B, x, delta, bes, true);
+                });
+                g = cg.graph;
+                ge = cg.exec;
+            }
             cudaError_t err = cudaSuccess;
             for (int n = 0; n < nstep && err == cudaSuccess; n++) err = cudaGraphLaunch(ge, c->stream);
             cudaGraphExecDestroy(ge);

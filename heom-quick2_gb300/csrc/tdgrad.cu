@@ -236,11 +236,14 @@ void td_gradient_run(heom_ctx *c, double dt, int nstep, int ck, const double _Co
         {
             cudaGraph_t g = nullptr;
             cudaGraphExec_t ge = nullptr;
-            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            if constexpr (std::is_same<T, double>::value) enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, true);
-            else enqueue_step_df(c, Kf.kdf, B, x, xv, gdT, delta, bes, true);
-            CK(cudaStreamEndCapture(s, &g));
-            CK(cudaGraphInstantiate(&ge, g, 0));
+            {
+                const CapturedGraph cg = capture_graph(s, [&] {
+                    if constexpr (std::is_same<T, double>::value) enqueue_step(c, HEOM_PROP_CHEBYSHEV, Kf.k64, B, x, delta, bes, true);
+                    else enqueue_step_df(c, Kf.kdf, B, x, xv, gdT, delta, bes, true);
+                });
+                g = cg.graph;
+                ge = cg.exec;
+            }
             cudaError_t err = cudaSuccess;
             for (int n = 0; n < nstep && err == cudaSuccess; n++) {
                 if (n % ck == 0) err = cudaMemcpyAsync(cp(n / ck), x, vb, cudaMemcpyDeviceToDevice, s);
