@@ -198,11 +198,11 @@ typedef struct {
                                  choice of interleave and lane_instances: the context times its
                                  first mixed batch solves of each batch size (and kind: whole or
                                  truncated hierarchies) with each candidate layout -- none;
-                                 interleave 2 with two instances per lane (not for truncated
-                                 batches); g = the smallest power of two >= nbatch (at most 32)
-                                 with one and with two instances per lane -- and keeps the
-                                 fastest for that size (heom_tuned_layout); single solves use
-                                 none.  An interleaved group runs until all its instances have
+                                 interleave 2 with two instances per lane; g = the smallest
+                                 power of two >= nbatch (at most 32) with one and with two
+                                 instances per lane (truncated batches: none and g with one) --
+                                 and keeps the fastest for that size and kind
+                                 (heom_tuned_layout); single solves use none.  An interleaved group runs until all its instances have
                                  finished. */
     int32_t lane_instances;   /* MIXED with interleave >= 2: instances of a group served by one
                                  thread of the inner kernels, 1 (0 selects 1) or 2: two adjacent
