@@ -198,9 +198,10 @@ typedef struct {
                                  choice of interleave and lane_instances: the context times its
                                  first mixed batch solves of each batch size (and kind: whole or
                                  truncated hierarchies) with each candidate layout -- none;
-                                 interleave 2 with two instances per lane; g = the smallest
-                                 power of two >= nbatch (at most 32) with one and with two
-                                 instances per lane (truncated batches: none and g with one) --
+                                 interleave 2 with two instances per lane; when g = the
+                                 smallest power of two >= nbatch (at most 32) exceeds 2, g with
+                                 one and with two instances per lane (truncated batches: none
+                                 and g with one) --
                                  and keeps the fastest for that size and kind
                                  (heom_tuned_layout); single solves use none.  An interleaved group runs until all its instances have
                                  finished. */
