@@ -7,6 +7,7 @@
 // construction of the operators, hashed multiset lookups for the coupling tables
 // and a boolean structural propagation for the per-ADO sparsity.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -356,6 +357,42 @@ uint64_t pack(const int *v, int n) {   // <= 7 entries of < 2^9 (one map per tie
     for (int i = 0; i < n; i++) k = (k << 9) | (uint64_t)v[i];
     return k;
 }
+// Open-addressing map from a packed drawer tuple to its ADO index (linear probing; the packed
+// keys are below 2^63, so all ones marks an empty slot)
+struct TupleIndex {
+    std::vector<uint64_t> key;
+    std::vector<int64_t> val;
+    uint64_t mask = 0;
+    explicit TupleIndex(size_t n = 0)
+    {
+        size_t cap = 16;
+        while (cap < 2 * n) cap <<= 1;
+        key.assign(cap, ~0ull);
+        val.assign(cap, 0);
+        mask = cap - 1;
+    }
+    static uint64_t mix(uint64_t k)
+    {
+        k ^= k >> 33;
+        k *= 0xff51afd7ed558ccdull;
+        k ^= k >> 33;
+        return k;
+    }
+    void put(uint64_t k, int64_t v)
+    {
+        size_t i = mix(k) & mask;
+        while (key[i] != ~0ull && key[i] != k) i = (i + 1) & mask;
+        key[i] = k;
+        val[i] = v;
+    }
+    const int64_t *get(uint64_t k) const
+    {
+        for (size_t i = mix(k) & mask; key[i] != ~0ull; i = (i + 1) & mask)
+            if (key[i] == k) return &val[i];
+        return nullptr;
+    }
+};
+
 // parity of the exchange sort of the reference (swap whenever a[i] > a[j], i < j)
 int exchange_sort(int *a, int n) {
     int f = 1;
@@ -370,7 +407,7 @@ void build_tables(heom_model &m) {
     if (m.nvar >= 512) heom::fail(HEOM_E_UNSUPPORTED, "too many drawers for the table builder");
     m.nfirst.assign(T, 1); m.nlast.assign(T, 1); m.ifirst.assign(T, 1); m.ilast.assign(T, 1);
     m.indextable.assign(1, 0);
-    std::vector<std::unordered_map<uint64_t, int64_t>> lookup(T + 1);
+    std::vector<TupleIndex> lookup(T + 1);
     for (int it = 2; it <= T; it++) {
         int nb = it - 1;
         // operator multisets: nondecreasing tuples, keep one of each complement pair
@@ -410,35 +447,36 @@ void build_tables(heom_model &m) {
             }
         }
         int64_t cnt = (int64_t)rows.size() / nb;
-        std::vector<int64_t> idx(cnt);
-        for (int64_t r = 0; r < cnt; r++) idx[r] = r;
-        std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
-            return std::lexicographical_compare(&rows[a * nb], &rows[a * nb] + nb, &rows[b * nb], &rows[b * nb] + nb);
-        });
+        // lexicographic order of the tuples = numeric order of their packed keys (fixed width)
+        std::vector<std::pair<uint64_t, int64_t>> keyed(cnt);
+        for (int64_t r = 0; r < cnt; r++) keyed[r] = {pack(&rows[r * nb], nb), r};
+        std::sort(keyed.begin(), keyed.end());
         m.nfirst[it - 1] = m.nlast[it - 2] + 1;
         m.nlast[it - 1] = m.nlast[it - 2] + cnt;
         m.ifirst[it - 1] = m.ilast[it - 2] + 1;
         m.ilast[it - 1] = m.ilast[it - 2] + cnt * nb;
+        lookup[it] = TupleIndex((size_t)cnt);
+        m.indextable.reserve(m.indextable.size() + (size_t)(cnt * nb));
         for (int64_t r = 0; r < cnt; r++) {
-            const int *row = &rows[idx[r] * nb];
+            const int *row = &rows[keyed[r].second * nb];
             m.indextable.insert(m.indextable.end(), row, row + nb);
-            lookup[it][pack(row, nb)] = m.nfirst[it - 1] + r;
+            lookup[it].put(keyed[r].first, m.nfirst[it - 1] + r);
         }
     }
     m.nunk = m.nlast[T - 1];
     // couplings: lower tier entries, then higher tier in sgn > spin > orbs > alf > cor order
     m.index_coef_ref.assign(m.nunk, 0);
     auto find = [&](int tier, const int *rec, int n, int &fact, int &itype) -> int64_t {
-        auto &L = lookup[tier];
-        auto hit = L.find(pack(rec, n));
-        if (hit != L.end()) { fact = 1; itype = 0; return hit->second; }
+        const TupleIndex &L = lookup[tier];
+        const int64_t *hit = L.get(pack(rec, n));
+        if (hit) { fact = 1; itype = 0; return *hit; }
         int c[16];
         for (int i = 0; i < n; i++) c[i] = m.iredex[rec[n - 1 - i] - 1];
         fact = exchange_sort(c, n);
-        hit = L.find(pack(c, n));
-        if (hit == L.end()) heom::fail(HEOM_E_ARG, "coupling target not found");
+        hit = L.get(pack(c, n));
+        if (!hit) heom::fail(HEOM_E_ARG, "coupling target not found");
         itype = 1;
-        return hit->second;
+        return *hit;
     };
     int64_t lnl = 1;
     for (int it = 2; it <= T; it++) {
@@ -540,57 +578,92 @@ void propagate_pattern(const heom_model &m, const Bits &e, const Bits &seed, Pat
     std::vector<std::vector<int>> rofc(m.norbs * m.nspin), cofr(m.norbs * m.nspin);
     for (int s = 1; s <= m.nspin; s++)
         for (int o = 1; o <= m.norbs; o++) opmaps(o, s, rofc[(o - 1) + (s - 1) * m.norbs], cofr[(o - 1) + (s - 1) * m.norbs]);
-    // pattern bits of every ADO in one flat array; scratch sets reused across ADOs
+    // The patterns repeat: an ADO's pattern is the union of one contribution per lower-tier
+    // coupling, and a contribution depends only on the lower ADO's pattern, the operator, its
+    // dagger and the coupling's transpose flag.  So every distinct pattern is kept once (a
+    // class), every ADO holds its class, and every contribution is computed once.
     const size_t nw = ((size_t)n * n + 63) / 64;
-    std::vector<uint64_t> pat((size_t)m.nunk * nw, 0);
-    std::copy(seed.w.begin(), seed.w.end(), pat.begin());
+    using Words = std::vector<uint64_t>;
+    std::vector<Words> cls;
+    std::map<Words, int> cls_id;
+    auto class_of = [&](const Words &w) {
+        auto it = cls_id.find(w);
+        if (it != cls_id.end()) return it->second;
+        const int id = (int)cls.size();
+        cls.push_back(w);
+        cls_id.emplace(w, id);
+        return id;
+    };
     auto bit = [n](const uint64_t *w, int i, int j) { size_t k = (size_t)i + (size_t)j * n; return (w[k >> 6] >> (k & 63)) & 1; };
-    Bits acc(n), sl(n), sr(n);
+    // E0 (op(a)(i, r) X(r, c) + X(r, c) op(a)(c, j)) on the structure of X (X^T when tr)
+    std::map<std::array<int, 4>, Words> contrib;
+    Bits sl(n), sr(n), acc(n);
+    auto contribution = [&](int c, int oi, bool dag, bool tr) -> const Words & {
+        const std::array<int, 4> key = {c, oi, dag ? 1 : 0, tr ? 1 : 0};
+        auto hit = contrib.find(key);
+        if (hit != contrib.end()) return hit->second;
+        const uint64_t *low = cls[c].data();
+        const std::vector<int> &rc = rofc[oi], &cr = cofr[oi];
+        std::fill(sl.w.begin(), sl.w.end(), 0);
+        std::fill(sr.w.begin(), sr.w.end(), 0);
+        std::fill(acc.w.begin(), acc.w.end(), 0);
+        for (int cc = 0; cc < n; cc++)
+            for (int r = 0; r < n; r++) {
+                if (!(tr ? bit(low, cc, r) : bit(low, r, cc))) continue;
+                int i = dag ? cr[r + 1] : rc[r + 1];    // left:  op(a)(i, r)
+                if (i) sl.set(i - 1, cc);
+                int jj = dag ? rc[cc + 1] : cr[cc + 1];   // right: op(a)(c, jj)
+                if (jj) sr.set(r, jj - 1);
+            }
+        for (const Bits *src : {&sl, &sr})
+            for (int j = 0; j < n; j++)
+                for (int k = 0; k < n; k++)
+                    if (src->get(k, j))
+                        for (int i : ecol[k]) acc.set(i, j);
+        return contrib.emplace(key, acc.w).first->second;
+    };
+    std::vector<int> ado_cls((size_t)m.nunk, 0);
+    ado_cls[0] = class_of(seed.w);
+    const Words none(nw, 0);
+    Words w(nw);
     for (int it = 2; it <= m.ntier; it++) {
         int nb = it - 1;
         for (int64_t lni = m.nfirst[it - 1]; lni <= m.nlast[it - 1]; lni++) {
-            std::fill(acc.w.begin(), acc.w.end(), 0);
+            std::fill(w.begin(), w.end(), 0);
             bool empty = false;
             int64_t lnl = m.index_coef_ref[lni - 1];
             for (int b = 0; b < nb; b++, lnl++) {
                 int d = m.indextable[m.ifirst[it - 1] - 1 + (lni - m.nfirst[it - 1]) * nb + b];
                 int o = m.morbs[d - 1], s = m.mspin[d - 1], a = m.ilead[d - 1];
                 if (std::fabs(m.hybrid[(a - 1) * m.norbs + (o - 1)]) <= heom::kDsmall) { empty = true; continue; }
-                const uint64_t *low = &pat[(size_t)(m.indexcoef[lnl - 1] - 1) * nw];
-                bool tr = m.itypecoef[lnl - 1] != 0, dag = m.mpm[d - 1] == 1;
-                const std::vector<int> &rc = rofc[(o - 1) + (s - 1) * m.norbs], &cr = cofr[(o - 1) + (s - 1) * m.norbs];
-                std::fill(sl.w.begin(), sl.w.end(), 0);
-                std::fill(sr.w.begin(), sr.w.end(), 0);
-                for (int c = 0; c < n; c++)
-                    for (int r = 0; r < n; r++) {
-                        if (!(tr ? bit(low, c, r) : bit(low, r, c))) continue;
-                        int i = dag ? cr[r + 1] : rc[r + 1];    // left:  op(a)(i, r)
-                        if (i) sl.set(i - 1, c);
-                        int jj = dag ? rc[c + 1] : cr[c + 1];   // right: op(a)(c, jj)
-                        if (jj) sr.set(r, jj - 1);
-                    }
-                for (const Bits *src : {&sl, &sr})
-                    for (int j = 0; j < n; j++)
-                        for (int k = 0; k < n; k++)
-                            if (src->get(k, j))
-                                for (int i : ecol[k]) acc.set(i, j);
+                const Words &cw = contribution(ado_cls[(size_t)(m.indexcoef[lnl - 1] - 1)], (o - 1) + (s - 1) * m.norbs,
+                                               m.mpm[d - 1] == 1, m.itypecoef[lnl - 1] != 0);
+                for (size_t q = 0; q < nw; q++) w[q] |= cw[q];
             }
-            if (!empty) std::copy(acc.w.begin(), acc.w.end(), pat.begin() + (size_t)(lni - 1) * nw);
+            ado_cls[(size_t)(lni - 1)] = class_of(empty ? none : w);
         }
     }
+    // entries of every class in column-major order
+    std::vector<std::vector<int32_t>> crow(cls.size()), ccol(cls.size());
+    for (size_t c = 0; c < cls.size(); c++)
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++)
+                if (bit(cls[c].data(), i, j)) { crow[c].push_back(i + 1); ccol[c].push_back(j + 1); }
     out = PatternOut();
     out.nnz.assign(m.nunk, 0);
     out.ind.assign(m.nunk, 0);
+    int64_t total = 0;
+    for (int64_t u = 0; u < m.nunk; u++) total += (int64_t)crow[ado_cls[(size_t)u]].size();
+    out.irow.reserve((size_t)total);
+    out.icol.reserve((size_t)total);
     int64_t off = 1;
     for (int64_t u = 0; u < m.nunk; u++) {
+        const int c = ado_cls[(size_t)u];
         out.ind[u] = off;
-        int cnt = 0;
-        const uint64_t *pu = &pat[(size_t)u * nw];
-        for (int j = 0; j < n; j++)
-            for (int i = 0; i < n; i++)
-                if (bit(pu, i, j)) { out.irow.push_back(i + 1); out.icol.push_back(j + 1); cnt++; }
-        out.nnz[u] = cnt;
-        off += cnt;
+        out.nnz[u] = (int32_t)crow[c].size();
+        out.irow.insert(out.irow.end(), crow[c].begin(), crow[c].end());
+        out.icol.insert(out.icol.end(), ccol[c].begin(), ccol[c].end());
+        off += out.nnz[u];
     }
     out.lunk = off - 1;
 }
