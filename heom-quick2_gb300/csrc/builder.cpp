@@ -7,6 +7,9 @@
 // construction of the operators, hashed multiset lookups for the coupling tables
 // and a boolean structural propagation for the per-ADO sparsity.
 #include <algorithm>
+#include <exception>
+#include <mutex>
+#include <thread>
 #include <array>
 #include <cmath>
 #include <cstring>
@@ -478,12 +481,33 @@ void build_tables(heom_model &m) {
         itype = 1;
         return *hit;
     };
+    // Every ADO's couplings sit at offsets known in advance: its nb lower-tier entries, then,
+    // below the last tier, one entry per unscreened (sign, spin, orbital, lead, memory)
+    // drawer.  The entries are filled in parallel over the ADOs of each tier.
+    int nhigh = 0;
+    for (int iopr = 1; iopr <= 2 * m.nspin * m.norbs * m.nalf; iopr++)
+        if (!(m.p.lscreen && m.jomit[iopr - 1])) nhigh += ncor;
     int64_t lnl = 1;
-    for (int it = 2; it <= T; it++) {
-        int nb = it - 1;
+    for (int it = 2; it <= T; it++)
         for (int64_t lni = m.nfirst[it - 1]; lni <= m.nlast[it - 1]; lni++) {
             m.index_coef_ref[lni - 1] = lnl;
+            lnl += (it - 1) + (it < T ? nhigh : 0);
+        }
+    const size_t total = (size_t)(lnl - 1);
+    m.indexcoef.assign(total, 0);
+    m.itypecoef.assign(total, 0);
+    m.ifactfcoef.assign(total, 0);
+    m.ifactrcoef.assign(total, 0);
+    auto fill = [&](int it, int64_t l0, int64_t l1) {
+        const int nb = it - 1;
+        for (int64_t lni = l0; lni < l1; lni++) {
+            size_t q = (size_t)(m.index_coef_ref[lni - 1] - 1);
             const int *nk = &m.indextable[m.ifirst[it - 1] - 1 + (lni - m.nfirst[it - 1]) * nb];
+            auto put = [&](int64_t tgt, int itype, int ff, int fr) {
+                m.indexcoef[q] = tgt; m.itypecoef[q] = (int8_t)itype;
+                m.ifactfcoef[q] = (int8_t)ff; m.ifactrcoef[q] = (int8_t)fr;
+                q++;
+            };
             for (int ni = 1; ni <= nb; ni++) {
                 int64_t tgt = 1; int fact = 1, itype = 0;
                 if (it > 2) {
@@ -493,9 +517,7 @@ void build_tables(heom_model &m) {
                 }
                 int ff = (ni % 2 == 0) ? -1 : 1, fr = ((it - 1 - ni) % 2 == 0) ? 1 : -1;
                 if (itype) { ff *= fact; fr *= fact; }
-                m.indexcoef.push_back(tgt); m.itypecoef.push_back((int8_t)itype);
-                m.ifactfcoef.push_back((int8_t)ff); m.ifactrcoef.push_back((int8_t)fr);
-                lnl++;
+                put(tgt, itype, ff, fr);
             }
             if (it < T) {
                 for (int sg = 1; sg <= 2; sg++)
@@ -508,18 +530,32 @@ void build_tables(heom_model &m) {
                                     int plus = (iopr - 1) * ncor + k;
                                     int fr_[16], rr[16];
                                     fr_[0] = plus;
-                                    for (int q = 0; q < nb; q++) fr_[q + 1] = nk[q], rr[q] = nk[q];
+                                    for (int q2 = 0; q2 < nb; q2++) fr_[q2 + 1] = nk[q2], rr[q2] = nk[q2];
                                     rr[nb] = plus;
                                     int ffact = exchange_sort(fr_, it), rfact = exchange_sort(rr, it);
                                     int fact, itype;
                                     int64_t tgt = find(it + 1, rr, it, fact, itype);
-                                    m.indexcoef.push_back(tgt); m.itypecoef.push_back((int8_t)itype);
-                                    m.ifactfcoef.push_back((int8_t)(ffact * fact)); m.ifactrcoef.push_back((int8_t)(rfact * fact));
-                                    lnl++;
+                                    put(tgt, itype, ffact * fact, rfact * fact);
                                 }
                             }
             }
         }
+    };
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (int it = 2; it <= T; it++) {
+        const int64_t l0 = m.nfirst[it - 1], l1 = m.nlast[it - 1] + 1, cnt = l1 - l0;
+        const int64_t per = std::max<int64_t>(2048, (cnt + hw - 1) / hw);
+        if (cnt <= per) { fill(it, l0, l1); continue; }
+        std::vector<std::thread> pool;
+        std::vector<std::exception_ptr> errs;
+        std::mutex mu;
+        for (int64_t a = l0; a < l1; a += per)
+            pool.emplace_back([&, a] {
+                try { fill(it, a, std::min(l1, a + per)); }
+                catch (...) { std::lock_guard<std::mutex> g(mu); errs.push_back(std::current_exception()); }
+            });
+        for (auto &t : pool) t.join();
+        if (!errs.empty()) std::rethrow_exception(errs.front());
     }
     m.lall = (int64_t)m.indexcoef.size();
 }
